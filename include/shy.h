@@ -1,0 +1,194 @@
+/* shy.h -- C ABI of simplehydrology_gb300, the GB300 (sm_103a) erosion engine.
+ *
+ * The reference (weigert/SimpleHydrology) is header-only C++ with process-wide
+ * statics and no FFI.  Its erosion entry points are
+ *   World::erode(int cycles)          source/world.h:33, body :54-88
+ *   World::cascade(vec2 pos)          source/world.h:34, body :90-168
+ *   Drop::Drop(vec2) / Drop::descend  source/water.h:14,37, body :58-156
+ *   quad::map accessors               source/cellpool.h:413-447
+ *   Vegetation::grow()                source/vegetation.h:49, body :122-188
+ * This header replaces them with plain C entry points over an opaque world
+ * handle.  A world owns one terrain on one GPU, its device maps and one CUDA
+ * stream; calls on one world are not reentrant (the reference's
+ * World::cascade uses a function-static array and is not reentrant either).
+ * Every call returns SHY_OK or a negative status and never throws; the
+ * message of the last failure on the calling thread is in shy_last_error().
+ *
+ * Maps are x-major like the reference (math::flatten, source/include/math.h:
+ * 11-14): cell (x, y) of an nx-by-ny map is element x * ny + y.
+ */
+#ifndef SHY_H
+#define SHY_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SHY_ABI_VERSION 1
+
+typedef struct shy_world shy_world;
+
+/* status codes */
+#define SHY_OK 0
+#define SHY_ERR_INVALID_ARG (-1)
+#define SHY_ERR_OUT_OF_MEMORY (-2)
+#define SHY_ERR_CUDA (-3)
+#define SHY_ERR_NO_DEVICE (-4)
+#define SHY_ERR_TIMEOUT (-5)   /* a bounded device-side wait gave up */
+#define SHY_ERR_STATE (-6)     /* call not valid in the world's current state */
+
+/* Per-cell fields, in the order of quad::cell (source/cellpool.h:207-220). */
+#define SHY_FIELD_HEIGHT 0
+#define SHY_FIELD_DISCHARGE 1
+#define SHY_FIELD_MOMENTUM_X 2
+#define SHY_FIELD_MOMENTUM_Y 3
+#define SHY_FIELD_DISCHARGE_TRACK 4
+#define SHY_FIELD_MOMENTUM_X_TRACK 5
+#define SHY_FIELD_MOMENTUM_Y_TRACK 6
+#define SHY_FIELD_ROOT_DENSITY 7
+#define SHY_FIELD_PLANT_SIZE 8  /* per-cell vegetation (no reference field) */
+#define SHY_FIELD_COUNT 9
+
+/* Model parameters.  Defaults (shy_params_default) are the reference's
+ * static parameter values. */
+typedef struct shy_params {
+  /* struct Drop, source/water.h:43-50 */
+  float evap_rate;          /* Drop::evapRate          0.001 */
+  float deposition_rate;    /* Drop::depositionRate    0.1   */
+  float min_vol;            /* Drop::minVol            0.01  */
+  float max_age;            /* Drop::maxAge            500   */
+  float entrainment;        /* Drop::entrainment       10    */
+  float gravity;            /* Drop::gravity           1     */
+  float momentum_transfer;  /* Drop::momentumTransfer  1     */
+  /* class World, source/world.h:42-44 */
+  float lrate;              /* World::lrate            0.1   */
+  float max_diff;           /* World::maxdiff          0.01  */
+  float settling;           /* World::settling         0.8   */
+  /* namespace quad, source/cellpool.h:165 */
+  float map_scale;          /* quad::mapscale          80    */
+  /* struct Plant, source/vegetation.h:38-42 */
+  float plant_max_size;       /* Plant::maxSize        1.5  */
+  float plant_grow_rate;      /* Plant::growRate       0.05 */
+  float plant_max_steep;      /* Plant::maxSteep       0.8  */
+  float plant_max_discharge;  /* Plant::maxDischarge   0.3  */
+  float plant_max_height;     /* Plant::maxTreeHeight  0.8  */
+  /* per-cell vegetation rates: a plant dies with 1/1000 chance per step and
+   * spreads with 1/20 chance (source/vegetation.h:71,160); new plants appear
+   * with plant_spawn_prob per cell per step */
+  float plant_spawn_prob;     /* 1e-4  */
+  float plant_death_prob;     /* 0.001 */
+  float plant_spread_prob;    /* 0.05  */
+  /* Batched mode: World::cascade becomes a per-cycle stencil over the cells
+   * drops visited; each pass moves cascade_weight * settling * excess / 2
+   * across every steep pair (no reference counterpart). */
+  float cascade_weight;       /* 0.125 */
+  int cascade_passes;         /* 1     */
+  int reserved[7];
+} shy_params;
+
+/* Droplet state, struct Drop source/water.h:20-27. */
+typedef struct shy_drop {
+  int age;
+  float pos[2];
+  float speed[2];
+  float volume;
+  float sediment;
+} shy_drop;
+
+/* Counters accumulated on the device since creation or shy_world_reset_stats. */
+typedef struct shy_stats {
+  uint64_t cycles;         /* batched cycles run (shy_erode) */
+  uint64_t drops;          /* drops that started descending */
+  uint64_t drops_skipped;  /* spawns on cells below height 0.1 (world.h:71) */
+  uint64_t drops_oob;      /* drops that left the map, sediment lost (water.h:139-142) */
+  uint64_t drop_steps;     /* descend() calls that passed the termination checks */
+  double evap_gain;        /* sediment created by evaporation (water.h:135), sum */
+  double boundary_loss;    /* sediment carried off the map, sum */
+} shy_stats;
+
+/* Optional per-kernel timing (CUDA events on the world's stream). */
+#define SHY_KERNEL_DROPS 0    /* batched descend kernel */
+#define SHY_KERNEL_APPLY 1    /* height apply + lrate blend + record rebuild */
+#define SHY_KERNEL_CASCADE 2  /* cascade stencil */
+#define SHY_KERNEL_OTHER 3    /* everything else launched by the world */
+#define SHY_KERNEL_KINDS 4
+typedef struct shy_timing {
+  double ms[SHY_KERNEL_KINDS];
+  uint64_t launches[SHY_KERNEL_KINDS];
+  uint64_t steps_timed;    /* drop steps done by the timed drop launches */
+} shy_timing;
+
+/* ---- library ---------------------------------------------------------- */
+int shy_version(void);
+const char* shy_last_error(void);
+int shy_params_default(shy_params* out);
+
+/* ---- world lifecycle (replaces World::map, source/world.h:22,40, and the
+ *      cell pool, SimpleHydrology.cpp:11,36) --------------------------------- */
+int shy_world_create(int nx, int ny, const shy_params* params, uint64_t seed,
+                     shy_world** out);
+int shy_world_destroy(shy_world* w);
+int shy_world_set_params(shy_world* w, const shy_params* params);
+int shy_world_get_params(shy_world* w, shy_params* out);
+int shy_world_size(shy_world* w, int* nx, int* ny);
+/* Host <-> device copies of one field (count = nx * ny floats). */
+int shy_world_set_field(shy_world* w, int field, const float* host, size_t count);
+int shy_world_get_field(shy_world* w, int field, float* host, size_t count);
+int shy_world_sync(shy_world* w);
+/* The world's cudaStream_t, for callers that order their own work with it. */
+int shy_world_stream(shy_world* w, void** stream);
+int shy_world_stats(shy_world* w, shy_stats* out);
+int shy_world_reset_stats(shy_world* w);
+/* Batched-mode random stream position: the next shy_erode cycle uses this
+ * cycle index for its spawn positions. */
+int shy_world_set_cycle(shy_world* w, uint64_t cycle);
+int shy_world_enable_timing(shy_world* w, int on);
+int shy_world_timing(shy_world* w, shy_timing* out);
+
+/* ---- erosion ------------------------------------------------------------ */
+
+/* Batched erosion: `cycles` times World::erode(drops) (source/world.h:54-88)
+ * with all `drops` of a cycle descending concurrently, one GPU thread each.
+ * Within a cycle every drop reads the heights, discharge and momentum as they
+ * were at the start of the cycle; height changes and the three track maps are
+ * summed in 32.32 fixed point with integer atomics, so the result is the same
+ * bits for any thread schedule.  At the end of each cycle the heights are
+ * updated, the discharge/momentum maps take the lrate blend (world.h:81-86)
+ * and World::cascade runs as a stencil over the cells drops visited.
+ * Spawn positions come from a counter-based generator keyed by (seed, cycle,
+ * drop index). */
+int shy_erode(shy_world* w, int drops, int cycles);
+
+/* Exact erosion: one World::erode(n) call (source/world.h:54-88) with the
+ * reference's sequential semantics -- every drop sees all earlier edits and
+ * World::cascade runs after every step -- with the n spawn positions given
+ * (spawn_xy[2i], spawn_xy[2i+1]), in place of the reference's rand() draws.
+ * Runs on one GPU thread; meant for parity and small maps. */
+int shy_erode_exact(shy_world* w, const int32_t* spawn_xy, int n);
+
+/* One Drop::descend() call (source/water.h:58-156) on the world, live, with
+ * the drop state held by the caller.  *more receives descend()'s result. */
+int shy_drop_descend(shy_world* w, shy_drop* drop, int* more);
+
+/* Drop d(pos); while (d.descend()); (source/world.h:74-76), recording the
+ * state after every descend() call as 8 floats: returned, age, pos.x, pos.y,
+ * speed.x, speed.y, volume, sediment.  *n_records receives the number of
+ * descend() calls (records beyond max_records are not written). */
+int shy_drop_run(shy_world* w, float x, float y, float* trace, int max_records,
+                 int* n_records);
+
+/* World::cascade(pos), source/world.h:90-168, on the live heights. */
+int shy_cascade(shy_world* w, float x, float y);
+
+/* quad::map::normal (source/cellpool.h:182-204) of every cell, 3 floats per
+ * cell, x-major. */
+int shy_normals(shy_world* w, float* host_xyz, size_t count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SHY_H */

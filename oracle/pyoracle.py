@@ -1,0 +1,270 @@
+"""ctypes front end of the CPU oracle -- TEST INFRASTRUCTURE, not product code.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module.  It loads
+
+* liboracle.so        -- the restatement of the reference's erosion algorithm
+                         (hydro_oracle.cpp), and
+* _ref/libshyref.so   -- the reference's own erosion headers compiled
+                         unmodified (ref_harness.cpp), where it was built.
+
+Maps are numpy arrays of shape (nx, ny), x-major like the reference
+(math::flatten, source/include/math.h:11-14).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libshyref.so")
+
+ERF_LIBM = 0
+ERF_SHY = 1
+
+FIELDS = ("height", "discharge", "momentum_x", "momentum_y",
+          "discharge_track", "momentum_x_track", "momentum_y_track", "root_density")
+
+
+class Params(C.Structure):
+    """Mirror of shy_params (include/shy.h)."""
+    _fields_ = [
+        ("evap_rate", C.c_float), ("deposition_rate", C.c_float), ("min_vol", C.c_float),
+        ("max_age", C.c_float), ("entrainment", C.c_float), ("gravity", C.c_float),
+        ("momentum_transfer", C.c_float), ("lrate", C.c_float), ("max_diff", C.c_float),
+        ("settling", C.c_float), ("map_scale", C.c_float), ("plant_max_size", C.c_float),
+        ("plant_grow_rate", C.c_float), ("plant_max_steep", C.c_float),
+        ("plant_max_discharge", C.c_float), ("plant_max_height", C.c_float),
+        ("plant_spawn_prob", C.c_float), ("plant_death_prob", C.c_float),
+        ("plant_spread_prob", C.c_float), ("cascade_weight", C.c_float),
+        ("cascade_passes", C.c_int), ("reserved", C.c_int * 7),
+    ]
+
+
+class Drop(C.Structure):
+    """Mirror of shy_drop (include/shy.h)."""
+    _fields_ = [("age", C.c_int), ("pos", C.c_float * 2), ("speed", C.c_float * 2),
+                ("volume", C.c_float), ("sediment", C.c_float)]
+
+
+class Acc(C.Structure):
+    _fields_ = [("drops", C.c_uint64), ("skipped", C.c_uint64), ("oob", C.c_uint64),
+                ("steps", C.c_uint64), ("gain", C.c_double), ("loss", C.c_double),
+                ("gain_q", C.c_int64), ("loss_q", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class GridF32(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("f", C.POINTER(C.c_float) * 8)]
+
+
+class GridF64(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("f", C.POINTER(C.c_double) * 8)]
+
+
+def build(quiet: bool = True) -> None:
+    """Build liboracle.so (and the reference harness where the checkout exists)."""
+    out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    if not quiet:
+        print(out.stdout)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        P = C.POINTER
+        L.orc_params_default.argtypes = [P(Params)]
+        L.orc_erode_seq_f32.argtypes = [P(GridF32), P(Params), P(C.c_int32), C.c_int, C.c_int, P(Acc)]
+        L.orc_erode_seq_f64.argtypes = [P(GridF64), P(Params), P(C.c_int32), C.c_int, C.c_int, P(Acc)]
+        L.orc_drop_run_f32.argtypes = [P(GridF32), P(Params), C.c_float, C.c_float, P(C.c_float),
+                                       C.c_int, C.c_int, P(Acc)]
+        L.orc_drop_run_f64.argtypes = [P(GridF64), P(Params), C.c_double, C.c_double, P(C.c_float),
+                                       C.c_int, C.c_int, P(Acc)]
+        L.orc_drop_descend_f32.argtypes = [P(GridF32), P(Params), P(Drop), C.c_int, P(Acc)]
+        L.orc_cascade_f32.argtypes = [P(GridF32), P(Params), C.c_float, C.c_float]
+        L.orc_normals_f32.argtypes = [P(GridF32), P(Params), P(C.c_float)]
+        L.orc_rand_spawns.argtypes = [C.c_uint, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int32)]
+        L.orc_erode_batched_f32.argtypes = [P(GridF32), P(Params), C.c_uint64, C.c_uint64, C.c_int,
+                                            C.c_int, P(Acc)]
+        L.orc_value_noise.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_int, P(C.c_float)]
+        L.orc_erff_libm.argtypes = [C.c_float]
+        L.orc_erff_libm.restype = C.c_float
+        L.orc_erff_shy.argtypes = [C.c_float]
+        L.orc_erff_shy.restype = C.c_float
+        L.orc_erf_shy_d.argtypes = [C.c_double]
+        L.orc_erf_shy_d.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_PATH)
+
+
+def ref():
+    """The reference's erosion code, compiled unmodified (512 x 512 map)."""
+    global _ref
+    if _ref is None:
+        R = C.CDLL(REF_PATH)
+        P = C.POINTER
+        R.ref_init.argtypes = [C.c_uint]
+        R.ref_set_field.argtypes = [C.c_int, P(C.c_float)]
+        R.ref_get_field.argtypes = [C.c_int, P(C.c_float)]
+        R.ref_srand.argtypes = [C.c_uint]
+        R.ref_erode.argtypes = [C.c_int]
+        R.ref_cascade.argtypes = [C.c_float, C.c_float]
+        R.ref_normal.argtypes = [C.c_int, C.c_int, P(C.c_float)]
+        R.ref_descend_trace.argtypes = [C.c_float, C.c_float, P(C.c_float), C.c_int]
+        R.ref_veg_get.argtypes = [P(C.c_float), C.c_int]
+        R.ref_init(1)
+        _ref = R
+    return _ref
+
+
+def fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def ipptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def default_params() -> Params:
+    p = Params()
+    lib().orc_params_default(C.byref(p))
+    return p
+
+
+class Maps:
+    """The eight quad::cell fields (source/cellpool.h:207-220) as (nx, ny) arrays."""
+
+    def __init__(self, nx, ny, dtype=np.float32, height=None):
+        self.nx, self.ny = nx, ny
+        self.dtype = np.dtype(dtype)
+        self.f = [np.zeros((nx, ny), dtype=self.dtype) for _ in range(8)]
+        if height is not None:
+            self.f[0][...] = height
+
+    def copy(self, dtype=None):
+        m = Maps(self.nx, self.ny, dtype or self.dtype)
+        for i in range(8):
+            m.f[i][...] = self.f[i]
+        return m
+
+    def __getattr__(self, name):
+        if name in FIELDS:
+            return self.f[FIELDS.index(name)]
+        raise AttributeError(name)
+
+    def grid(self):
+        if self.dtype == np.float32:
+            g = GridF32()
+            g.nx, g.ny = self.nx, self.ny
+            for i in range(8):
+                assert self.f[i].flags.c_contiguous
+                g.f[i] = fptr(self.f[i])
+        else:
+            g = GridF64()
+            g.nx, g.ny = self.nx, self.ny
+            for i in range(8):
+                g.f[i] = dptr(self.f[i])
+        return g
+
+
+def value_noise(nx, ny, seed, octaves=8):
+    out = np.empty((nx, ny), np.float32)
+    lib().orc_value_noise(nx, ny, seed, octaves, fptr(out))
+    return out
+
+
+def erode_seq(maps: Maps, spawns, params=None, erf_mode=ERF_LIBM):
+    """World::erode(len(spawns)) with the given spawn cells, in place."""
+    params = params or default_params()
+    sp = np.ascontiguousarray(np.asarray(spawns, np.int32).reshape(-1, 2))
+    acc = Acc()
+    g = maps.grid()
+    fn = lib().orc_erode_seq_f32 if maps.dtype == np.float32 else lib().orc_erode_seq_f64
+    fn(C.byref(g), C.byref(params), ipptr(sp), len(sp), erf_mode, C.byref(acc))
+    return acc
+
+
+def drop_run(maps: Maps, x, y, params=None, erf_mode=ERF_LIBM, max_records=1024):
+    """Drop d(pos); while (d.descend()); -> (trace[n, 8], Acc)."""
+    params = params or default_params()
+    tr = np.zeros((max_records, 8), np.float32)
+    acc = Acc()
+    g = maps.grid()
+    fn = lib().orc_drop_run_f32 if maps.dtype == np.float32 else lib().orc_drop_run_f64
+    n = fn(C.byref(g), C.byref(params), x, y, fptr(tr), max_records, erf_mode, C.byref(acc))
+    return tr[:min(n, max_records)].copy(), acc
+
+
+def cascade(maps: Maps, x, y, params=None):
+    params = params or default_params()
+    g = maps.grid()
+    lib().orc_cascade_f32(C.byref(g), C.byref(params), x, y)
+
+
+def normals(maps: Maps, params=None):
+    params = params or default_params()
+    out = np.zeros((maps.nx, maps.ny, 3), np.float32)
+    g = maps.grid()
+    lib().orc_normals_f32(C.byref(g), C.byref(params), fptr(out))
+    return out
+
+
+def rand_spawns(seed, n, nx, ny, order):
+    out = np.zeros((n, 2), np.int32)
+    lib().orc_rand_spawns(seed, n, nx, ny, order, ipptr(out))
+    return out
+
+
+def erode_batched(maps: Maps, seed, cycle0, drops, cycles, params=None):
+    params = params or default_params()
+    acc = Acc()
+    g = maps.grid()
+    lib().orc_erode_batched_f32(C.byref(g), C.byref(params), seed, cycle0, drops, cycles,
+                                C.byref(acc))
+    return acc
+
+
+# ---- the compiled reference (512 x 512) -----------------------------------
+
+def ref_set_maps(maps: Maps):
+    R = ref()
+    for i in range(8):
+        a = np.ascontiguousarray(maps.f[i], dtype=np.float32)
+        R.ref_set_field(i, fptr(a))
+
+
+def ref_get_maps(nx=512, ny=512) -> Maps:
+    R = ref()
+    m = Maps(nx, ny)
+    for i in range(8):
+        R.ref_get_field(i, fptr(m.f[i]))
+    return m
+
+
+def ref_drop_run(x, y, max_records=1024):
+    tr = np.zeros((max_records, 8), np.float32)
+    n = ref().ref_descend_trace(x, y, fptr(tr), max_records)
+    return tr[:min(n, max_records)].copy()
