@@ -1,0 +1,351 @@
+"""Benchmark of the erosion hot path: drop-steps/s on one GB300.
+
+Workload (the plain-method GPU configuration): a 1024 x 1024 fp32 heightmap
+of seeded fractal value noise (8 octaves, lacunarity 2, gain 0.5, normalised
+to [0, 1], seed 2), 65,536 drops per cycle with uniform random spawns, the
+reference's default Drop/World parameters, 32.32 fixed-point integer-atomic
+scatter, lrate blend and cascade.  One step = one erosion cycle
+(World::erode(65536), source/world.h:54-88).  Synthetic data: there is no
+dataset; the terrain recipe stands in for the reference's FastNoiseLite map.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is device throughput with the maps resident in HBM; between timed
+steps the L2 is flushed by writing a 256 MiB buffer (untimed).  `e2e` is the
+same metric through the C ABI with the world state (height, discharge,
+momentum) copied in from pinned host memory and back out every step.  The
+reference arm runs the reference's sequential erosion on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX = NY = 1024
+DROPS = 65536
+SEED = 2
+METRIC = "drop-steps/s"
+WORKLOAD = "plain method, GPU batched: 1024x1024 value-noise terrain, 65536 drops/cycle"
+# algorithmic bytes: 72 B per drop-step (5 own-cell f32 fields, 4 neighbour
+# heights and h2 = 40 B read; height delta and 3 tracks = 32 B of scatter) and
+# 80 B per cell per cycle (tracks read + reset, 3 fields read + write, height)
+BYTES_PER_STEP = 72
+BYTES_PER_CELL_CYCLE = 80
+FALLBACK_HBM_GBS = 6800.0
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the lock-step kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "lockstep_kernel_1024.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (200 ms period)."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(n_gpus):
+    if n_gpus <= 1 or "RANK" not in os.environ:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank, world = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world, dist
+
+
+def cpu_baseline_sample(seconds=10.0):
+    """The oracle's restatement of the reference's sequential World::erode
+    (pinned bit for bit against the reference) timed on one host core on a
+    bounded sample of the workload: 1024^2 terrain, drops in batches of 512."""
+    import numpy as np
+    from oracle import pyoracle as po
+    po.build()
+    H = po.value_noise(NX, NY, SEED)
+    m = po.Maps(NX, NY, height=H)
+    rng = np.random.default_rng(SEED)
+    steps = drops = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        sp = np.stack([rng.integers(0, NX, 512), rng.integers(0, NY, 512)], 1)
+        a = po.erode_seq(m, sp)
+        steps += a.steps
+        drops += 512
+    dt = time.perf_counter() - t0
+    return {"value": steps / dt, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": f"{drops} drops of World::erode on the 1024^2 terrain ({steps} drop-steps, {dt:.1f} s, 1 thread)"}
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import simplehydrology_gb300 as shy
+    from simplehydrology_gb300 import build as shybuild
+
+    shybuild.build()
+    rank, world_size, dist = dist_setup(args.gpus)
+    dev = torch.cuda.current_device()
+
+    w = shy.World(NX, NY, seed=SEED)
+    w.generate(SEED, 8)
+    h0 = w.get_field("height")
+    zero = np.zeros_like(h0)
+
+    def reset():
+        w.set_field("height", h0)
+        for f in ("discharge", "momentum_x", "momentum_y"):
+            w.set_field(f, zero)
+        w.set_cycle(0)
+
+    # warm-up on the same workload, then restart from the initial terrain
+    for _ in range(args.warmup):
+        w.erode(DROPS)
+    reset()
+    w.reset_stats()
+
+    stream = torch.cuda.ExternalStream(w.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stops = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    w.enable_timing(True)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    with ClockSampler(dev) as clk:
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)        # untimed L2 flush
+                starts[k].record(stream)
+            w.erode(DROPS)
+            with torch.cuda.stream(stream):
+                stops[k].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, stops)]
+    dev_s = sum(step_ms) / 1e3
+    st = w.stats()
+    tm = w.timing()
+    w.enable_timing(False)
+    steps_total = st.drop_steps
+    if dist:
+        t = torch.tensor([dev_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t.item())
+        s = torch.tensor([float(steps_total)], dtype=torch.float64, device=dev)
+        dist.all_reduce(s)
+        steps_all = float(s.item())
+    else:
+        steps_all = float(steps_total)
+    value = steps_all / dev_s
+
+    # roofline of the dominant kernel (the lock-step drops kernel)
+    n_launch = max(1, tm.launches[0])
+    avg_ms = tm.ms[0] / n_launch
+    bytes_per_launch = BYTES_PER_STEP * steps_total / n_launch
+    achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = profiled_traffic()
+
+    # end to end through the C ABI with pinned host buffers
+    fields = ("height", "discharge", "momentum_x", "momentum_y")
+    host = {f: torch.empty((NX, NY), dtype=torch.float32, pin_memory=True).numpy() for f in fields}
+    host["height"][...] = h0
+    for f in fields[1:]:
+        host[f][...] = 0.0
+    reset()
+    w.reset_stats()
+    e2e_steps = min(args.steps, 50)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        for f in fields:
+            w.set_field(f, host[f])
+        w.erode(DROPS)
+        for f in fields:
+            w.get_field(f, out=host[f])
+    e2e_s = time.perf_counter() - t0
+    e2e_value = w.stats().drop_steps * world_size / e2e_s
+    nbytes = NX * NY * 4 * len(fields)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world_size,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded value-noise terrain, counter-based spawns)",
+        "config": {"workload": WORKLOAD, "map": [NX, NY], "drops_per_cycle": DROPS,
+                   "step": "one erosion cycle", "l2": "flushed between steps (256 MiB write, untimed)",
+                   "parallelism": f"replicas x{world_size}" if world_size > 1 else "single GPU"},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "steps": e2e_steps},
+        "gpu_launches": int(sum(tm.launches)),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "lockstep_kernel", "avg_launch_ms": avg_ms,
+                     "algorithmic_bytes_per_launch": bytes_per_launch},
+        "kernel_ms": {"drops": tm.ms[0], "cycle_end": tm.ms[1], "relax": tm.ms[2]},
+        "drop_steps": steps_total, "wall_s": wall,
+    }
+    out["clocks"] = clk.summary()
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
+def _ref_worker(args):
+    """One host core: the oracle's sequential World::erode on `n` drops per step."""
+    idx, steps, warmup, n = args
+    import numpy as np
+    from oracle import pyoracle as po
+    H = po.value_noise(NX, NY, SEED)
+    m = po.Maps(NX, NY, height=H)
+    rng = np.random.default_rng(1000 + idx)
+    out = []
+    for k in range(warmup + steps):
+        sp = np.stack([rng.integers(0, NX, n), rng.integers(0, NY, n)], 1)
+        t0 = time.perf_counter()
+        a = po.erode_seq(m, sp)
+        out.append((time.perf_counter() - t0, a.steps))
+    return out[warmup:]
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    from oracle import pyoracle as po
+    po.build()
+    cores = os.cpu_count() or 1
+    per = max(1, 4096 // cores)  # 4096 drops per step across all cores
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(_ref_worker, [(i, args.steps, args.warmup, per) for i in range(cores)])
+        wall = time.perf_counter() - t0
+    steps = sum(s for r in res for _, s in r)
+    busy = max(sum(t for t, _ in r) for r in res)
+    value = steps / busy
+    sample = (f"{args.steps} steps of {per} drops x {cores} host processes of the sequential "
+              f"World::erode restatement (bit-exact with the reference) on the 1024^2 terrain")
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": busy * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded value-noise terrain)",
+        "config": {"workload": WORKLOAD, "map": [NX, NY], "drops_per_step": per * cores,
+                   "step": "a bounded sample of one erosion cycle"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -81,11 +81,13 @@ typedef struct shy_params {
   float plant_spawn_prob;     /* 1e-4  */
   float plant_death_prob;     /* 0.001 */
   float plant_spread_prob;    /* 0.05  */
-  /* Batched mode: World::cascade becomes a per-cycle stencil over the cells
-   * drops visited; each pass moves cascade_weight * settling * excess / 2
-   * across every steep pair (no reference counterpart). */
+  /* Batched mode, optional extra slope relaxation at the end of each cycle:
+   * cascade_passes passes of World::cascade's transfer rule as a symmetric
+   * stencil over neighbour pairs next to visited cells, each pass moving
+   * cascade_weight * settling * excess / 2 (no reference counterpart; the
+   * reference's own per-step cascade always runs). */
   float cascade_weight;       /* 0.125 */
-  int cascade_passes;         /* 1     */
+  int cascade_passes;         /* 0     */
   int reserved[7];
 } shy_params;
 
@@ -148,18 +150,31 @@ int shy_world_set_cycle(shy_world* w, uint64_t cycle);
 int shy_world_enable_timing(shy_world* w, int on);
 int shy_world_timing(shy_world* w, shy_timing* out);
 
+/* Source of erf(0.4 * discharge) (source/cellpool.h:242-244) for the exact
+ * mode.  SHY_ERF_DEVICE (default) is the library's own erf, evaluated on the
+ * GPU and correctly rounded to float.  SHY_ERF_HOST_LIBM evaluates the host C
+ * library's erff once per cell whenever the discharge map changed -- what a
+ * reference build on the same host calls, so that the exact mode reproduces
+ * that build bit for bit.  The batched mode always uses SHY_ERF_DEVICE. */
+#define SHY_ERF_DEVICE 0
+#define SHY_ERF_HOST_LIBM 1
+int shy_world_set_erf_source(shy_world* w, int source);
+
 /* ---- erosion ------------------------------------------------------------ */
 
 /* Batched erosion: `cycles` times World::erode(drops) (source/world.h:54-88)
- * with all `drops` of a cycle descending concurrently, one GPU thread each.
- * Within a cycle every drop reads the heights, discharge and momentum as they
- * were at the start of the cycle; height changes and the three track maps are
- * summed in 32.32 fixed point with integer atomics, so the result is the same
- * bits for any thread schedule.  At the end of each cycle the heights are
- * updated, the discharge/momentum maps take the lrate blend (world.h:81-86)
- * and World::cascade runs as a stencil over the cells drops visited.
- * Spawn positions come from a counter-based generator keyed by (seed, cycle,
- * drop index). */
+ * with all `drops` of a cycle descending at once, one GPU thread slot each,
+ * in lock step.  In step t every live drop takes one Drop::descend step
+ * against the heights left by step t-1; World::cascade then runs once at
+ * every cell a drop moved to; then all height changes apply.  Drops sharing a
+ * cell share its sediment exchange (each uses depositionRate / n, so a cell
+ * gets one drop's worth of exchange per step; n = 1 is the reference).
+ * Height changes and the three track maps are summed in 32.32 fixed point
+ * with integer atomics, so the result is the same bits for any thread
+ * schedule.  Discharge and momentum stay fixed during a cycle, as in the
+ * reference, and take the lrate blend (world.h:81-86) at its end.  Spawn
+ * positions come from a counter-based generator keyed by (seed, cycle, drop
+ * index); spawns on cells below height 0.1 are skipped (world.h:71). */
 int shy_erode(shy_world* w, int drops, int cycles);
 
 /* Exact erosion: one World::erode(n) call (source/world.h:54-88) with the
@@ -186,6 +201,27 @@ int shy_cascade(shy_world* w, float x, float y);
 /* quad::map::normal (source/cellpool.h:182-204) of every cell, 3 floats per
  * cell, x-major. */
 int shy_normals(shy_world* w, float* host_xyz, size_t count);
+
+/* ---- batches of terrains ---------------------------------------------------
+ * A world created by shy_batch_create holds n independent terrains of their
+ * own sizes, seeds and drops per cycle, packed into one set of device maps;
+ * shy_batch_erode runs every terrain's cycle in the same lock-step launch.
+ * The single-terrain calls above act on terrain 0. */
+int shy_batch_create(int n_terrains, const int* nx, const int* ny, const int* drops_per_cycle,
+                     const uint64_t* seeds, const shy_params* params, shy_world** out);
+int shy_batch_erode(shy_world* w, int cycles);
+int shy_batch_size(shy_world* w, int* n_terrains);
+int shy_terrain_size(shy_world* w, int terrain, int* nx, int* ny, int* drops_per_cycle);
+int shy_terrain_set_field(shy_world* w, int terrain, int field, const float* host, size_t count);
+int shy_terrain_get_field(shy_world* w, int terrain, int field, float* host, size_t count);
+int shy_terrain_erode_exact(shy_world* w, int terrain, const int32_t* spawn_xy, int n);
+
+/* Terrain input: fill a terrain's heights with seeded fractal value noise
+ * (`octaves` octaves, lacunarity 2, gain 0.5, base frequency 4 per longer
+ * side) min-max normalised to [0, 1], generated on the device.  Replaces the
+ * reference's FastNoiseLite initialisation (source/cellpool.h:323-411) with
+ * the workloads' recipe; the normalisation is the reference's (:382-409). */
+int shy_terrain_generate(shy_world* w, int terrain, uint64_t seed, int octaves);
 
 #ifdef __cplusplus
 }

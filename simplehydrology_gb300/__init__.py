@@ -1,0 +1,236 @@
+"""simplehydrology_gb300 -- the SimpleHydrology erosion path on one GB300 GPU.
+
+The engine is libshy.so (CUDA, sm_103a) behind the C ABI in include/shy.h.
+This module mirrors the reference's erosion interface on top of it:
+
+  World(nx, ny).erode(cycles)   World::erode(int cycles)      source/world.h:54-88
+  World.erode_exact(spawns)     World::erode with given spawns, sequential
+  World.cascade(pos)            World::cascade(vec2)           source/world.h:90-168
+  Drop(world, pos).descend()    Drop::descend()                source/water.h:58-156
+  World.height/discharge/normal quad::map accessors            source/cellpool.h:413-447
+
+Arrays are numpy float32 of shape (nx, ny), x-major like the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import (ERF_DEVICE, ERF_HOST_LIBM, FIELD_NAMES, DropState, Params, ShyError, Stats,
+                    Timing, check, default_params, lib)
+
+__all__ = ["World", "Batch", "Drop", "Params", "Stats", "Timing", "ShyError", "default_params",
+           "lib", "ERF_DEVICE", "ERF_HOST_LIBM", "FIELD_NAMES"]
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _field_index(field):
+    if isinstance(field, str):
+        return FIELD_NAMES.index(field)
+    return int(field)
+
+
+class _Handle:
+    def __init__(self):
+        self._w = C.c_void_p()
+
+    def close(self):
+        if self._w:
+            lib().shy_world_destroy(self._w)
+            self._w = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # counters and timing
+    def stats(self) -> Stats:
+        s = Stats()
+        check(lib().shy_world_stats(self._w, C.byref(s)))
+        return s
+
+    def reset_stats(self):
+        check(lib().shy_world_reset_stats(self._w))
+
+    def enable_timing(self, on=True):
+        check(lib().shy_world_enable_timing(self._w, 1 if on else 0))
+
+    def timing(self) -> Timing:
+        t = Timing()
+        check(lib().shy_world_timing(self._w, C.byref(t)))
+        return t
+
+    def set_cycle(self, cycle: int):
+        check(lib().shy_world_set_cycle(self._w, cycle))
+
+    def sync(self):
+        check(lib().shy_world_sync(self._w))
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(lib().shy_world_stream(self._w, C.byref(s)))
+        return s.value or 0
+
+    @property
+    def params(self) -> Params:
+        p = Params()
+        check(lib().shy_world_get_params(self._w, C.byref(p)))
+        return p
+
+    @params.setter
+    def params(self, p: Params):
+        check(lib().shy_world_set_params(self._w, C.byref(p)))
+
+
+class World(_Handle):
+    """One terrain: the reference's class World (source/world.h:17-36)."""
+
+    def __init__(self, nx: int, ny: int, params: Params | None = None, seed: int = 1):
+        super().__init__()
+        p = C.byref(params) if params is not None else None
+        check(lib().shy_world_create(nx, ny, p, seed, C.byref(self._w)))
+        self.nx, self.ny = nx, ny
+
+    # ---- fields ----
+    def set_field(self, field, values):
+        a = np.ascontiguousarray(values, dtype=np.float32).reshape(self.nx, self.ny)
+        check(lib().shy_world_set_field(self._w, _field_index(field), _fptr(a), a.size))
+
+    def get_field(self, field, out=None):
+        if out is None:
+            out = np.empty((self.nx, self.ny), np.float32)
+        check(lib().shy_world_get_field(self._w, _field_index(field), _fptr(out), out.size))
+        return out
+
+    def generate(self, seed: int, octaves: int = 8):
+        """Seeded fractal value-noise heights, normalised to [0, 1], on the GPU."""
+        check(lib().shy_terrain_generate(self._w, 0, seed, octaves))
+
+    def set_erf_source(self, source: int):
+        check(lib().shy_world_set_erf_source(self._w, source))
+
+    # ---- erosion (source/world.h:54-168, source/water.h:58-156) ----
+    def erode(self, cycles: int, repeat: int = 1):
+        """World::erode(cycles): `cycles` drops, batched, `repeat` times."""
+        check(lib().shy_erode(self._w, cycles, repeat))
+
+    def erode_exact(self, spawns):
+        sp = np.ascontiguousarray(np.asarray(spawns, np.int32).reshape(-1, 2))
+        check(lib().shy_erode_exact(self._w, sp.ctypes.data_as(C.POINTER(C.c_int32)), len(sp)))
+
+    def cascade(self, pos):
+        check(lib().shy_cascade(self._w, float(pos[0]), float(pos[1])))
+
+    def drop_run(self, x, y, max_records=1024):
+        tr = np.zeros((max_records, 8), np.float32)
+        n = C.c_int()
+        check(lib().shy_drop_run(self._w, float(x), float(y), _fptr(tr), max_records, C.byref(n)))
+        return tr[:min(n.value, max_records)].copy()
+
+    def normals(self):
+        out = np.empty((self.nx, self.ny, 3), np.float32)
+        check(lib().shy_normals(self._w, _fptr(out), out.size))
+        return out
+
+    # ---- quad::map accessors (source/cellpool.h:413-447), from a host copy ----
+    def oob(self, p):
+        x, y = int(p[0]), int(p[1])
+        return x < 0 or y < 0 or x >= self.nx or y >= self.ny
+
+    def height(self, p):
+        if self.oob(p):
+            return 0.0
+        return float(self.get_field("height")[int(p[0]), int(p[1])])
+
+    def discharge(self, p):
+        """erf(0.4 * discharge) (source/cellpool.h:242-244, 439-443)."""
+        if self.oob(p):
+            return 0.0
+        from math import erf
+        return erf(0.4 * float(self.get_field("discharge")[int(p[0]), int(p[1])]))
+
+
+class Drop:
+    """struct Drop (source/water.h:12-39) descending on a World."""
+
+    def __init__(self, world: World, pos):
+        self.world = world
+        self.state = DropState()
+        self.state.age = 0
+        self.state.pos[0], self.state.pos[1] = float(pos[0]), float(pos[1])
+        self.state.speed[0] = self.state.speed[1] = 0.0
+        self.state.volume = 1.0
+        self.state.sediment = 0.0
+
+    def descend(self) -> bool:
+        more = C.c_int()
+        check(lib().shy_drop_descend(self.world._w, C.byref(self.state), C.byref(more)))
+        return bool(more.value)
+
+    @property
+    def pos(self):
+        return (self.state.pos[0], self.state.pos[1])
+
+    @property
+    def speed(self):
+        return (self.state.speed[0], self.state.speed[1])
+
+    @property
+    def volume(self):
+        return self.state.volume
+
+    @property
+    def sediment(self):
+        return self.state.sediment
+
+    @property
+    def age(self):
+        return self.state.age
+
+
+class Batch(_Handle):
+    """Many independent terrains eroded in one lock-step launch per cycle."""
+
+    def __init__(self, sizes, drops_per_cycle, seeds, params: Params | None = None):
+        super().__init__()
+        n = len(sizes)
+        nx = (C.c_int * n)(*[int(s[0]) for s in sizes])
+        ny = (C.c_int * n)(*[int(s[1]) for s in sizes])
+        dr = (C.c_int * n)(*[int(d) for d in drops_per_cycle])
+        sd = (C.c_uint64 * n)(*[int(s) for s in seeds])
+        p = C.byref(params) if params is not None else None
+        check(lib().shy_batch_create(n, nx, ny, dr, sd, p, C.byref(self._w)))
+        self.sizes = [(int(s[0]), int(s[1])) for s in sizes]
+
+    def __len__(self):
+        return len(self.sizes)
+
+    def set_field(self, t, field, values):
+        nx, ny = self.sizes[t]
+        a = np.ascontiguousarray(values, dtype=np.float32).reshape(nx, ny)
+        check(lib().shy_terrain_set_field(self._w, t, _field_index(field), _fptr(a), a.size))
+
+    def get_field(self, t, field):
+        nx, ny = self.sizes[t]
+        out = np.empty((nx, ny), np.float32)
+        check(lib().shy_terrain_get_field(self._w, t, _field_index(field), _fptr(out), out.size))
+        return out
+
+    def generate(self, t, seed: int, octaves: int = 8):
+        check(lib().shy_terrain_generate(self._w, t, seed, octaves))
+
+    def erode(self, cycles: int = 1):
+        check(lib().shy_batch_erode(self._w, cycles))

@@ -1,0 +1,149 @@
+"""ctypes declarations of the C ABI in include/shy.h.
+
+The library is loaded from this package directory (built in place by
+simplehydrology_gb300/build.py).  There is no fallback: if libshy.so is
+missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libshy.so")
+
+SHY_OK = 0
+SHY_ERR_INVALID_ARG = -1
+SHY_ERR_OUT_OF_MEMORY = -2
+SHY_ERR_CUDA = -3
+SHY_ERR_NO_DEVICE = -4
+SHY_ERR_TIMEOUT = -5
+SHY_ERR_STATE = -6
+
+FIELD_HEIGHT = 0
+FIELD_DISCHARGE = 1
+FIELD_MOMENTUM_X = 2
+FIELD_MOMENTUM_Y = 3
+FIELD_DISCHARGE_TRACK = 4
+FIELD_MOMENTUM_X_TRACK = 5
+FIELD_MOMENTUM_Y_TRACK = 6
+FIELD_ROOT_DENSITY = 7
+FIELD_PLANT_SIZE = 8
+FIELD_COUNT = 9
+FIELD_NAMES = ("height", "discharge", "momentum_x", "momentum_y", "discharge_track",
+               "momentum_x_track", "momentum_y_track", "root_density", "plant_size")
+
+KERNEL_DROPS, KERNEL_APPLY, KERNEL_CASCADE, KERNEL_OTHER = 0, 1, 2, 3
+
+ERF_DEVICE = 0
+ERF_HOST_LIBM = 1
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("evap_rate", C.c_float), ("deposition_rate", C.c_float), ("min_vol", C.c_float),
+        ("max_age", C.c_float), ("entrainment", C.c_float), ("gravity", C.c_float),
+        ("momentum_transfer", C.c_float), ("lrate", C.c_float), ("max_diff", C.c_float),
+        ("settling", C.c_float), ("map_scale", C.c_float), ("plant_max_size", C.c_float),
+        ("plant_grow_rate", C.c_float), ("plant_max_steep", C.c_float),
+        ("plant_max_discharge", C.c_float), ("plant_max_height", C.c_float),
+        ("plant_spawn_prob", C.c_float), ("plant_death_prob", C.c_float),
+        ("plant_spread_prob", C.c_float), ("cascade_weight", C.c_float),
+        ("cascade_passes", C.c_int), ("reserved", C.c_int * 7),
+    ]
+
+
+class DropState(C.Structure):
+    _fields_ = [("age", C.c_int), ("pos", C.c_float * 2), ("speed", C.c_float * 2),
+                ("volume", C.c_float), ("sediment", C.c_float)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("cycles", C.c_uint64), ("drops", C.c_uint64), ("drops_skipped", C.c_uint64),
+                ("drops_oob", C.c_uint64), ("drop_steps", C.c_uint64), ("evap_gain", C.c_double),
+                ("boundary_loss", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Timing(C.Structure):
+    _fields_ = [("ms", C.c_double * 4), ("launches", C.c_uint64 * 4), ("steps_timed", C.c_uint64)]
+
+
+class ShyError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"shy error {code}: {msg}")
+        self.code = code
+
+
+W = C.c_void_p
+P = C.POINTER
+FP = P(C.c_float)
+
+# name -> (restype, argtypes); every entry point of include/shy.h
+SIGNATURES = {
+    "shy_version": (C.c_int, []),
+    "shy_last_error": (C.c_char_p, []),
+    "shy_params_default": (C.c_int, [P(Params)]),
+    "shy_world_create": (C.c_int, [C.c_int, C.c_int, P(Params), C.c_uint64, P(W)]),
+    "shy_world_destroy": (C.c_int, [W]),
+    "shy_world_set_params": (C.c_int, [W, P(Params)]),
+    "shy_world_get_params": (C.c_int, [W, P(Params)]),
+    "shy_world_size": (C.c_int, [W, P(C.c_int), P(C.c_int)]),
+    "shy_world_set_field": (C.c_int, [W, C.c_int, FP, C.c_size_t]),
+    "shy_world_get_field": (C.c_int, [W, C.c_int, FP, C.c_size_t]),
+    "shy_world_sync": (C.c_int, [W]),
+    "shy_world_stream": (C.c_int, [W, P(C.c_void_p)]),
+    "shy_world_stats": (C.c_int, [W, P(Stats)]),
+    "shy_world_reset_stats": (C.c_int, [W]),
+    "shy_world_set_cycle": (C.c_int, [W, C.c_uint64]),
+    "shy_world_enable_timing": (C.c_int, [W, C.c_int]),
+    "shy_world_timing": (C.c_int, [W, P(Timing)]),
+    "shy_world_set_erf_source": (C.c_int, [W, C.c_int]),
+    "shy_erode": (C.c_int, [W, C.c_int, C.c_int]),
+    "shy_erode_exact": (C.c_int, [W, P(C.c_int32), C.c_int]),
+    "shy_drop_descend": (C.c_int, [W, P(DropState), P(C.c_int)]),
+    "shy_drop_run": (C.c_int, [W, C.c_float, C.c_float, FP, C.c_int, P(C.c_int)]),
+    "shy_cascade": (C.c_int, [W, C.c_float, C.c_float]),
+    "shy_normals": (C.c_int, [W, FP, C.c_size_t]),
+    "shy_batch_create": (C.c_int, [C.c_int, P(C.c_int), P(C.c_int), P(C.c_int), P(C.c_uint64),
+                                   P(Params), P(W)]),
+    "shy_batch_erode": (C.c_int, [W, C.c_int]),
+    "shy_batch_size": (C.c_int, [W, P(C.c_int)]),
+    "shy_terrain_size": (C.c_int, [W, C.c_int, P(C.c_int), P(C.c_int), P(C.c_int)]),
+    "shy_terrain_set_field": (C.c_int, [W, C.c_int, C.c_int, FP, C.c_size_t]),
+    "shy_terrain_get_field": (C.c_int, [W, C.c_int, C.c_int, FP, C.c_size_t]),
+    "shy_terrain_erode_exact": (C.c_int, [W, C.c_int, P(C.c_int32), C.c_int]),
+    "shy_terrain_generate": (C.c_int, [W, C.c_int, C.c_uint64, C.c_int]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded libshy.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with simplehydrology_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != SHY_OK:
+        msg = lib().shy_last_error()
+        raise ShyError(rc, msg.decode() if msg else "")
+    return rc
+
+
+def default_params() -> Params:
+    p = Params()
+    check(lib().shy_params_default(C.byref(p)))
+    return p

@@ -1,0 +1,227 @@
+// shy_device.cuh -- device-side building blocks of the erosion model.
+//
+// Every floating-point expression here reproduces the reference's evaluation
+// order (the library is compiled with --fmad=false, so nothing is fused into
+// an FMA, and with IEEE-rounded division and square root), which is what lets
+// the exact mode match the reference bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "shy_internal.h"
+#include "shy_math.h"
+
+namespace shy {
+
+// ---- 32.32 fixed point ------------------------------------------------------
+__device__ __forceinline__ long long q32(float v) { return __float2ll_rn(v * 4294967296.0f); }
+__device__ __forceinline__ long long q64(double v) { return __double2ll_rn(v * 4294967296.0); }
+__device__ __forceinline__ float unq(long long q) {
+  return __double2float_rn(__ll2double_rn(q) * (1.0 / 4294967296.0));
+}
+// h plus a fixed-point sum, rounded once
+__device__ __forceinline__ float addq(float h, long long q) {
+  return __double2float_rn((double)h + __ll2double_rn(q) * (1.0 / 4294967296.0));
+}
+
+// ---- glm semantics on float2/float3 (component-wise, dot summed left to right)
+__device__ __forceinline__ float dot2(float ax, float ay, float bx, float by) { return ax * bx + ay * by; }
+__device__ __forceinline__ float len2(float x, float y) { return sqrtf(dot2(x, y, x, y)); }
+
+__device__ __forceinline__ float3 cross_scaled(float3 a, float3 b, float ms) {
+  // cross(s * a, s * b) with s = vec3(1, mapscale, 1)  (source/cellpool.h:185-198)
+  const float3 sa = make_float3(1.0f * a.x, ms * a.y, 1.0f * a.z);
+  const float3 sb = make_float3(1.0f * b.x, ms * b.y, 1.0f * b.z);
+  return make_float3(sa.y * sb.z - sb.y * sa.z, sa.z * sb.x - sb.z * sa.x, sa.x * sb.y - sb.x * sa.y);
+}
+
+__device__ __forceinline__ bool oob(int x, int y, int nx, int ny) {
+  return x < 0 || y < 0 || x >= nx || y >= ny;
+}
+
+// quad::_normal (source/cellpool.h:182-204) on a height map `h` (terrain
+// base already applied), map.height() returning 0 outside the map.
+template <class HeightAt>
+__device__ __forceinline__ float3 normal_from(HeightAt hat, int px, int py, int nx, int ny, float ms) {
+  float3 n = make_float3(0.0f, 0.0f, 0.0f);
+  const float hp = hat(px, py);
+  auto add = [&](float3 a, float3 b) {
+    const float3 c = cross_scaled(a, b, ms);
+    n = make_float3(n.x + c.x, n.y + c.y, n.z + c.z);
+  };
+  if (!oob(px + 1, py + 1, nx, ny))
+    add(make_float3(0.0f, hat(px, py + 1) - hp, 1.0f), make_float3(1.0f, hat(px + 1, py) - hp, 0.0f));
+  if (!oob(px - 1, py - 1, nx, ny))
+    add(make_float3(0.0f, hat(px, py - 1) - hp, -1.0f), make_float3(-1.0f, hat(px - 1, py) - hp, 0.0f));
+  if (!oob(px + 1, py - 1, nx, ny))
+    add(make_float3(1.0f, hat(px + 1, py) - hp, 0.0f), make_float3(0.0f, hat(px, py - 1) - hp, -1.0f));
+  if (!oob(px - 1, py + 1, nx, ny))
+    add(make_float3(-1.0f, hat(px - 1, py) - hp, 0.0f), make_float3(0.0f, hat(px, py + 1) - hp, 1.0f));
+  const float dd = n.x * n.x + n.y * n.y + n.z * n.z;
+  if (sqrtf(dd) > 0.0f) {
+    const float r = 1.0f / sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+    n = make_float3(n.x * r, n.y * r, n.z * r);
+  }
+  return n;
+}
+
+struct PlainHeights {
+  const float* h;  // terrain-local
+  int nx, ny;
+  __device__ __forceinline__ float operator()(int x, int y) const {
+    return oob(x, y, nx, ny) ? 0.0f : h[(long long)x * ny + y];
+  }
+};
+
+// The neighbour order of World::cascade (source/world.h:94-103).
+__device__ __forceinline__ int nb_dx(int k) { return k < 3 ? -1 : (k < 5 ? 0 : 1); }
+__device__ __forceinline__ int nb_dy(int k) {
+  // -1, 0, 1, -1, 1, -1, 0, 1
+  return (k == 0 || k == 3 || k == 5) ? -1 : ((k == 1 || k == 6) ? 0 : 1);
+}
+
+// Sediment and volume evaporation, source/water.h:135-136, in double as the
+// reference evaluates them.
+__device__ __forceinline__ float evap_div(float s, float evap) {
+  return __double2float_rn((double)s / (1.0 - (double)evap));
+}
+__device__ __forceinline__ float evap_mul(float v, float evap) {
+  return __double2float_rn((double)v * (1.0 - (double)evap));
+}
+
+// ---- exact (sequential, live) model ------------------------------------------
+
+struct DropS {
+  int age;
+  float px, py, sx, sy, vol, sed;
+};
+
+// World::cascade (source/world.h:90-168) on live heights, in place.
+__device__ __forceinline__ void cascade_live(float* h, int nx, int ny, float px, float py,
+                                             const shy_params& P) {
+  int sxs[8], sys_[8];
+  float sh[8], sd[8];
+  int num = 0;
+  const int ix = (int)px, iy = (int)py;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int x = ix + nb_dx(k), y = iy + nb_dy(k);
+    if (oob(x, y, nx, ny)) continue;
+    const float fx = (float)nb_dx(k), fy = (float)nb_dy(k);
+    sxs[num] = x;
+    sys_[num] = y;
+    sh[num] = h[(long long)x * ny + y];
+    sd[num] = len2(fx, fy);
+    ++num;
+  }
+  // stable insertion sort by height (std::sort on <= 16 elements)
+  for (int i = 1; i < num; ++i) {
+    const int vx = sxs[i], vy = sys_[i];
+    const float vh = sh[i], vd = sd[i];
+    int j = i;
+    while (j > 0 && vh < sh[j - 1]) {
+      sxs[j] = sxs[j - 1];
+      sys_[j] = sys_[j - 1];
+      sh[j] = sh[j - 1];
+      sd[j] = sd[j - 1];
+      --j;
+    }
+    sxs[j] = vx;
+    sys_[j] = vy;
+    sh[j] = vh;
+    sd[j] = vd;
+  }
+  float* hc = h + (long long)ix * ny + iy;
+  for (int i = 0; i < num; ++i) {
+    const float diff = *hc - sh[i];
+    if (diff == 0.0f) continue;
+    float excess;
+    if ((double)sh[i] > 0.1)
+      excess = fabsf(diff) - sd[i] * P.max_diff;
+    else
+      excess = fabsf(diff);
+    if (excess <= 0.0f) continue;
+    const float transfer = P.settling * excess / 2.0f;
+    float* hn = h + (long long)sxs[i] * ny + sys_[i];
+    if (diff > 0.0f) {
+      *hc -= transfer;
+      *hn += transfer;
+    } else {
+      *hc += transfer;
+      *hn -= transfer;
+    }
+  }
+}
+
+// Drop::descend (source/water.h:58-156) on live maps.  `rec` holds the
+// per-cell {momentumx, momentumy, discharge, 1 + entrainment*erf(0.4 d)}.
+__device__ __forceinline__ bool descend_live(float* h, const float4* rec, const float* effd,
+                                             float* td, float* tmx, float* tmy, int nx, int ny,
+                                             DropS& d, const shy_params& P, double& gain,
+                                             double& loss, unsigned long long& steps,
+                                             unsigned long long& oobs) {
+  const int ix = (int)d.px, iy = (int)d.py;
+  if (oob(ix, iy, nx, ny)) return false;
+  const long long c = (long long)ix * ny + iy;
+  const float3 n = normal_from(PlainHeights{h, nx, ny}, ix, iy, nx, ny, P.map_scale);
+  if ((float)d.age > P.max_age) {
+    h[c] += d.sed;
+    return false;
+  }
+  if (d.vol < P.min_vol) {
+    h[c] += d.sed;
+    return false;
+  }
+  ++steps;
+  const float4 r = rec[c];
+  const float ed = effd[c];
+  d.sx = d.sx + (P.gravity * n.x) / d.vol;
+  d.sy = d.sy + (P.gravity * n.z) / d.vol;
+  if (len2(r.x, r.y) > 0.0f && len2(d.sx, d.sy) > 0.0f) {
+    const float rf = 1.0f / sqrtf(dot2(r.x, r.y, r.x, r.y));
+    const float rs = 1.0f / sqrtf(dot2(d.sx, d.sy, d.sx, d.sy));
+    const float k = (P.momentum_transfer * dot2(r.x * rf, r.y * rf, d.sx * rs, d.sy * rs)) / (d.vol + r.z);
+    d.sx = d.sx + k * r.x;
+    d.sy = d.sy + k * r.y;
+  }
+  if (len2(d.sx, d.sy) > 0.0f) {
+    const float root2 = sqrtf(2.0f);
+    const float rs = 1.0f / sqrtf(dot2(d.sx, d.sy, d.sx, d.sy));
+    const float ux = d.sx * rs, uy = d.sy * rs;
+    d.sx = root2 * ux;
+    d.sy = root2 * uy;
+  }
+  d.px = d.px + d.sx;
+  d.py = d.py + d.sy;
+  td[c] += d.vol;
+  tmx[c] += d.vol * d.sx;
+  tmy[c] += d.vol * d.sy;
+  const int jx = (int)d.px, jy = (int)d.py;
+  const bool out = oob(jx, jy, nx, ny);
+  float h2;
+  if (out)
+    h2 = __double2float_rn((double)h[c] - 0.002);
+  else
+    h2 = h[(long long)jx * ny + jy];
+  float ceq = r.w * (h[c] - h2);
+  if (ceq < 0.0f) ceq = 0.0f;
+  const float cdiff = ceq - d.sed;
+  d.sed += ed * cdiff;
+  h[c] -= ed * cdiff;
+  const float s0 = d.sed;
+  d.sed = evap_div(d.sed, P.evap_rate);
+  d.vol = evap_mul(d.vol, P.evap_rate);
+  gain += (double)d.sed - (double)s0;
+  if (out) {
+    d.vol = 0.0f;
+    ++oobs;
+    loss += (double)d.sed;
+    return false;
+  }
+  cascade_live(h, nx, ny, d.px, d.py, P);
+  d.age++;
+  return true;
+}
+
+}  // namespace shy

@@ -1,0 +1,149 @@
+// shy_internal.h -- engine internals shared by the .cu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/shy.h"
+
+namespace shy {
+
+// One terrain of a world, as the kernels see it.  A world holds one or more
+// terrains packed back to back in every per-cell array; cell (x, y) of
+// terrain t is element cell_base + x * ny + y (x-major like the reference's
+// math::flatten, source/include/math.h:11-14).
+struct Terrain {
+  long long cell_base;
+  int nx, ny;
+  int drop_base;   // first drop slot of this terrain in a batched cycle
+  int drops;       // drops per batched cycle
+  unsigned long long seed;
+};
+
+// Per-cell 32.32 fixed-point accumulators of the batched mode, one 32-byte
+// sector per cell so that a drop-step's four atomics share one L2 sector.
+struct alignas(32) Acc4 {
+  long long e;    // height change from erosion / deposition this step
+  long long td;   // discharge track (source/water.h:115)
+  long long tmx;  // momentum-x track (:116)
+  long long tmy;  // momentum-y track (:117)
+};
+
+// Device-side counters (see shy_stats).
+struct DevStats {
+  unsigned long long cycles, drops, skipped, oob, steps;
+  long long gain_q, loss_q;  // batched mode, 32.32 fixed point
+  double gain_exact, loss_exact;  // exact (sequential) mode
+};
+
+// Grid barrier state of the persistent lock-step kernel.
+struct GridBar {
+  unsigned long long arrive;  // monotonically increasing arrival count
+  int abort;                  // set when a bounded wait gives up
+  int error;                  // first error code seen on the device
+  unsigned long long live;    // drops still descending in the current cycle
+  unsigned long long tick;    // lock-step step counter (dedupe tags)
+  unsigned long long cycle;   // batched cycle index (spawn RNG)
+};
+
+enum ErfSource { ERF_DEVICE = 0, ERF_HOST_LIBM = 1 };
+
+// Per-kernel CUDA-event timing: events are recorded around each launch on the
+// world's stream and only read back (and summed) when the caller asks.
+struct Timing {
+  bool on = false;
+  double ms[SHY_KERNEL_KINDS] = {0, 0, 0, 0};
+  unsigned long long launches[SHY_KERNEL_KINDS] = {0, 0, 0, 0};
+  struct Pair { cudaEvent_t a, b; int kind; };
+  std::vector<Pair> pending;
+  std::vector<cudaEvent_t> spare;
+};
+
+}  // namespace shy
+
+struct shy_world {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  shy_params P;
+  std::vector<shy::Terrain> terrains;  // host copy
+  long long cells = 0;                 // all terrains
+  int max_drops = 0;                   // drop slots allocated
+  int sm_count = 0;
+
+  // reference-visible per-cell fields
+  float* h = nullptr;         // height
+  float* root = nullptr;      // rootdensity
+  float* plant = nullptr;     // per-cell plant size (vegetation)
+  float* track_f = nullptr;   // 3 x cells: float tracks (d, mx, my)
+  // engine-internal per-cell state
+  float4* rec = nullptr;      // {momentumx, momentumy, discharge, 1 + entrainment*erf(0.4 d)}
+  float* effd = nullptr;      // max(0, depositionRate * (1 - rootdensity))
+  shy::Acc4* acc = nullptr;   // batched fixed-point accumulators
+  long long* casc = nullptr;  // batched cascade deltas
+  int* cnt = nullptr;         // 2 x cells: drops per cell, by step parity
+  unsigned* stamp = nullptr;  // per-cell dedupe tags
+  float* scratch = nullptr;   // cells floats, gather/scatter staging
+  float* relax = nullptr;     // cells floats, second height buffer of the relax stencil
+
+  // drop slots (struct of arrays)
+  float2* dpos = nullptr;
+  float2* dspd = nullptr;
+  float2* dvs = nullptr;      // {volume, sediment}
+  int* dage = nullptr;        // -1: not descending
+  double* dgain = nullptr;    // evaporation gain so far
+  int* dterr = nullptr;       // terrain of the slot
+  long long* dcell = nullptr; // cell of this step's exchange, -1 if none
+  long long* dctr = nullptr;  // cascade centre this slot runs this step, -1 if none
+  int* dcmask = nullptr;      // cells the centre's cascade changed (bit k: neighbour k, bit 8: centre)
+
+  shy::Terrain* dterrains = nullptr;
+  shy::DevStats* stats = nullptr;
+  shy::GridBar* bar = nullptr;
+  shy_drop* ddrop = nullptr;  // single-drop state for shy_drop_descend
+  float* dtrace = nullptr;    // trace buffer for shy_drop_run
+  int dtrace_cap = 0;
+  int* dint = nullptr;        // small scratch (returned flags, counts)
+  int2* dspawn = nullptr;     // exact-mode spawn list
+  int dspawn_cap = 0;
+
+  int erf_source = shy::ERF_DEVICE;
+  int ceq_source = -1;        // erf source of the current ceqfac values (-1 stale)
+  int track_mode = 0;         // 0: track_f holds the last call's tracks
+  int batch_grid = 0;         // CTAs of the lock-step kernel
+  int batch_block = 256;      // threads per CTA
+  int cycles_per_graph = 8;
+  cudaGraphExec_t graph = nullptr;
+  int graph_cycles = 0;
+  int graph_grid = 0;
+
+  shy::Timing timing;
+  float* normals = nullptr;   // 3 x cells, lazily allocated
+};
+
+namespace shy {
+
+// ---- launchers (defined in the .cu files) --------------------------------
+cudaError_t launch_rebuild_records(shy_world* w, int kind_for_timing);
+cudaError_t launch_exact_erode(shy_world* w, int terrain, int n);
+cudaError_t launch_exact_blend(shy_world* w, int terrain);
+cudaError_t launch_drop_descend(shy_world* w, int terrain);
+cudaError_t launch_drop_run(shy_world* w, int terrain, float x, float y, int max_records);
+cudaError_t launch_cascade(shy_world* w, int terrain, float x, float y);
+cudaError_t launch_normals(shy_world* w, int terrain, float* out3);
+cudaError_t launch_batched_cycle(shy_world* w);
+cudaError_t launch_value_noise(shy_world* w, int terrain, unsigned long long seed, int octaves,
+                               double* raw, unsigned long long* minmax);
+cudaError_t launch_gather_comp(shy_world* w, int terrain, int comp, float* out);
+cudaError_t launch_scatter_comp(shy_world* w, int terrain, int comp, const float* in);
+// timing: open a launch interval of `kind` (returns the pair index or -1)
+cudaError_t timing_begin(shy_world* w, int kind, int* slot);
+cudaError_t timing_end(shy_world* w, int slot);
+int batched_max_grid(shy_world* w, int block);
+
+void set_error(const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+
+}  // namespace shy

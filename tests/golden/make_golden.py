@@ -1,0 +1,128 @@
+"""Generate the golden fixtures in this directory from the REFERENCE itself.
+
+The reference's erosion headers are compiled unmodified into
+oracle/_ref/libshyref.so (oracle/Makefile, oracle/ref_harness.cpp); this
+script drives that build through its own entry points -- World::erode,
+Drop::descend, World::cascade, quad::map::normal -- on the reference's
+512 x 512 map and records what it returns:
+
+  ref_traces.npz   per-step drop traces (8 floats per descend() call:
+                   returned, age, pos.x, pos.y, speed.x, speed.y, volume,
+                   sediment) from 12 spawns on the fresh terrain and 8 spawns
+                   on the terrain after the erosion calls below, plus a
+                   SHA-256 of the height map after each of those drops
+  ref_erode.json   srand(1); World::erode(512) four times: SHA-256 of all 8
+                   cell fields after every call, field sums, the budget
+  ref_cascade.json World::cascade at 10 positions of a rough map
+  ref_normals.json SHA-256 of quad::map::normal over the whole terrain
+
+The input terrain is the workloads' value noise (seed 1) written over the
+reference's own map after World::map.init.  Values that go through erf (the
+discharge-coupled parts after the first erosion call) are the host C
+library's erff; these fixtures were made with glibc 2.39 on x86-64.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import platform
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import pyoracle as po  # noqa: E402
+
+N = 512
+SEED = 1
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, np.float32).tobytes()).hexdigest()
+
+
+def main():
+    po.build()
+    assert po.ref_available(), "oracle/_ref/libshyref.so was not built (needs the reference checkout)"
+    R = po.ref()
+    assert R.ref_tilesize() == N
+    order = R.ref_spawn_arg_order()
+    H = po.value_noise(N, N, SEED)
+    base = po.Maps(N, N, height=H)
+
+    rng = np.random.default_rng(0)
+    spawns_fresh = []
+    while len(spawns_fresh) < 12:
+        x, y = rng.integers(0, N, 2)
+        if H[x, y] >= 0.1:
+            spawns_fresh.append((float(x) + 0.5, float(y) + 0.25))
+    traces = {}
+    post_sha = {}
+    for i, (x, y) in enumerate(spawns_fresh):
+        po.ref_set_maps(base)
+        traces[f"fresh_{i}"] = po.ref_drop_run(x, y)
+        post_sha[f"fresh_{i}"] = sha(po.ref_get_maps().height)
+
+    po.ref_set_maps(base)
+    R.ref_srand(SEED)
+    erode = {"order": order, "calls": []}
+    h0 = H.astype(np.float64).sum()
+    for c in range(4):
+        R.ref_erode(512)
+        m = po.ref_get_maps()
+        erode["calls"].append({
+            "sha": {f: sha(m.f[k]) for k, f in enumerate(po.FIELDS)},
+            "sum": {f: float(m.f[k].astype(np.float64).sum()) for k, f in enumerate(po.FIELDS)},
+        })
+    eroded = po.ref_get_maps()
+    erode["height_change"] = float(eroded.height.astype(np.float64).sum() - h0)
+
+    spawns_eroded = []
+    while len(spawns_eroded) < 8:
+        x, y = rng.integers(0, N, 2)
+        if eroded.height[x, y] >= 0.1 and eroded.discharge[x, y] > 0.0:
+            spawns_eroded.append((float(x) + 0.75, float(y) + 0.5))
+    for i, (x, y) in enumerate(spawns_eroded):
+        po.ref_set_maps(eroded)
+        traces[f"eroded_{i}"] = po.ref_drop_run(x, y)
+        post_sha[f"eroded_{i}"] = sha(po.ref_get_maps().height)
+
+    rough = po.Maps(N, N, height=(np.random.default_rng(7).random((N, N)) ** 3).astype(np.float32))
+    po.ref_set_maps(rough)
+    pts = [(0.5, 0.5), (511.9, 511.2), (100.0, 200.0), (300.7, 0.0), (-0.5, 3.0), (255.5, 255.5),
+           (1.0, 510.0), (100.0, 200.0), (17.3, 480.9), (400.0, 400.0)]
+    for x, y in pts:
+        R.ref_cascade(x, y)
+    cascade = {"points": pts, "height_sha": sha(po.ref_get_maps().height), "rough_seed": 7}
+
+    nm = np.zeros((N, N, 3), np.float32)
+    out = np.zeros(3, np.float32)
+    po.ref_set_maps(base)
+    for x in range(N):
+        for y in range(N):
+            R.ref_normal(x, y, po.fptr(out))
+            nm[x, y] = out
+    normals = {"sha": sha(nm)}
+
+    meta = {"generator": "tests/golden/make_golden.py", "map": N, "terrain_seed": SEED,
+            "machine": platform.machine(), "libc": " ".join(platform.libc_ver())}
+    np.savez_compressed(os.path.join(HERE, "ref_traces.npz"),
+                        spawns_fresh=np.array(spawns_fresh, np.float32),
+                        spawns_eroded=np.array(spawns_eroded, np.float32), **traces)
+    with open(os.path.join(HERE, "ref_traces_post.json"), "w") as f:
+        json.dump({"meta": meta, "post_height_sha": post_sha}, f, indent=1)
+    with open(os.path.join(HERE, "ref_erode.json"), "w") as f:
+        json.dump({"meta": meta, **erode}, f, indent=1)
+    with open(os.path.join(HERE, "ref_cascade.json"), "w") as f:
+        json.dump({"meta": meta, **cascade}, f, indent=1)
+    with open(os.path.join(HERE, "ref_normals.json"), "w") as f:
+        json.dump({"meta": meta, **normals}, f, indent=1)
+    print("wrote fixtures:", sorted(os.listdir(HERE)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,127 @@
+"""GPU parity and properties of the batched (lock-step) mode.
+
+At sizes the oracle finishes in seconds the engine must reproduce the
+oracle's Lockstep restatement bit for bit (integer fixed-point sums make the
+schedule deterministic).  At the full 1024^2 / 65,536-drop size the checks
+are size-independent properties: run-to-run bit identity, the height budget
+(sum of height changes = evaporation gain - boundary loss, FP64), finite and
+bounded maps.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def compare_all(get, m, po, what):
+    for k, name in enumerate(po.FIELDS):
+        got = get(name)
+        if not np.array_equal(bits(got), bits(m.f[k])):
+            d = np.abs(got.astype(np.float64) - m.f[k]).max()
+            raise AssertionError(f"{what}: field {name} differs (max |diff| {d:.3g})")
+
+
+@pytest.mark.parametrize("nx,ny,drops,cycles", [(128, 128, 512, 3), (96, 200, 2000, 2), (64, 64, 4096, 2)])
+def test_batched_bitwise_vs_oracle(shy, po, nx, ny, drops, cycles):
+    H = po.value_noise(nx, ny, 21)
+    w = shy.World(nx, ny, seed=77)
+    w.set_field("height", H)
+    w.erode(drops, cycles)
+    m = po.Maps(nx, ny, height=H)
+    acc = po.erode_batched(m, 77, 0, drops, cycles)
+    compare_all(w.get_field, m, po, f"{nx}x{ny}")
+    st = w.stats()
+    assert st.drop_steps == acc.steps
+    assert st.drops == acc.drops and st.drops_skipped == acc.skipped and st.drops_oob == acc.oob
+    assert st.evap_gain == pytest.approx(acc.gain_q / 2**32, abs=1e-9)
+    assert st.boundary_loss == pytest.approx(acc.loss_q / 2**32, abs=1e-9)
+    assert st.cycles == cycles
+    w.close()
+
+
+def test_relax_passes_bitwise(shy, po):
+    nx, ny = 80, 72
+    H = po.value_noise(nx, ny, 4)
+    p = shy.default_params()
+    p.cascade_passes = 2
+    w = shy.World(nx, ny, params=p, seed=5)
+    w.set_field("height", H)
+    w.erode(800, 2)
+    pp = po.default_params()
+    pp.cascade_passes = 2
+    m = po.Maps(nx, ny, height=H)
+    po.erode_batched(m, 5, 0, 800, 2, pp)
+    compare_all(w.get_field, m, po, "relax")
+
+
+def test_batch_of_terrains_matches_each_alone(shy, po):
+    sizes = [(64, 96), (128, 128), (100, 37), (130, 70)]
+    drops = [1536, 4096, 925, 2275]
+    seeds = [1000, 1001, 1002, 1003]
+    b = shy.Batch(sizes, drops, seeds)
+    Hs = []
+    for t, (nx, ny) in enumerate(sizes):
+        b.generate(t, seeds[t], 8)
+        Hs.append(po.value_noise(nx, ny, seeds[t]))
+        assert np.array_equal(bits(b.get_field(t, "height")), bits(Hs[t]))
+    b.erode(2)
+    for t, (nx, ny) in enumerate(sizes):
+        m = po.Maps(nx, ny, height=Hs[t])
+        po.erode_batched(m, seeds[t], 0, drops[t], 2)
+        compare_all(lambda f: b.get_field(t, f), m, po, f"terrain {t}")
+    b.close()
+
+
+def test_empty_and_degenerate(shy, po):
+    # no drops: a cycle still blends (tracks are zero)
+    w = shy.World(16, 16)
+    H = po.value_noise(16, 16, 3)
+    w.set_field("height", H)
+    w.set_field("discharge", np.full((16, 16), 2.0, np.float32))
+    w.erode(0, 1)
+    assert np.array_equal(w.get_field("height"), H)
+    assert np.allclose(w.get_field("discharge"), 1.8)
+    # all spawns below 0.1 are skipped
+    w.set_field("height", np.full((16, 16), 0.05, np.float32))
+    w.reset_stats()
+    w.erode(100, 1)
+    st = w.stats()
+    assert st.drops == 0 and st.drops_skipped == 100 and st.drop_steps == 0
+    w.close()
+    # a 1 x 1 map: every drop leaves at once
+    w = shy.World(1, 1)
+    w.set_field("height", np.ones((1, 1), np.float32))
+    w.erode(50, 1)
+    m = po.Maps(1, 1, height=np.ones((1, 1), np.float32))
+    acc = po.erode_batched(m, 1, 0, 50, 1)
+    assert w.stats().drop_steps == acc.steps
+    compare_all(w.get_field, m, po, "1x1")
+    w.close()
+
+
+def test_full_size_properties(shy):
+    """1024^2, 65,536 drops per cycle: bit-reproducible, budget holds."""
+    n, drops, cycles = 1024, 65536, 4
+    outs = []
+    for rep in range(2):
+        w = shy.World(n, n, seed=2)
+        w.generate(2, 8)
+        h0 = w.get_field("height").astype(np.float64)
+        w.erode(drops, cycles)
+        st = w.stats()
+        h = w.get_field("height")
+        outs.append((h, w.get_field("discharge"), w.get_field("momentum_x"), st.drop_steps))
+        assert np.isfinite(h).all() and h.min() > -1.0 and h.max() < 2.0
+        dH = h.astype(np.float64).sum() - h0.sum()
+        budget = st.evap_gain - st.boundary_loss
+        # float rounding of one height update per touched cell and step
+        assert abs(dH - budget) < 1e-3 * max(1.0, abs(budget)), (dH, budget)
+        assert st.drop_steps > drops * cycles * 50
+        w.close()
+    for a, b in zip(outs[0][:3], outs[1][:3]):
+        assert np.array_equal(bits(a), bits(b))
+    assert outs[0][3] == outs[1][3]
