@@ -314,7 +314,10 @@ int drop_run(Grid<T>& g, const shy_params& P, T x, T y, float* trace, int max_re
 //     Height changes and the three tracks are summed in 32.32 fixed point.
 //  C  World::cascade (source/world.h:90-168) runs once at every distinct cell
 //     a drop moved to, on the heights after phase A's changes; its transfers
-//     are summed in fixed point too.
+//     are summed in fixed point too.  Where the 3 x 3 blocks of k cascades
+//     overlap, a pair's transfer is divided by k (the larger count of its two
+//     cells), so overlapping cascades together move what one would; k = 1
+//     (no overlap) is the reference.
 //  D  heights take phase A's and then phase C's sums.
 // Integer sums make the result independent of the order drops are visited,
 // which is what lets the GPU reproduce it bit for bit.
@@ -338,7 +341,9 @@ struct Lockstep {
   std::vector<float> ceqfac, effd, hbuf;
   std::vector<int64_t> E, Cq, td, tmx, tmy;
   std::vector<int32_t> cnt;
-  std::vector<int64_t> stamp;  // per-cell dedupe tags
+  std::vector<int64_t> stamp;   // per-cell tag: changed this step (phase D list)
+  std::vector<int64_t> cstamp;  // per-cell tag: cascade centre claimed this step
+  std::vector<int32_t> cover;   // cascade centres whose 3 x 3 block holds the cell
   std::vector<int64_t> touched, centers, occupied;
   std::vector<unsigned char> mask;
   int64_t tag = 0;
@@ -393,8 +398,9 @@ struct Lockstep {
       const float excess =
           (double)sn[i].h > 0.1 ? std::fabs(diff) - sn[i].d * P.max_diff : std::fabs(diff);
       if (excess <= 0.0f) continue;
-      const float transfer = P.settling * excess / 2.0f;
       const size_t n = g.at(sn[i].x, sn[i].y);
+      const int32_t k = cover[c] > cover[n] ? cover[c] : cover[n];
+      const float transfer = P.settling * excess / 2.0f / (float)k;
       if (diff > 0.0f) {
         hc -= transfer;
         Cq[n] += q32(transfer);
@@ -459,8 +465,8 @@ struct Lockstep {
       return false;
     }
     const int64_t cc = (int64_t)g.at(jx, jy);  // water.h:151 -> phase C
-    if (stamp[cc] != tag + 1) {
-      stamp[cc] = tag + 1;
+    if (cstamp[cc] != tag) {
+      cstamp[cc] = tag;
       centers.push_back(cc);
     }
     dr.age++;
@@ -476,6 +482,8 @@ struct Lockstep {
     tmy.assign(N, 0);
     cnt.assign(N, 0);
     stamp.assign(N, -1);
+    cstamp.assign(N, -1);
+    cover.assign(N, 0);
     tag = 0;
     std::vector<LDrop> L;
     for (int k = 0; k < drops; ++k) {
@@ -511,14 +519,26 @@ struct Lockstep {
           acc->gain_q += q64(ld.gain);
         }
       }
+      for (int64_t c : centers) {  // how many cascades reach each cell
+        const int x = (int)(c / g.ny), y = (int)(c % g.ny);
+        for (int dx = -1; dx <= 1; ++dx)
+          for (int dy = -1; dy <= 1; ++dy)
+            if (!g.oob(x + dx, y + dy)) cover[g.at(x + dx, y + dy)]++;
+      }
       for (int64_t c : centers) cascade_delta((int)(c / g.ny), (int)(c % g.ny));  // phase C
+      for (int64_t c : centers) {
+        const int x = (int)(c / g.ny), y = (int)(c % g.ny);
+        for (int dx = -1; dx <= 1; ++dx)
+          for (int dy = -1; dy <= 1; ++dy)
+            if (!g.oob(x + dx, y + dy)) cover[g.at(x + dx, y + dy)] = 0;
+      }
       for (int64_t c : touched) {  // phase D
         g.h[c] = addq(addq(g.h[c], E[c]), Cq[c]);
         E[c] = 0;
         Cq[c] = 0;
       }
       for (int64_t c : occupied) cnt[c] = 0;
-      tag += 2;
+      tag += 1;
     }
     // world.h:81-86: tracks to float, lrate blend
     mask.assign(N, 0);

@@ -84,6 +84,7 @@ struct shy_world {
   shy::Acc4* acc = nullptr;   // batched fixed-point accumulators
   long long* casc = nullptr;  // batched cascade deltas
   int* cnt = nullptr;         // 2 x cells: drops per cell, by step parity
+  int* cover = nullptr;       // cascades per step whose 3 x 3 block holds the cell
   unsigned* stamp = nullptr;  // per-cell dedupe tags
   float* scratch = nullptr;   // cells floats, gather/scatter staging
   float* relax = nullptr;     // cells floats, second height buffer of the relax stencil

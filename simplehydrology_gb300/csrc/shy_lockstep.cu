@@ -12,6 +12,9 @@
 //      cell).  The first drop to claim its new cell runs that cell's cascade.
 //   C  World::cascade (source/world.h:90-168) at every claimed cell on the
 //      heights as phase A left them; transfers go to fixed-point accumulators.
+//      Where the 3 x 3 blocks of k cascades overlap, a pair's transfer is
+//      divided by k (the larger count of its two cells), so overlapping
+//      cascades together move what one would.
 //   D  every changed cell is applied once (the first toucher claims it), the
 //      per-cell drop counts move to the next step, finished drops retire.
 // Integer sums make every result independent of thread timing: the same
@@ -95,6 +98,7 @@ struct LockArgs {
   Acc4* acc;
   long long* casc;
   int* cnt;
+  int* cover;
   unsigned* stamp;
   float2* pos;
   float2* spd;
@@ -261,7 +265,15 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
         continue;
       }
       const long long c2 = T.cell_base + (long long)jx * T.ny + jy;  // water.h:151
-      a.ctr[d] = (atomicExch(&a.stamp[c2], ctag) != ctag) ? c2 : -1;
+      if (atomicExch(&a.stamp[c2], ctag) != ctag) {
+        a.ctr[d] = c2;
+        // count the cascades whose 3 x 3 block holds each cell
+        for (int dx = -1; dx <= 1; ++dx)
+          for (int dy = -1; dy <= 1; ++dy)
+            if (!oob(jx + dx, jy + dy, T.nx, T.ny)) atomicAdd(&a.cover[c2 + (long long)dx * T.ny + dy], 1);
+      } else {
+        a.ctr[d] = -1;
+      }
       a.age[d] = ag + 1;
       a.pos[d] = p;
       a.spd[d] = s;
@@ -305,6 +317,7 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
         sd[j] = vd;
       }
       const float h0 = addq(a.h[c2], a.acc[c2].e);
+      const int kc = a.cover[c2];
       float hcv = h0;
       int mask = 256;
       for (int i = 0; i < num; ++i) {
@@ -312,9 +325,12 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
         if (diff == 0.0f) continue;
         const float excess = (double)sh[i] > 0.1 ? fabsf(diff) - sd[i] * P.max_diff : fabsf(diff);
         if (excess <= 0.0f) continue;
-        const float transfer = P.settling * excess / 2.0f;
         const int k = sk[i];
         const long long nc = c2 + (long long)nb_dx(k) * T.ny + nb_dy(k);
+        // centres whose blocks overlap share the pair: divide by the larger
+        // cover count (1 where cascades do not overlap: the reference)
+        const int kn = a.cover[nc];
+        const float transfer = P.settling * excess / 2.0f / (float)(kc > kn ? kc : kn);
         if (diff > 0.0f) {
           hcv -= transfer;
           add_i64(&a.casc[nc], q32(transfer));
@@ -347,6 +363,11 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
         for (int k = 0; k < 8; ++k)
           if (m & (1 << k)) apply_cell(a, c2 + (long long)nb_dx(k) * T.ny + nb_dy(k), atag);
         apply_cell(a, c2, atag);
+        const long long lc = c2 - T.cell_base;
+        const int ix = (int)(lc / T.ny), iy = (int)(lc - (long long)ix * T.ny);
+        for (int dx = -1; dx <= 1; ++dx)
+          for (int dy = -1; dy <= 1; ++dy)
+            if (!oob(ix + dx, iy + dy, T.nx, T.ny)) a.cover[c2 + (long long)dx * T.ny + dy] = 0;
       }
       if (ag == -2) {
         a.age[d] = -1;
@@ -480,6 +501,7 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.acc = w->acc;
   a.casc = w->casc;
   a.cnt = w->cnt;
+  a.cover = w->cover;
   a.stamp = w->stamp;
   a.pos = w->dpos;
   a.spd = w->dspd;

@@ -96,7 +96,7 @@ template <class T> cudaError_t dalloc(T** p, size_t n) {
 void free_world(shy_world* w) {
   if (!w) return;
   if (w->stream) cudaStreamSynchronize(w->stream);
-  void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->acc, w->casc, w->cnt,
+  void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->acc, w->casc, w->cnt, w->cover,
                   w->stamp, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
                   w->dterr, w->dcell, w->dctr, w->dcmask, w->dterrains, w->stats, w->bar, w->ddrop,
                   w->dtrace, w->dint, w->dspawn, w->normals};
@@ -242,6 +242,7 @@ int create_world(int n, const int* nx, const int* ny, const int* drops, const ui
   if ((e = dalloc(&w->acc, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->casc, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->cnt, 2 * N)) != cudaSuccess) return fail(e, "allocate maps");
+  if ((e = dalloc(&w->cover, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->stamp, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->scratch, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->relax, N)) != cudaSuccess) return fail(e, "allocate maps");
@@ -259,6 +260,7 @@ int create_world(int n, const int* nx, const int* ny, const int* drops, const ui
   cudaMemsetAsync(w->acc, 0, sizeof(Acc4) * N, s);
   cudaMemsetAsync(w->casc, 0, sizeof(long long) * N, s);
   cudaMemsetAsync(w->cnt, 0, sizeof(int) * 2 * N, s);
+  cudaMemsetAsync(w->cover, 0, sizeof(int) * N, s);
   cudaMemsetAsync(w->stamp, 0xFF, sizeof(unsigned) * N, s);
   cudaMemsetAsync(w->stats, 0, sizeof(DevStats), s);
   cudaMemsetAsync(w->bar, 0, sizeof(GridBar), s);
