@@ -168,6 +168,7 @@ def run_ours(args):
     rank, world_size, dist = dist_setup(args.gpus)
     dev = torch.cuda.current_device()
 
+    NX, NY, DROPS = args.map, args.map, args.drops
     w = shy.World(NX, NY, seed=SEED)
     w.generate(SEED, 8)
     h0 = w.get_field("height")
@@ -190,6 +191,7 @@ def run_ours(args):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     stops = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     w.enable_timing(True)
+    ph0, it0 = w.lockstep_profile()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -208,6 +210,7 @@ def run_ours(args):
     dev_s = sum(step_ms) / 1e3
     st = w.stats()
     tm = w.timing()
+    ph1, it1 = w.lockstep_profile()
     w.enable_timing(False)
     steps_total = st.drop_steps
     if dist:
@@ -231,13 +234,16 @@ def run_ours(args):
 
     # end to end through the C ABI with pinned host buffers
     fields = ("height", "discharge", "momentum_x", "momentum_y")
+    if args.no_e2e:
+        fields = ()
     host = {f: torch.empty((NX, NY), dtype=torch.float32, pin_memory=True).numpy() for f in fields}
-    host["height"][...] = h0
-    for f in fields[1:]:
-        host[f][...] = 0.0
+    if fields:
+        host["height"][...] = h0
+        for f in fields[1:]:
+            host[f][...] = 0.0
     reset()
     w.reset_stats()
-    e2e_steps = min(args.steps, 50)
+    e2e_steps = min(args.steps, 50) if fields else 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(e2e_steps):
@@ -247,7 +253,7 @@ def run_ours(args):
         for f in fields:
             w.get_field(f, out=host[f])
     e2e_s = time.perf_counter() - t0
-    e2e_value = w.stats().drop_steps * world_size / e2e_s
+    e2e_value = w.stats().drop_steps * world_size / e2e_s if e2e_steps else None
     nbytes = NX * NY * 4 * len(fields)
 
     out = {
@@ -255,7 +261,9 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded value-noise terrain, counter-based spawns)",
-        "config": {"workload": WORKLOAD, "map": [NX, NY], "drops_per_cycle": DROPS,
+        "config": {"workload": WORKLOAD if (NX, DROPS) == (1024, 65536) else
+                   f"profiling case: {NX}x{NY} value-noise terrain, {DROPS} drops/cycle",
+                   "map": [NX, NY], "drops_per_cycle": DROPS,
                    "step": "one erosion cycle", "l2": "flushed between steps (256 MiB write, untimed)",
                    "parallelism": f"replicas x{world_size}" if world_size > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
@@ -266,6 +274,9 @@ def run_ours(args):
                      "kernel": "lockstep_kernel", "avg_launch_ms": avg_ms,
                      "algorithmic_bytes_per_launch": bytes_per_launch},
         "kernel_ms": {"drops": tm.ms[0], "cycle_end": tm.ms[1], "relax": tm.ms[2]},
+        "lockstep": {"iterations": it1 - it0,
+                     "phase_ms": dict(zip(["descend", "wait_a", "cascade", "wait_c", "apply_and_wait", "spawn_exit"],
+                                          [b - a for a, b in zip(ph0, ph1)]))},
         "drop_steps": steps_total, "wall_s": wall,
     }
     out["clocks"] = clk.summary()
@@ -338,6 +349,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # smaller cases for profiling captures; the bench line itself uses the defaults
+    ap.add_argument("--map", type=int, default=NX)
+    ap.add_argument("--drops", type=int, default=DROPS)
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

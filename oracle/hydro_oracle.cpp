@@ -319,26 +319,27 @@ int drop_run(Grid<T>& g, const shy_params& P, T x, T y, float* trace, int max_re
 //     cells), so overlapping cascades together move what one would; k = 1
 //     (no overlap) is the reference.
 //  D  heights take phase A's and then phase C's sums.
-// Integer sums make the result independent of the order drops are visited,
-// which is what lets the GPU reproduce it bit for bit.
+// Heights are held in 32.32 fixed point during batched cycles (hq), with the
+// float maps holding their values rounded to float; the drops read the float
+// values, and phase D adds the step's integer sums to hq.  Integer sums make
+// the result independent of the order drops are visited, which is what lets
+// the GPU reproduce it bit for bit.
 
 const double kQ = 4294967296.0;  // 2^32: 32.32 fixed point
 inline int64_t q32(float v) { return (int64_t)llrintf(v * 4294967296.0f); }
-inline int64_t q64(double v) { return (int64_t)llrint(v * kQ); }
 inline float unq(int64_t q) { return (float)((double)q * (1.0 / kQ)); }
-// height h plus a fixed-point sum, rounded once
-inline float addq(float h, int64_t q) { return (float)((double)h + (double)q * (1.0 / kQ)); }
 
 struct LDrop {
   Drop<float> d;
   bool alive;
-  double gain;
+  int64_t gain_q;  // evaporation gain, 32.32, summed per step
 };
 
 struct Lockstep {
   Grid<float> g;
   shy_params P;
-  std::vector<float> ceqfac, effd, hbuf;
+  std::vector<float> ceqfac, effd;
+  std::vector<int64_t> hq, hqbuf;  // heights, 32.32 fixed point
   std::vector<int64_t> E, Cq, td, tmx, tmy;
   std::vector<int32_t> cnt;
   std::vector<int64_t> stamp;   // per-cell tag: changed this step (phase D list)
@@ -378,7 +379,7 @@ struct Lockstep {
       if (g.oob(x, y)) continue;
       const V2<float> nn = {(float)kNb[k][0], (float)kNb[k][1]};
       const size_t n = g.at(x, y);
-      sn[num++] = {x, y, addq(g.h[n], E[n]), len2(nn)};
+      sn[num++] = {x, y, unq(hq[n] + E[n]), len2(nn)};
     }
     for (int i = 1; i < num; ++i) {
       Pt v = sn[i];
@@ -390,7 +391,7 @@ struct Lockstep {
       sn[j] = v;
     }
     const size_t c = g.at(ix, iy);
-    const float h0 = addq(g.h[c], E[c]);
+    const float h0 = unq(hq[c] + E[c]);
     float hc = h0;
     for (int i = 0; i < num; ++i) {
       const float diff = hc - sn[i].h;
@@ -457,11 +458,11 @@ struct Lockstep {
     const float s0 = dr.sediment;  // water.h:135-136
     dr.sediment = evap_div(dr.sediment, P.evap_rate);
     dr.volume = evap_mul(dr.volume, P.evap_rate);
-    ld.gain += (double)dr.sediment - (double)s0;
+    ld.gain_q += q32(dr.sediment - s0);  // exact difference (Sterbenz)
     if (out) {  // water.h:139-142
       acc->oob++;
       acc->loss += (double)dr.sediment;
-      acc->loss_q += q64((double)dr.sediment);
+      acc->loss_q += q32(dr.sediment);
       return false;
     }
     const int64_t cc = (int64_t)g.at(jx, jy);  // water.h:151 -> phase C
@@ -497,7 +498,7 @@ struct Lockstep {
       LDrop ld;
       ld.d.pos = {(float)x, (float)y};
       ld.alive = true;
-      ld.gain = 0.0;
+      ld.gain_q = 0;
       L.push_back(ld);
     }
     size_t alive = L.size();
@@ -515,8 +516,8 @@ struct Lockstep {
         if (!step(ld, acc)) {
           ld.alive = false;
           --alive;
-          acc->gain += ld.gain;
-          acc->gain_q += q64(ld.gain);
+          acc->gain += (double)ld.gain_q / kQ;
+          acc->gain_q += ld.gain_q;
         }
       }
       for (int64_t c : centers) {  // how many cascades reach each cell
@@ -533,7 +534,8 @@ struct Lockstep {
             if (!g.oob(x + dx, y + dy)) cover[g.at(x + dx, y + dy)] = 0;
       }
       for (int64_t c : touched) {  // phase D
-        g.h[c] = addq(addq(g.h[c], E[c]), Cq[c]);
+        hq[c] += E[c] + Cq[c];
+        g.h[c] = unq(hq[c]);
         E[c] = 0;
         Cq[c] = 0;
       }
@@ -563,12 +565,12 @@ struct Lockstep {
   // moving cascade_weight * settling * excess / 2.  Off by default.
   void relax_pass() {
     const size_t N = (size_t)g.nx * g.ny;
-    hbuf.resize(N);
+    hqbuf.resize(N);
     for (int x = 0; x < g.nx; ++x)
       for (int y = 0; y < g.ny; ++y) {
         const size_t c = g.at(x, y);
         const float hc = g.h[c];
-        double sum = 0.0;
+        int64_t sum = 0;
         for (int k = 0; k < 8; ++k) {
           const int x2 = x + kNb[k][0], y2 = y + kNb[k][1];
           if (g.oob(x2, y2)) continue;
@@ -583,11 +585,12 @@ struct Lockstep {
               (double)lo > 0.1 ? std::fabs(diff) - dist * P.max_diff : std::fabs(diff);
           if (excess <= 0.0f) continue;
           const float transfer = P.cascade_weight * (P.settling * excess / 2.0f);
-          sum += diff > 0.0f ? -(double)transfer : (double)transfer;
+          sum += diff > 0.0f ? -q32(transfer) : q32(transfer);
         }
-        hbuf[c] = (float)((double)hc + sum);
+        hqbuf[c] = hq[c] + sum;
       }
-    std::memcpy(g.h, hbuf.data(), N * sizeof(float));
+    hq.swap(hqbuf);
+    for (size_t i = 0; i < N; ++i) g.h[i] = unq(hq[i]);
   }
 };
 
@@ -695,14 +698,24 @@ void orc_rand_spawns(unsigned seed, int n, int nx, int ny, int order, int32_t* o
 }
 
 // `cycles` batched cycles of `drops` drops each, starting at cycle index
-// `cycle0`.  Tracks come back as the last cycle's sums (as floats).
+// `cycle0`.  Tracks come back as the last cycle's sums (as floats).  The
+// fixed-point heights can be carried between calls in `hq_io` (nx * ny
+// int64): used as the starting state when `hq_in` is nonzero (else derived
+// from the float heights), and written back when `hq_io` is not null.
 int orc_erode_batched_f32(orc_grid_f32* gr, const shy_params* p, uint64_t seed, uint64_t cycle0,
-                          int drops, int cycles, orc_acc* acc) {
+                          int drops, int cycles, orc_acc* acc, int64_t* hq_io, int hq_in) {
   Lockstep b;
   b.g = make_grid<float>(gr);
   b.P = *p;
   b.rebuild_records();
+  const size_t N = (size_t)b.g.nx * b.g.ny;
+  b.hq.resize(N);
+  for (size_t i = 0; i < N; ++i) {  // heights to 32.32 fixed point
+    b.hq[i] = (hq_io && hq_in) ? hq_io[i] : q32(b.g.h[i]);
+    b.g.h[i] = unq(b.hq[i]);
+  }
   for (int c = 0; c < cycles; ++c) b.cycle(seed, cycle0 + (uint64_t)c, drops, acc);
+  if (hq_io) std::memcpy(hq_io, b.hq.data(), N * sizeof(int64_t));
   return 0;
 }
 
@@ -722,6 +735,14 @@ void orc_value_noise(int nx, int ny, uint64_t seed, int octaves, float* out) {
     }
   const double span = hi - lo;
   for (size_t i = 0; i < N; ++i) out[i] = span > 0.0 ? (float)((v[i] - lo) / span) : 0.0f;
+}
+
+// The integer routines the GPU's batched kernels use, for the tests.
+int64_t orc_q32_int(float v) { return shy_q32(v); }
+float orc_unq_int(int64_t q) { return shy_unq(q); }
+float orc_evap_div_int(float s, float evap) {
+  const shy_evap E = shy_evap_make(evap);
+  return shy_evap_div(s, &E);
 }
 
 float orc_erff_libm(float x) { return std::erf(x); }

@@ -100,7 +100,7 @@ def lib():
         L.orc_normals_f32.argtypes = [P(GridF32), P(Params), P(C.c_float)]
         L.orc_rand_spawns.argtypes = [C.c_uint, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int32)]
         L.orc_erode_batched_f32.argtypes = [P(GridF32), P(Params), C.c_uint64, C.c_uint64, C.c_int,
-                                            C.c_int, P(Acc)]
+                                            C.c_int, P(Acc), P(C.c_int64), C.c_int]
         L.orc_value_noise.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_int, P(C.c_float)]
         L.orc_erff_libm.argtypes = [C.c_float]
         L.orc_erff_libm.restype = C.c_float
@@ -161,6 +161,7 @@ class Maps:
         self.nx, self.ny = nx, ny
         self.dtype = np.dtype(dtype)
         self.f = [np.zeros((nx, ny), dtype=self.dtype) for _ in range(8)]
+        self.hq_valid = False
         if height is not None:
             self.f[0][...] = height
 
@@ -171,6 +172,8 @@ class Maps:
         return m
 
     def __getattr__(self, name):
+        if name.startswith("__"):
+            raise AttributeError(name)
         if name in FIELDS:
             return self.f[FIELDS.index(name)]
         raise AttributeError(name)
@@ -238,12 +241,24 @@ def rand_spawns(seed, n, nx, ny, order):
     return out
 
 
-def erode_batched(maps: Maps, seed, cycle0, drops, cycles, params=None):
+def erode_batched(maps: Maps, seed, cycle0, drops, cycles, params=None, hq=None):
+    """Batched (lock-step) cycles in place.  `hq`, an (nx, ny) int64 array,
+    carries the fixed-point heights between calls: pass the same array to a
+    later call to continue exactly where this one stopped (it is filled on
+    the first call, when maps.hq_valid is not set)."""
     params = params or default_params()
     acc = Acc()
     g = maps.grid()
+    hq_ptr = None
+    hq_in = 0
+    if hq is not None:
+        assert hq.dtype == np.int64 and hq.flags.c_contiguous and hq.size == maps.nx * maps.ny
+        hq_ptr = hq.ctypes.data_as(C.POINTER(C.c_int64))
+        hq_in = 1 if getattr(maps, "hq_valid", False) else 0
     lib().orc_erode_batched_f32(C.byref(g), C.byref(params), seed, cycle0, drops, cycles,
-                                C.byref(acc))
+                                C.byref(acc), hq_ptr, hq_in)
+    if hq is not None:
+        maps.hq_valid = True
     return acc
 
 

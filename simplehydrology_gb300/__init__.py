@@ -73,6 +73,13 @@ class _Handle:
         check(lib().shy_world_timing(self._w, C.byref(t)))
         return t
 
+    def lockstep_profile(self):
+        """(phase_ms[6], iterations) of the batched kernel, seen by its first CTA."""
+        ph = (C.c_double * 6)()
+        it = C.c_uint64()
+        check(lib().shy_world_lockstep_profile(self._w, ph, C.byref(it)))
+        return list(ph), it.value
+
     def set_cycle(self, cycle: int):
         check(lib().shy_world_set_cycle(self._w, cycle))
 

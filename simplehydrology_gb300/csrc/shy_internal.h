@@ -23,13 +23,22 @@ struct Terrain {
   unsigned long long seed;
 };
 
-// Per-cell 32.32 fixed-point accumulators of the batched mode, one 32-byte
-// sector per cell so that a drop-step's four atomics share one L2 sector.
-struct alignas(32) Acc4 {
-  long long e;    // height change from erosion / deposition this step
+// Per-cell 32.32 fixed-point accumulators of the batched mode.
+// Track sums over a cycle: one 32-byte sector per cell, so a drop-step's
+// three track atomics share one L2 sector.
+struct alignas(32) Tracks {
   long long td;   // discharge track (source/water.h:115)
   long long tmx;  // momentum-x track (:116)
   long long tmy;  // momentum-y track (:117)
+  long long pad;
+};
+// Batched-mode state of a cell: one 32-byte sector, so that a drop's reads
+// and writes of its cell's height, pending changes and count share it.
+struct alignas(32) CellQ {
+  long long hq;   // height, 32.32 fixed point
+  long long e;    // erosion / deposition of the current step (phase A sums)
+  long long q;    // cascade transfers of the current step (phase C sums)
+  int cnt[2];     // drops at the cell at the start of a step, by step parity
 };
 
 // Device-side counters (see shy_stats).
@@ -39,14 +48,27 @@ struct DevStats {
   double gain_exact, loss_exact;  // exact (sequential) mode
 };
 
+// A cascade of the current step that will move height: its centre, the
+// drop slot that runs it and the nine heights it starts from.
+struct alignas(16) SteepCell {
+  long long c2;
+  int d, ti, ix, iy;
+  float h0;
+  float v[8];
+};
+
 // Grid barrier state of the persistent lock-step kernel.
 struct GridBar {
   unsigned long long arrive;  // monotonically increasing arrival count
   int abort;                  // set when a bounded wait gives up
   int error;                  // first error code seen on the device
   unsigned long long live;    // drops still descending in the current cycle
-  unsigned long long tick;    // lock-step step counter (dedupe tags)
+  unsigned long long tick;    // unused
   unsigned long long cycle;   // batched cycle index (spawn RNG)
+  // CTA 0's view of the lock-step phases: A, wait, C, wait, D + wait, other
+  unsigned long long phase_ns[6];
+  unsigned long long iterations;  // lock-step steps run
+  unsigned steep;                 // entries in the steep-cascade queue
 };
 
 enum ErfSource { ERF_DEVICE = 0, ERF_HOST_LIBM = 1 };
@@ -74,18 +96,19 @@ struct shy_world {
   int sm_count = 0;
 
   // reference-visible per-cell fields
-  float* h = nullptr;         // height
+  float* h = nullptr;         // height (in batched mode: hq rounded to float)
   float* root = nullptr;      // rootdensity
   float* plant = nullptr;     // per-cell plant size (vegetation)
   float* track_f = nullptr;   // 3 x cells: float tracks (d, mx, my)
   // engine-internal per-cell state
   float4* rec = nullptr;      // {momentumx, momentumy, discharge, 1 + entrainment*erf(0.4 d)}
   float* effd = nullptr;      // max(0, depositionRate * (1 - rootdensity))
-  shy::Acc4* acc = nullptr;   // batched fixed-point accumulators
-  long long* casc = nullptr;  // batched cascade deltas
-  int* cnt = nullptr;         // 2 x cells: drops per cell, by step parity
-  int* cover = nullptr;       // cascades per step whose 3 x 3 block holds the cell
-  unsigned* stamp = nullptr;  // per-cell dedupe tags
+  shy::Tracks* trk = nullptr; // batched track sums
+  shy::CellQ* cq = nullptr;   // batched-mode cell state (fixed-point heights)
+  long long* hq_relax = nullptr;  // second fixed-point buffer of the relax stencil
+  float* voltab = nullptr;    // drop volume after k evaporations
+  int voltab_len = 0;
+  bool hq_stale = true;       // h changed outside the batched mode (cq.hq stale)
   float* scratch = nullptr;   // cells floats, gather/scatter staging
   float* relax = nullptr;     // cells floats, second height buffer of the relax stencil
 
@@ -94,11 +117,13 @@ struct shy_world {
   float2* dspd = nullptr;
   float2* dvs = nullptr;      // {volume, sediment}
   int* dage = nullptr;        // -1: not descending
-  double* dgain = nullptr;    // evaporation gain so far
+  long long* dgain = nullptr; // evaporation gain so far, 32.32
+  long long* down = nullptr;  // the drop's own height change this step, 32.32
   int* dterr = nullptr;       // terrain of the slot
   long long* dcell = nullptr; // cell of this step's exchange, -1 if none
   long long* dctr = nullptr;  // cascade centre this slot runs this step, -1 if none
   int* dcmask = nullptr;      // cells the centre's cascade changed (bit k: neighbour k, bit 8: centre)
+  shy::SteepCell* dsteep = nullptr;  // steep-cascade queue (one entry per drop slot at most)
 
   shy::Terrain* dterrains = nullptr;
   shy::DevStats* stats = nullptr;
@@ -135,6 +160,7 @@ cudaError_t launch_drop_run(shy_world* w, int terrain, float x, float y, int max
 cudaError_t launch_cascade(shy_world* w, int terrain, float x, float y);
 cudaError_t launch_normals(shy_world* w, int terrain, float* out3);
 cudaError_t launch_batched_cycle(shy_world* w);
+cudaError_t launch_heights_to_fixed(shy_world* w);
 cudaError_t launch_value_noise(shy_world* w, int terrain, unsigned long long seed, int octaves,
                                double* raw, unsigned long long* minmax);
 cudaError_t launch_gather_comp(shy_world* w, int terrain, int comp, float* out);

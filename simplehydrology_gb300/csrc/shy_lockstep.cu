@@ -7,24 +7,29 @@
 //   A  each live drop takes one Drop::descend step (source/water.h:58-156)
 //      against the heights after step t-1.  A drop sharing its cell with n-1
 //      other live drops exchanges sediment at rate effD / n (n = 1 is the
-//      reference).  Height change and the three tracks go to 32.32
-//      fixed-point accumulators with integer atomics (one 32-byte sector per
-//      cell).  The first drop to claim its new cell runs that cell's cascade.
+//      reference).  The height change goes to the cell's pending erosion sum
+//      and the three tracks to its track record, as 32.32 fixed-point integer
+//      atomics.  Each drop registers at its new cell (the count of the next
+//      step); the first to arrive runs that cell's cascade.
 //   C  World::cascade (source/world.h:90-168) at every claimed cell on the
-//      heights as phase A left them; transfers go to fixed-point accumulators.
+//      heights as phase A left them; transfers go to the pending records.
+//      Cascades that move nothing are settled by their own thread; the steep
+//      ones are queued and run one per warp after one more barrier.
 //      Where the 3 x 3 blocks of k cascades overlap, a pair's transfer is
 //      divided by k (the larger count of its two cells), so overlapping
-//      cascades together move what one would.
-//   D  every changed cell is applied once (the first toucher claims it), the
-//      per-cell drop counts move to the next step, finished drops retire.
+//      cascades together move what one would; the counts come from the
+//      arrivals registered in the 5 x 5 block around the centre.
+//   D  every drop adds its own height change to its cell's fixed-point
+//      height and clears the cell's pending sum and count; each cascade adds
+//      what it moved; finished drops retire.
+// Heights live in 32.32 fixed point for the whole cycle (the float map is
+// rewritten at its end), so every update is an integer addition.
 // Integer sums make every result independent of thread timing: the same
 // inputs give the same bits on every run, and oracle/hydro_oracle.cpp
 // (Lockstep) restates the schedule on the CPU.
 //
 // The end-of-cycle kernel converts the tracks to float, applies the lrate
 // blend (source/world.h:81-86) and rebuilds the per-cell records.
-#include <cooperative_groups.h>
-
 #include "shy_device.cuh"
 
 namespace shy {
@@ -32,6 +37,7 @@ namespace shy {
 namespace {
 
 const int kLockBlock = 256;
+const int kSmemTerrains = 128;
 // A grid barrier gives up (and flags SHY_ERR_TIMEOUT) after this long.
 const unsigned long long kBarrierLimitNs = 2000000000ull;
 
@@ -46,27 +52,35 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ void red_release_add_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 __device__ __forceinline__ int ld_relaxed_i32(const int* p) {
   int v;
   asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
 
-// Grid-wide barrier over a monotonically increasing arrival counter.  Every
-// wait is bounded: past kBarrierLimitNs the waiter sets bar->abort and every
-// later barrier returns false at once, so the kernel always ends.
-__device__ bool grid_barrier(GridBar* bar) {
+__device__ __forceinline__ void add_i64(long long* p, long long v) {
+  atomicAdd((unsigned long long*)p, (unsigned long long)v);
+}
+
+// Grid-wide barrier over a monotonically increasing arrival counter (reset to
+// zero between launches).  `passed` counts the barriers this CTA has passed.
+// Every wait is bounded: past kBarrierLimitNs the waiter sets bar->abort and
+// every later barrier returns false at once, so the kernel always ends.
+__device__ bool grid_barrier(GridBar* bar, unsigned long long& passed) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned long long nb = gridDim.x;
-    __threadfence();
-    const unsigned long long old = atomicAdd(&bar->arrive, 1ull);
-    const unsigned long long target = (old / nb + 1) * nb;
+    const unsigned long long target = (passed + 1) * (unsigned long long)gridDim.x;
+    red_release_add_u64(&bar->arrive, 1ull);
     int ok = 1;
-    const unsigned long long t0 = global_ns();
-    unsigned sleep = 32;
+    unsigned long long t0 = 0;
+    unsigned spins = 0;
     while (ld_acquire_u64(&bar->arrive) < target) {
+      if (++spins < 64) continue;
+      if (t0 == 0) t0 = global_ns();
       if (ld_relaxed_i32(&bar->abort)) {
         ok = 0;
         break;
@@ -77,13 +91,12 @@ __device__ bool grid_barrier(GridBar* bar) {
         ok = 0;
         break;
       }
-      __nanosleep(sleep);
-      if (sleep < 256) sleep <<= 1;
+      __nanosleep(64);
     }
-    __threadfence();
     s_ok = ok;
   }
   __syncthreads();
+  ++passed;
   return s_ok != 0;
 }
 
@@ -92,32 +105,29 @@ struct LockArgs {
   int n_terrains;
   int total_drops;
   long long cells;
-  float* h;
+  const float* h;  // heights rounded to float at cycle start (spawn test)
+  CellQ* cq;       // fixed-point heights, pending changes, drop counts
   const float4* rec;
   const float* effd;
-  Acc4* acc;
-  long long* casc;
-  int* cnt;
-  int* cover;
-  unsigned* stamp;
+  const float* voltab;  // volume after k evaporations (source/water.h:136)
+  shy_evap ev;
+  Tracks* trk;
   float2* pos;
   float2* spd;
   float2* vs;
   int* age;
-  double* gain;
+  long long* gain;  // evaporation gain of the drop so far, 32.32
+  long long* own;   // the drop's own height change this step, 32.32
   int* terr;
   long long* cell;
   long long* ctr;
   int* cmask;
+  SteepCell* steep;  // this step's steep cascades
   shy_params P;
   DevStats* st;
   GridBar* bar;
   int max_steps;
 };
-
-__device__ __forceinline__ void add_i64(long long* p, long long v) {
-  atomicAdd((unsigned long long*)p, (unsigned long long)v);
-}
 
 __device__ __forceinline__ int find_terrain(const Terrain* T, int n, int d) {
   int lo = 0, hi = n - 1;
@@ -126,16 +136,6 @@ __device__ __forceinline__ int find_terrain(const Terrain* T, int n, int d) {
     if (T[mid].drop_base <= d) lo = mid; else hi = mid - 1;
   }
   return lo;
-}
-
-// apply one cell's phase-A and phase-C sums, once per step (first claimer)
-__device__ __forceinline__ void apply_cell(const LockArgs& a, long long x, unsigned atag) {
-  if (atomicExch(&a.stamp[x], atag) == atag) return;
-  const long long e = a.acc[x].e, q = a.casc[x];
-  if (e == 0 && q == 0) return;
-  a.h[x] = addq(addq(a.h[x], e), q);
-  a.acc[x].e = 0;
-  a.casc[x] = 0;
 }
 
 __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v) {
@@ -150,27 +150,94 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v
   return s;  // valid in thread 0
 }
 
+// compare-exchange on (height, neighbour index) keys: a total order, so any
+// sorting network yields exactly the stable sort by height that the
+// reference's std::sort of <= 16 elements (an insertion sort) produces
+__device__ __forceinline__ void cswap(float& ha, int& ka, float& hb, int& kb) {
+  const bool sw = hb < ha || (hb == ha && kb < ka);
+  const float th = sw ? hb : ha, uh = sw ? ha : hb;
+  const int tk = sw ? kb : ka, uk = sw ? ka : kb;
+  ha = th; ka = tk; hb = uh; kb = uk;
+}
+
+__device__ __forceinline__ void sort8(float* h, int* k) {
+#define SHY_CS(i, j) cswap(h[i], k[i], h[j], k[j])
+  SHY_CS(0, 2); SHY_CS(1, 3); SHY_CS(4, 6); SHY_CS(5, 7);
+  SHY_CS(0, 4); SHY_CS(1, 5); SHY_CS(2, 6); SHY_CS(3, 7);
+  SHY_CS(0, 1); SHY_CS(2, 3); SHY_CS(4, 5); SHY_CS(6, 7);
+  SHY_CS(2, 4); SHY_CS(3, 5);
+  SHY_CS(1, 4); SHY_CS(3, 6);
+  SHY_CS(1, 2); SHY_CS(3, 4); SHY_CS(5, 6);
+#undef SHY_CS
+}
+
+// quad::_normal (source/cellpool.h:182-204) from the five heights it reads;
+// the diagonal in-bounds tests decide which triangles count.
+__device__ __forceinline__ float3 normal5(float hp, float hxp, float hxm, float hyp, float hym, bool pp,
+                                          bool mm, bool pm, bool mp, float ms) {
+  float3 n = make_float3(0.0f, 0.0f, 0.0f);
+  auto add = [&](float3 a, float3 b) {
+    const float3 c = cross_scaled(a, b, ms);
+    n = make_float3(n.x + c.x, n.y + c.y, n.z + c.z);
+  };
+  if (pp) add(make_float3(0.0f, hyp - hp, 1.0f), make_float3(1.0f, hxp - hp, 0.0f));
+  if (mm) add(make_float3(0.0f, hym - hp, -1.0f), make_float3(-1.0f, hxm - hp, 0.0f));
+  if (pm) add(make_float3(1.0f, hxp - hp, 0.0f), make_float3(0.0f, hym - hp, -1.0f));
+  if (mp) add(make_float3(-1.0f, hxm - hp, 0.0f), make_float3(0.0f, hyp - hp, 1.0f));
+  const float dd = n.x * n.x + n.y * n.y + n.z * n.z;
+  if (sqrtf(dd) > 0.0f) {
+    const float r = 1.0f / sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+    n = make_float3(n.x * r, n.y * r, n.z * r);
+  }
+  return n;
+}
+
+// the fixed-point height and this step's pending erosion of a cell, in one
+// 16-byte load
+__device__ __forceinline__ longlong2 hq_e(const CellQ* c) {
+  return *reinterpret_cast<const longlong2*>(c);
+}
+
 __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
+  __shared__ Terrain sT[kSmemTerrains];
+  const bool smem_t = a.n_terrains <= kSmemTerrains;
+  if (smem_t)
+    for (int i = threadIdx.x; i < a.n_terrains; i += blockDim.x) sT[i] = a.terrains[i];
+  __syncthreads();
+  const Terrain* TT = smem_t ? sT : a.terrains;
+
   const long long G = (long long)gridDim.x * blockDim.x;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const shy_params& P = a.P;
   const unsigned long long cycle = a.bar->cycle;
-  const unsigned long long tick0 = a.bar->tick;
+  const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long ph[6] = {0, 0, 0, 0, 0, 0};
+  unsigned long long tprev = timer ? global_ns() : 0;
+  auto lap = [&](int i) {
+    if (timer) {
+      const unsigned long long t = global_ns();
+      ph[i] += t - tprev;
+      tprev = t;
+    }
+  };
+  unsigned long long passed = 0;
   unsigned long long n_steps = 0, n_oob = 0, n_drops = 0, n_skipped = 0;
   long long gain_q = 0, loss_q = 0;
+  const shy_evap ev = a.ev;
 
   // spawn (source/world.h:64-74)
   unsigned long long born = 0;
   for (long long d = tid; d < a.total_drops; d += G) {
-    const int t = find_terrain(a.terrains, a.n_terrains, (int)d);
-    const Terrain T = a.terrains[t];
+    const int t = find_terrain(TT, a.n_terrains, (int)d);
+    const Terrain T = TT[t];
     int x, y;
     shy_spawn_xy(T.seed, cycle, (unsigned)(d - T.drop_base), T.nx, T.ny, &x, &y);
     const long long c = T.cell_base + (long long)x * T.ny + y;
     a.terr[d] = t;
     a.cell[d] = -1;
     a.ctr[d] = -1;
-    if ((double)a.h[c] < 0.1) {  // world.h:71
+    // world.h:71; no float lies between 0.1 and 0.1f, so this is h < 0.1
+    if (a.h[c] < 0.1f) {
       a.age[d] = -1;
       ++n_skipped;
       continue;
@@ -181,46 +248,63 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
     a.pos[d] = make_float2((float)x, (float)y);
     a.spd[d] = make_float2(0.0f, 0.0f);
     a.vs[d] = make_float2(1.0f, 0.0f);
-    a.gain[d] = 0.0;
-    atomicAdd(&a.cnt[c], 1);
+    a.gain[d] = 0;
+    atomicAdd(&a.cq[c].cnt[0], 1);
   }
   {
     const unsigned long long s = block_sum_u64(born);
     if (threadIdx.x == 0 && s) atomicAdd(&a.bar->live, s);
   }
-  bool ok = grid_barrier(a.bar);
+  bool ok = grid_barrier(a.bar, passed);
 
   int step = 0;
   for (; ok && step < a.max_steps; ++step) {
     if (*((volatile unsigned long long*)&a.bar->live) == 0) break;
     const int par = step & 1;
-    int* cnt_now = a.cnt + par * a.cells;
-    int* cnt_next = a.cnt + (par ^ 1) * a.cells;
-    const unsigned ctag = (unsigned)(2ull * (tick0 + (unsigned long long)step));
-    const unsigned atag = ctag + 1u;
+    lap(5);
 
     // ---- phase A: one descend step per live drop ----
     for (long long d = tid; d < a.total_drops; d += G) {
       const int ag = a.age[d];
-      if (ag < 0) continue;
-      const Terrain T = a.terrains[a.terr[d]];
-      const float* hT = a.h + T.cell_base;
+      const int ti = a.terr[d];
       float2 p = a.pos[d], s = a.spd[d], v = a.vs[d];
-      double gn = a.gain[d];
+      long long gn = a.gain[d];
+      if (ag < 0) continue;
+      const Terrain T = TT[ti];
+      const CellQ* RT = a.cq + T.cell_base;
       const int ix = (int)p.x, iy = (int)p.y;
-      const long long c = T.cell_base + (long long)ix * T.ny + iy;
+      const long long lc = (long long)ix * T.ny + iy;
+      const long long c = T.cell_base + lc;
       a.cell[d] = c;
-      const float3 n = normal_from(PlainHeights{hT, T.nx, T.ny}, ix, iy, T.nx, T.ny, P.map_scale);
+      // the five heights quad::_normal reads (0 outside the map)
+      const bool xp = ix + 1 < T.nx, xm = ix > 0, yp = iy + 1 < T.ny, ym = iy > 0;
+      // all loads issued together; a neighbour outside the map reads the
+      // centre and is masked to height 0
+      const long long q0 = RT[lc].hq;
+      const int nhere = RT[lc].cnt[par];
+      long long qxp = RT[xp ? lc + T.ny : lc].hq;
+      long long qxm = RT[xm ? lc - T.ny : lc].hq;
+      long long qyp = RT[yp ? lc + 1 : lc].hq;
+      long long qym = RT[ym ? lc - 1 : lc].hq;
+      const float4 r = __ldg(&a.rec[c]);
+      const float ed = __ldg(&a.effd[c]);
+      qxp = xp ? qxp : 0;
+      qxm = xm ? qxm : 0;
+      qyp = yp ? qyp : 0;
+      qym = ym ? qym : 0;
+      const float hp = shy_unq(q0);
+      const float3 n = normal5(hp, shy_unq(qxp), shy_unq(qxm), shy_unq(qyp), shy_unq(qym), xp && yp, xm && ym,
+                               xp && ym, xm && yp, P.map_scale);
       if ((float)ag > P.max_age || v.x < P.min_vol) {  // water.h:74-83
-        add_i64(&a.acc[c].e, q32(v.y));
-        gain_q += q64(gn);
+        const long long dep = shy_q32(v.y);
+        add_i64(&a.cq[c].e, dep);
+        a.own[d] = dep;
+        gain_q += gn;
         a.age[d] = -2;
         a.ctr[d] = -1;
         continue;
       }
       ++n_steps;
-      const float4 r = __ldg(&a.rec[c]);
-      const float ed = __ldg(&a.effd[c]);
       s.x = s.x + (P.gravity * n.x) / v.x;  // water.h:95
       s.y = s.y + (P.gravity * n.z) / v.x;
       if (len2(r.x, r.y) > 0.0f && len2(s.x, s.y) > 0.0f) {  // water.h:97-99
@@ -239,152 +323,257 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
       }
       p.x = p.x + s.x;  // water.h:111
       p.y = p.y + s.y;
-      add_i64(&a.acc[c].td, q32(v.x));  // water.h:115-117
-      add_i64(&a.acc[c].tmx, q32(v.x * s.x));
-      add_i64(&a.acc[c].tmy, q32(v.x * s.y));
       const int jx = (int)p.x, jy = (int)p.y;
       const bool out = oob(jx, jy, T.nx, T.ny);
-      const float hc = hT[(long long)ix * T.ny + iy];
-      const float h2 = out ? __double2float_rn((double)hc - 0.002) : hT[(long long)jx * T.ny + jy];
-      float ceq = r.w * (hc - h2);  // water.h:127-128
+      const long long c2 = T.cell_base + (long long)jx * T.ny + jy;
+      // the next cell's height and the drop's registration there travel
+      // together; the first drop to arrive runs the cell's cascade
+      int arrived_before = 1;
+      long long qn = 0;
+      if (!out) {
+        qn = a.cq[c2].hq;
+        arrived_before = atomicAdd(&a.cq[c2].cnt[par ^ 1], 1);
+      }
+      add_i64(&a.trk[c].td, shy_q32(v.x));  // water.h:115-117
+      add_i64(&a.trk[c].tmx, shy_q32(v.x * s.x));
+      add_i64(&a.trk[c].tmy, shy_q32(v.x * s.y));
+      const float h2 = out ? __double2float_rn((double)hp - 0.002) : shy_unq(qn);  // water.h:120-124
+      float ceq = r.w * (hp - h2);  // water.h:127-128
       if (ceq < 0.0f) ceq = 0.0f;
-      const float edn = ed / (float)cnt_now[c];
+      const float edn = ed / (float)nhere;
       const float ex = edn * (ceq - v.y);  // water.h:129-132
       v.y += ex;
-      add_i64(&a.acc[c].e, -q32(ex));
-      const float s0 = v.y;  // water.h:135-136
-      v.y = evap_div(v.y, P.evap_rate);
-      v.x = evap_mul(v.x, P.evap_rate);
-      gn += (double)v.y - (double)s0;
+      const long long de = -shy_q32(ex);
+      add_i64(&a.cq[c].e, de);
+      a.own[d] = de;
+      const float s0 = v.y;  // water.h:135-136, without the FP64 unit
+      v.y = shy_evap_div(v.y, &ev);
+      v.x = __ldg(&a.voltab[ag + 1]);
+      gn += shy_q32(v.y - s0);  // exact difference (Sterbenz)
       if (out) {  // water.h:139-142
         ++n_oob;
-        loss_q += q64((double)v.y);
-        gain_q += q64(gn);
+        loss_q += shy_q32(v.y);
+        gain_q += gn;
         a.age[d] = -2;
         a.ctr[d] = -1;
         continue;
       }
-      const long long c2 = T.cell_base + (long long)jx * T.ny + jy;  // water.h:151
-      if (atomicExch(&a.stamp[c2], ctag) != ctag) {
-        a.ctr[d] = c2;
-        // count the cascades whose 3 x 3 block holds each cell
-        for (int dx = -1; dx <= 1; ++dx)
-          for (int dy = -1; dy <= 1; ++dy)
-            if (!oob(jx + dx, jy + dy, T.nx, T.ny)) atomicAdd(&a.cover[c2 + (long long)dx * T.ny + dy], 1);
-      } else {
-        a.ctr[d] = -1;
-      }
+      a.ctr[d] = arrived_before == 0 ? c2 : -1;  // World::cascade(pos), water.h:151
       a.age[d] = ag + 1;
       a.pos[d] = p;
       a.spd[d] = s;
       a.vs[d] = v;
       a.gain[d] = gn;
     }
-    if (!grid_barrier(a.bar)) { ok = false; break; }
+    lap(0);
+    if (!grid_barrier(a.bar, passed)) { ok = false; break; }
+    lap(1);
 
     // ---- phase C: World::cascade at each claimed cell ----
-    for (long long d = tid; d < a.total_drops; d += G) {
-      const long long c2 = a.ctr[d];
-      if (c2 < 0) continue;
-      const Terrain T = a.terrains[a.terr[d]];
-      const long long lc = c2 - T.cell_base;
-      const int ix = (int)(lc / T.ny), iy = (int)(lc - (long long)ix * T.ny);
-      int sk[8];
-      float sh[8], sd[8];
-      int num = 0;
+    // C1: each cascade computes the nine heights it works on; most move
+    // nothing (no neighbour starts with excess) and are settled here.  The
+    // steep ones go to a queue, which C2 works through one cell per warp after
+    // a barrier, so that no warp carries more than its share of them.
+    long long sq_c2 = 0;
+    int sq_ti = 0, sq_ix = 0, sq_iy = 0;
+    float sq_h0 = 0.0f, sq_v[8];
+    for (long long d0 = tid - (threadIdx.x & 31); d0 < a.total_drops; d0 += G) {
+      // warp-uniform loop, so that the warp can take queue slots together
+      const int lane = threadIdx.x & 31;
+      const long long d = d0 + lane;
+      const long long c2 = d < a.total_drops ? a.ctr[d] : -1;
+      const int ti = d < a.total_drops ? a.terr[d] : 0;
+      bool steep = false;
+      if (c2 >= 0) {
+      const Terrain T = TT[ti];
+      const int lc = (int)(c2 - T.cell_base);  // < 2^31 cells per terrain
+      const int ix = lc / T.ny, iy = lc - ix * T.ny;
+      // heights after phase A: fixed point plus the step's erosion.  All nine
+      // loads are issued together: a neighbour outside the map reads the
+      // centre instead and is masked out.
+      longlong2 nv[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        const int x = ix + nb_dx(k), y = iy + nb_dy(k);
-        if (oob(x, y, T.nx, T.ny)) continue;
-        const long long nc = T.cell_base + (long long)x * T.ny + y;
-        sk[num] = k;
-        sh[num] = addq(a.h[nc], a.acc[nc].e);
-        sd[num] = len2((float)nb_dx(k), (float)nb_dy(k));
-        ++num;
+        const bool in = !oob(ix + nb_dx(k), iy + nb_dy(k), T.nx, T.ny);
+        nv[k] = hq_e(&a.cq[in ? c2 + (long long)nb_dx(k) * T.ny + nb_dy(k) : c2]);
       }
-      for (int i = 1; i < num; ++i) {  // stable insertion sort by height
-        const int vk = sk[i];
-        const float vh = sh[i], vd = sd[i];
-        int j = i;
-        while (j > 0 && vh < sh[j - 1]) {
-          sk[j] = sk[j - 1];
-          sh[j] = sh[j - 1];
-          sd[j] = sd[j - 1];
-          --j;
+      const longlong2 v0 = hq_e(&a.cq[c2]);
+      float sh[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        sh[k] = oob(ix + nb_dx(k), iy + nb_dy(k), T.nx, T.ny) ? __int_as_float(0x7f800000)  // never used
+                                                              : shy_unq(nv[k].x + nv[k].y);
+      const float h0 = shy_unq(v0.x + v0.y);
+      // the centre only changes through a transfer, so without any excess to
+      // begin with the sequential loop moves nothing
+      bool any = false;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const float diff = h0 - sh[k];
+        const float dist = (nb_dx(k) != 0 && nb_dy(k) != 0) ? sqrtf(2.0f) : 1.0f;
+        const float excess = sh[k] >= 0.1f ? fabsf(diff) - dist * P.max_diff : fabsf(diff);
+        any |= (sh[k] < __int_as_float(0x7f800000)) && diff != 0.0f && excess > 0.0f;
+      }
+      a.cmask[d] = 0;
+      steep = any;
+      if (any) {
+        // keep what the queue entry needs until the warp has its slots
+        sq_c2 = c2; sq_ti = ti; sq_ix = ix; sq_iy = iy; sq_h0 = h0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) sq_v[k] = sh[k];
+      }
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, steep);
+      if (bal) {
+        unsigned base = 0;
+        if (lane == __ffs(bal) - 1) base = atomicAdd(&a.bar->steep, (unsigned)__popc(bal));
+        base = __shfl_sync(0xffffffffu, base, __ffs(bal) - 1);
+        if (steep) {
+          SteepCell& q = a.steep[base + __popc(bal & ((1u << lane) - 1u))];
+          q.c2 = sq_c2;
+          q.d = (int)d;
+          q.ti = sq_ti;
+          q.ix = sq_ix;
+          q.iy = sq_iy;
+          q.h0 = sq_h0;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) q.v[k] = sq_v[k];
         }
-        sk[j] = vk;
-        sh[j] = vh;
-        sd[j] = vd;
       }
-      const float h0 = addq(a.h[c2], a.acc[c2].e);
-      const int kc = a.cover[c2];
-      float hcv = h0;
-      int mask = 256;
-      for (int i = 0; i < num; ++i) {
-        const float diff = hcv - sh[i];
-        if (diff == 0.0f) continue;
-        const float excess = (double)sh[i] > 0.1 ? fabsf(diff) - sd[i] * P.max_diff : fabsf(diff);
-        if (excess <= 0.0f) continue;
-        const int k = sk[i];
-        const long long nc = c2 + (long long)nb_dx(k) * T.ny + nb_dy(k);
-        // centres whose blocks overlap share the pair: divide by the larger
-        // cover count (1 where cascades do not overlap: the reference)
-        const int kn = a.cover[nc];
-        const float transfer = P.settling * excess / 2.0f / (float)(kc > kn ? kc : kn);
-        if (diff > 0.0f) {
-          hcv -= transfer;
-          add_i64(&a.casc[nc], q32(transfer));
-        } else {
-          hcv += transfer;
-          add_i64(&a.casc[nc], -q32(transfer));
-        }
-        mask |= 1 << k;
-      }
-      add_i64(&a.casc[c2], q32(hcv - h0));
-      a.cmask[d] = mask;
     }
-    if (!grid_barrier(a.bar)) { ok = false; break; }
+    lap(2);
+    if (!grid_barrier(a.bar, passed)) { ok = false; break; }
 
-    // ---- phase D: apply, move counts, retire ----
+    // C2: the steep cascades, each by one whole warp
+    {
+      const int lane = threadIdx.x & 31;
+      const unsigned nsteep = *((volatile unsigned*)&a.bar->steep);
+      const long long warp = tid >> 5, nwarps = G >> 5;
+      for (long long i = warp; i < nsteep; i += nwarps) {
+        const SteepCell& qc = a.steep[i];
+        const long long sc2 = qc.c2;
+        const int six = qc.ix, siy = qc.iy;
+        const float sh0 = qc.h0;
+        const Terrain T = TT[qc.ti];
+        float v[8];
+        int sk[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          v[k] = qc.v[k];
+          sk[k] = k;
+        }
+        // cascade centres of this step in the 5 x 5 block (cells a drop moved
+        // to): lane l looks at (dx, dy) = (l / 5 - 2, l % 5 - 2); bit l
+        bool is_c = false;
+        {
+          const int dx = lane < 25 ? lane / 5 - 2 : 0, dy = lane < 25 ? lane % 5 - 2 : 0;
+          const bool in = lane < 25 && !oob(six + dx, siy + dy, T.nx, T.ny);
+          const int cv = a.cq[in ? sc2 + (long long)dx * T.ny + dy : sc2].cnt[par ^ 1];
+          is_c = in && cv > 0;
+        }
+        const unsigned cen = __ballot_sync(0xffffffffu, is_c);
+        // cascades whose 3 x 3 block holds cell (dx, dy): popcount of a window
+        auto cover = [&](int dx, int dy) {
+          const unsigned row = 7u << (dy + 1);  // 3 bits centred on dy
+          const unsigned win = (row << (5 * (dx + 1))) | (row << (5 * (dx + 2))) | (row << (5 * (dx + 3)));
+          return __popc(cen & win);
+        };
+        unsigned kv = 0;  // 4 bits per neighbour
+#pragma unroll
+        for (int k = 0; k < 8; ++k) kv |= (unsigned)cover(nb_dx(k), nb_dy(k)) << (4 * k);
+        const int kc = cover(0, 0);
+        sort8(v, sk);
+        // the reference's sequential loop (every lane, same values)
+        float hcv = sh0;
+        float tr[8];
+        int mask = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          tr[j] = 0.0f;
+          if (!(v[j] < __int_as_float(0x7f800000))) continue;
+          const float diff = hcv - v[j];
+          if (diff == 0.0f) continue;
+          const int k = sk[j];
+          const float dist = (nb_dx(k) != 0 && nb_dy(k) != 0) ? sqrtf(2.0f) : 1.0f;
+          // h > 0.1 in double is h >= 0.1f in float (no float lies between)
+          const float excess = v[j] >= 0.1f ? fabsf(diff) - dist * P.max_diff : fabsf(diff);
+          if (excess <= 0.0f) continue;
+          const int kn = (int)((kv >> (4 * k)) & 15u);
+          const int kk = kc > kn ? kc : kn;
+          float transfer = P.settling * excess / 2.0f;
+          if (kk > 1) transfer = transfer / (float)kk;
+          if (diff > 0.0f) {
+            hcv -= transfer;
+            tr[j] = transfer;
+          } else {
+            hcv += transfer;
+            tr[j] = -transfer;
+          }
+          mask |= 1 << k;
+        }
+        if (mask) mask |= 256;
+        // the fixed-point sums: lane j < 8 the j-th sorted neighbour, lane 8
+        // the centre
+        float t = 0.0f;
+        int kt = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (lane == j) {
+            t = tr[j];
+            kt = sk[j];
+          }
+        if (lane < 8 && t != 0.0f)
+          add_i64(&a.cq[sc2 + (long long)nb_dx(kt) * T.ny + nb_dy(kt)].q, shy_q32(t));
+        if (lane == 8 && mask) add_i64(&a.cq[sc2].q, shy_q32(hcv - sh0));
+        if (lane == 0) a.cmask[qc.d] = mask;
+      }
+    }
+    lap(2);
+    if (!grid_barrier(a.bar, passed)) { ok = false; break; }
+    lap(3);
+
+    // ---- phase D: apply, reset counts, retire ----
+    if (tid == 0) a.bar->steep = 0;
+    // Every drop adds its own erosion to its cell's fixed-point height; the
+    // cascades add what they moved.  All integer additions, so the order
+    // does not matter.
     unsigned long long retired = 0;
     for (long long d = tid; d < a.total_drops; d += G) {
       const int ag = a.age[d];
-      if (ag == -1) continue;
       const long long c = a.cell[d];
-      if (c >= 0) {
-        apply_cell(a, c, atag);
-        cnt_now[c] = 0;
-      }
       const long long c2 = a.ctr[d];
-      if (c2 >= 0) {
-        const Terrain T = a.terrains[a.terr[d]];
-        const int m = a.cmask[d];
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-          if (m & (1 << k)) apply_cell(a, c2 + (long long)nb_dx(k) * T.ny + nb_dy(k), atag);
-        apply_cell(a, c2, atag);
-        const long long lc = c2 - T.cell_base;
-        const int ix = (int)(lc / T.ny), iy = (int)(lc - (long long)ix * T.ny);
-        for (int dx = -1; dx <= 1; ++dx)
-          for (int dy = -1; dy <= 1; ++dy)
-            if (!oob(ix + dx, iy + dy, T.nx, T.ny)) a.cover[c2 + (long long)dx * T.ny + dy] = 0;
+      const long long own = a.own[d];
+      const int ti = a.terr[d];
+      const int m = c2 >= 0 ? a.cmask[d] : 0;
+      if (ag == -1) continue;
+      if (c >= 0) {
+        if (own != 0) add_i64(&a.cq[c].hq, own);
+        a.cq[c].e = 0;
+        a.cq[c].cnt[par] = 0;
+      }
+      if (m) {  // the cells its cascade changed
+        const Terrain T = TT[ti];
+        for (int k = 0; k < 9; ++k) {
+          if (!(m & (1 << (k == 8 ? 8 : k)))) continue;
+          const long long x = k == 8 ? c2 : c2 + (long long)nb_dx(k) * T.ny + nb_dy(k);
+          const long long q = (long long)atomicExch((unsigned long long*)&a.cq[x].q, 0ull);
+          if (q != 0) add_i64(&a.cq[x].hq, q);
+        }
       }
       if (ag == -2) {
         a.age[d] = -1;
         a.cell[d] = -1;
         ++retired;
-      } else {
-        const Terrain T = a.terrains[a.terr[d]];
-        const float2 p = a.pos[d];
-        atomicAdd(&cnt_next[T.cell_base + (long long)(int)p.x * T.ny + (int)p.y], 1);
       }
     }
     {
       const unsigned long long s = block_sum_u64(retired);
       if (threadIdx.x == 0 && s) atomicAdd(&a.bar->live, (unsigned long long)(-(long long)s));
     }
-    if (!grid_barrier(a.bar)) { ok = false; break; }
+    lap(4);
+    if (!grid_barrier(a.bar, passed)) { ok = false; break; }
   }
+  lap(5);
 
   // counters
   {
@@ -398,22 +587,25 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
     v = block_sum_u64((unsigned long long)loss_q);
     if (threadIdx.x == 0 && v) atomicAdd((unsigned long long*)&a.st->loss_q, v);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    a.bar->tick = tick0 + (unsigned long long)step + 1ull;
+  if (timer) {
+    for (int i = 0; i < 6; ++i) a.bar->phase_ns[i] += ph[i];
+    a.bar->iterations += (unsigned long long)step;
     if (ok && a.bar->live != 0) atomicCAS(&a.bar->error, 0, SHY_ERR_STATE);
   }
 }
 
 // End of a batched cycle: tracks to float, lrate blend (source/world.h:81-86),
 // records for the next cycle, accumulators cleared.
-__global__ void cycle_end_kernel(Acc4* __restrict__ acc, float4* __restrict__ rec,
-                                 float* __restrict__ track_f, long long cells, shy_params P,
-                                 GridBar* bar, DevStats* st) {
+__global__ void cycle_end_kernel(Tracks* __restrict__ trk, float4* __restrict__ rec,
+                                 float* __restrict__ track_f, const CellQ* __restrict__ cq,
+                                 float* __restrict__ h, long long cells, shy_params P, GridBar* bar,
+                                 DevStats* st) {
   const float a = 1.0f - P.lrate, b = P.lrate;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells;
        i += (long long)gridDim.x * blockDim.x) {
-    const Acc4 q = acc[i];
-    const float fd = unq(q.td), fx = unq(q.tmx), fy = unq(q.tmy);
+    h[i] = shy_unq(cq[i].hq);
+    const Tracks q = trk[i];
+    const float fd = shy_unq(q.td), fx = shy_unq(q.tmx), fy = shy_unq(q.tmy);
     track_f[i] = fd;
     track_f[cells + i] = fx;
     track_f[2 * cells + i] = fy;
@@ -423,16 +615,17 @@ __global__ void cycle_end_kernel(Acc4* __restrict__ acc, float4* __restrict__ re
     r.y = a * r.y + b * fy;
     r.w = 1.0f + P.entrainment * shy_erff(0.4f * r.z);
     rec[i] = r;
-    Acc4 z;
-    z.e = q.e;  // zero after a completed cycle; kept for a consistency check
+    Tracks z;
     z.td = 0;
     z.tmx = 0;
     z.tmy = 0;
-    acc[i] = z;
+    z.pad = 0;
+    trk[i] = z;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     bar->arrive = 0;
     bar->live = 0;
+    bar->steep = 0;
     bar->cycle += 1;
     st->cycles += 1;
   }
@@ -440,9 +633,11 @@ __global__ void cycle_end_kernel(Acc4* __restrict__ acc, float4* __restrict__ re
 
 // Optional slope relaxation: World::cascade's transfer rule
 // (source/world.h:138-164) as a symmetric stencil over neighbour pairs of
-// which at least one cell was visited this cycle, from `hin` to `hout`.
+// which at least one cell was visited this cycle.  Reads (hin, hqin), writes
+// (hout, hqout); transfers are summed in 32.32 fixed point.
 __global__ void relax_kernel(const Terrain* __restrict__ terrains, int n_terrains,
-                             const float* __restrict__ hin, float* __restrict__ hout,
+                             const float* __restrict__ hin, const CellQ* __restrict__ cqin,
+                             float* __restrict__ hout, long long* __restrict__ hqout,
                              const float* __restrict__ td, long long cells, shy_params P) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells;
        i += (long long)gridDim.x * blockDim.x) {
@@ -453,7 +648,7 @@ __global__ void relax_kernel(const Terrain* __restrict__ terrains, int n_terrain
     const int x = (int)(lc / T.ny), y = (int)(lc - (long long)x * T.ny);
     const float hc = hin[i];
     const bool mc = td[i] != 0.0f;
-    double sum = 0.0;
+    long long sum = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       const int x2 = x + nb_dx(k), y2 = y + nb_dy(k);
@@ -465,12 +660,31 @@ __global__ void relax_kernel(const Terrain* __restrict__ terrains, int n_terrain
       if (diff == 0.0f) continue;
       const float dist = (nb_dx(k) != 0 && nb_dy(k) != 0) ? sqrtf(2.0f) : 1.0f;
       const float lo = hc < hn ? hc : hn;
-      const float excess = (double)lo > 0.1 ? fabsf(diff) - dist * P.max_diff : fabsf(diff);
+      const float excess = lo >= 0.1f ? fabsf(diff) - dist * P.max_diff : fabsf(diff);
       if (excess <= 0.0f) continue;
       const float transfer = P.cascade_weight * (P.settling * excess / 2.0f);
-      sum += diff > 0.0f ? -(double)transfer : (double)transfer;
+      sum += diff > 0.0f ? -shy_q32(transfer) : shy_q32(transfer);
     }
-    hout[i] = __double2float_rn((double)hc + sum);
+    const long long nh = cqin[i].hq + sum;
+    hqout[i] = nh;
+    hout[i] = shy_unq(nh);
+  }
+}
+
+__global__ void relax_commit_kernel(CellQ* __restrict__ cq, const long long* __restrict__ hq, long long cells) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells;
+       i += (long long)gridDim.x * blockDim.x)
+    cq[i].hq = hq[i];
+}
+
+// Heights into the batched mode's fixed point, and the float maps re-rounded
+// from it.
+__global__ void heights_to_fixed_kernel(float* __restrict__ h, CellQ* __restrict__ cq, long long cells) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long q = shy_q32(h[i]);
+    cq[i].hq = q;
+    h[i] = shy_unq(q);
   }
 }
 
@@ -496,22 +710,23 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   for (const auto& T : w->terrains) a.total_drops += T.drops;
   a.cells = w->cells;
   a.h = w->h;
+  a.cq = w->cq;
   a.rec = w->rec;
   a.effd = w->effd;
-  a.acc = w->acc;
-  a.casc = w->casc;
-  a.cnt = w->cnt;
-  a.cover = w->cover;
-  a.stamp = w->stamp;
+  a.voltab = w->voltab;
+  a.ev = shy_evap_make(w->P.evap_rate);
+  a.trk = w->trk;
   a.pos = w->dpos;
   a.spd = w->dspd;
   a.vs = w->dvs;
   a.age = w->dage;
   a.gain = w->dgain;
+  a.own = w->down;
   a.terr = w->dterr;
   a.cell = w->dcell;
   a.ctr = w->dctr;
   a.cmask = w->dcmask;
+  a.steep = w->dsteep;
   a.P = w->P;
   a.st = w->stats;
   a.bar = w->bar;
@@ -532,21 +747,29 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   if ((e = timing_end(w, slot)) != cudaSuccess) return e;
 
   if ((e = timing_begin(w, SHY_KERNEL_APPLY, &slot)) != cudaSuccess) return e;
-  cycle_end_kernel<<<cells_grid(w->cells), 256, 0, w->stream>>>(w->acc, w->rec, w->track_f, w->cells,
-                                                                w->P, w->bar, w->stats);
+  cycle_end_kernel<<<cells_grid(w->cells), 256, 0, w->stream>>>(w->trk, w->rec, w->track_f, w->cq, w->h,
+                                                                w->cells, w->P, w->bar, w->stats);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if ((e = timing_end(w, slot)) != cudaSuccess) return e;
 
   for (int p = 0; p < w->P.cascade_passes; ++p) {
     if ((e = timing_begin(w, SHY_KERNEL_CASCADE, &slot)) != cudaSuccess) return e;
-    relax_kernel<<<cells_grid(w->cells), 256, 0, w->stream>>>(w->dterrains, (int)w->terrains.size(),
-                                                              w->h, w->relax, w->track_f, w->cells, w->P);
+    relax_kernel<<<cells_grid(w->cells), 256, 0, w->stream>>>(w->dterrains, (int)w->terrains.size(), w->h,
+                                                              w->cq, w->relax, w->hq_relax, w->track_f,
+                                                              w->cells, w->P);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     e = cudaMemcpyAsync(w->h, w->relax, sizeof(float) * w->cells, cudaMemcpyDeviceToDevice, w->stream);
     if (e != cudaSuccess) return e;
+    relax_commit_kernel<<<cells_grid(w->cells), 256, 0, w->stream>>>(w->cq, w->hq_relax, w->cells);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = timing_end(w, slot)) != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+cudaError_t launch_heights_to_fixed(shy_world* w) {
+  heights_to_fixed_kernel<<<cells_grid(w->cells), 256, 0, w->stream>>>(w->h, w->cq, w->cells);
+  return cudaGetLastError();
 }
 
 }  // namespace shy

@@ -149,3 +149,137 @@ SHY_HD double shy_value_noise(uint64_t seed, int x, int y, int side, int octaves
   }
   return total;
 }
+
+// ---- integer-only conversions for the batched kernels ---------------------
+// The GPU's FP64 and 64-bit conversion units are far slower than its integer
+// and FP32 units, so the batched hot loop does these three roundings with
+// integer arithmetic.  Each gives exactly the bits of the expression named;
+// oracle/emulation_check.c verifies them over every normal float.
+
+#if defined(__CUDA_ARCH__)
+#define SHY_CLZ64(x) __clzll((long long)(x))
+#define SHY_MULHI64(a, b) __umul64hi((a), (b))
+#define SHY_AS_UINT(f) __float_as_uint(f)
+#define SHY_AS_FLOAT(u) __uint_as_float(u)
+#else
+#include <string.h>
+static inline uint32_t shy_as_uint_h(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+static inline float shy_as_float_h(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+#define SHY_CLZ64(x) __builtin_clzll((unsigned long long)(x))
+#define SHY_MULHI64(a, b) ((uint64_t)(((unsigned __int128)(a) * (unsigned __int128)(b)) >> 64))
+#define SHY_AS_UINT(f) shy_as_uint_h(f)
+#define SHY_AS_FLOAT(u) shy_as_float_h(u)
+#endif
+
+// Round x (> 0) to nearest-even after dropping its `cut` low bits (cut >= 1);
+// `sticky` says whether nonzero bits were already dropped below x.
+SHY_HD uint64_t shy_rne_drop(uint64_t x, int cut, int sticky) {
+  const uint64_t keep = x >> cut;
+  const uint64_t rest = x & ((1ull << cut) - 1ull);
+  const uint64_t half = 1ull << (cut - 1);
+  const int up = rest > half || (rest == half && (sticky || (keep & 1ull)));
+  return (keep + (uint64_t)up) << cut;
+}
+
+// llrintf(v * 2^32): v in 32.32 fixed point, round half to even.  |v| < 2^31.
+SHY_HD int64_t shy_q32(float v) {
+  const uint32_t u = SHY_AS_UINT(v);
+  const int ef = (int)((u >> 23) & 0xFFu);
+  uint64_t m = u & 0x7FFFFFu;
+  int e;  // v = m * 2^e
+  if (ef == 0) {
+    e = -149;
+  } else {
+    m |= 0x800000u;
+    e = ef - 150;
+  }
+  const int s = -(e + 32);  // v * 2^32 = m * 2^(e + 32)
+  uint64_t r;
+  if (s <= 0) {
+    r = m << (-s);
+  } else if (s > 25) {
+    r = 0;  // |v * 2^32| < 1/2
+  } else {
+    const uint64_t keep = m >> s, rest = m & ((1ull << s) - 1ull), half = 1ull << (s - 1);
+    r = keep + (uint64_t)(rest > half || (rest == half && (keep & 1ull)));
+  }
+  return (u >> 31) ? -(int64_t)r : (int64_t)r;
+}
+
+// (float)((double)q * 2^-32): a 32.32 fixed-point value rounded to float.
+// |q| < 2^53, where the double product is exact and this is one rounding.
+SHY_HD float shy_unq(int64_t q) {
+  if (q == 0) return 0.0f;
+  const uint32_t sign = q < 0 ? 0x80000000u : 0u;
+  uint64_t a = q < 0 ? (uint64_t)(-q) : (uint64_t)q;
+  int lead = 63 - SHY_CLZ64(a);
+  if (lead > 23) {
+    a = shy_rne_drop(a, lead - 23, 0);
+    lead = 63 - SHY_CLZ64(a);
+  }
+  // value = a * 2^-32, leading bit `lead`; biased exponent lead - 32 + 127
+  const int be = lead + 95;
+  if (be <= 0) {  // subnormal result: |q| * 2^-32 < 2^-126 cannot happen for |q| >= 1
+    return 0.0f;
+  }
+  const uint64_t mant = lead >= 23 ? (a >> (lead - 23)) : (a << (23 - lead));
+  return SHY_AS_FLOAT(sign | ((uint32_t)be << 23) | ((uint32_t)mant & 0x7FFFFFu));
+}
+
+// (float)((double)s / (1.0 - (double)evap)) of the reference's evaporation
+// (source/water.h:135), for the evaporation constant described by `ev`.
+typedef struct shy_evap {
+  uint64_t nc;    // 1 - evap = nc * 2^-k exactly
+  uint64_t inv;   // floor((2^64 - 1) / nc)
+  uint64_t d;     // evap = d * 2^-k
+  int k;
+  int fast;       // 0: use the double expression
+  double c;       // 1 - (double)evap
+} shy_evap;
+
+SHY_HD shy_evap shy_evap_make(float evap) {
+  shy_evap E;
+  E.c = 1.0 - (double)evap;
+  E.fast = 0;
+  E.nc = E.inv = E.d = 0;
+  E.k = 0;
+  const uint32_t u = SHY_AS_UINT(evap);
+  const int ef = (int)((u >> 23) & 0xFFu);
+  if ((u >> 31) == 0 && ef > 0 && ef < 127) {  // 0 < evap < 1, normal
+    const int k = 150 - ef;                     // evap = d * 2^-k
+    if (k <= 34) {
+      E.k = k;
+      E.d = (u & 0x7FFFFFu) | 0x800000u;
+      E.nc = (1ull << k) - E.d;
+      E.inv = ~0ull / E.nc;
+      E.fast = 1;
+    }
+  }
+  return E;
+}
+
+SHY_HD float shy_evap_div(float s, const shy_evap* E) {
+  const uint32_t u = SHY_AS_UINT(s);
+  const int ef = (int)((u >> 23) & 0xFFu);
+  if (!E->fast || (u >> 31) || ef == 0 || ef > 252) return (float)((double)s / E->c);
+  // s = m * 2^(ef-150); s / c = s + s * d / nc
+  const uint64_t m = (u & 0x7FFFFFu) | 0x800000u;
+  const uint64_t y = m * E->d;  // < 2^48
+  uint64_t qi = SHY_MULHI64(y, E->inv);
+  uint64_t r = y - qi * E->nc;
+  while (r >= E->nc) { r -= E->nc; ++qi; }
+  const uint64_t rs = r << 30;  // r < nc < 2^34
+  uint64_t f = SHY_MULHI64(rs, E->inv);
+  uint64_t r2 = rs - f * E->nc;
+  while (r2 >= E->nc) { r2 -= E->nc; ++f; }
+  // exact quotient = ((m + qi) * 2^30 + f + r2 / nc) * 2^(ef - 180)
+  uint64_t x = ((m + qi) << 30) | f;
+  int lead = 63 - SHY_CLZ64(x);
+  x = shy_rne_drop(x, lead - 52, r2 != 0);  // to double: 53 significant bits
+  lead = 63 - SHY_CLZ64(x);
+  x = shy_rne_drop(x, lead - 23, 0);         // then to float: 24 bits
+  lead = 63 - SHY_CLZ64(x);
+  const int be = ef + lead - 53;
+  const uint64_t mant = x >> (lead - 23);
+  return SHY_AS_FLOAT(((uint32_t)be << 23) | ((uint32_t)mant & 0x7FFFFFu));
+}

@@ -96,10 +96,9 @@ template <class T> cudaError_t dalloc(T** p, size_t n) {
 void free_world(shy_world* w) {
   if (!w) return;
   if (w->stream) cudaStreamSynchronize(w->stream);
-  void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->acc, w->casc, w->cnt, w->cover,
-                  w->stamp, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
+  void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
                   w->dterr, w->dcell, w->dctr, w->dcmask, w->dterrains, w->stats, w->bar, w->ddrop,
-                  w->dtrace, w->dint, w->dspawn, w->normals};
+                  w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (w->graph) cudaGraphExecDestroy(w->graph);
@@ -114,13 +113,15 @@ void free_world(shy_world* w) {
 
 int alloc_drop_slots(shy_world* w, int n) {
   if (n <= w->max_drops) return SHY_OK;
-  void* ptrs[] = {w->dpos, w->dspd, w->dvs, w->dage, w->dgain, w->dterr, w->dcell, w->dctr, w->dcmask};
+  void* ptrs[] = {w->dpos, w->dspd, w->dvs, w->dage, w->dgain, w->dterr, w->dcell, w->dctr, w->dcmask, w->down,
+                  w->dsteep};
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
   for (void* p : ptrs)
     if (p) cudaFree(p);
   w->dpos = w->dspd = w->dvs = nullptr;
   w->dage = w->dterr = w->dcmask = nullptr;
-  w->dgain = nullptr;
+  w->dgain = w->down = nullptr;
+  w->dsteep = nullptr;
   w->dcell = w->dctr = nullptr;
   w->max_drops = 0;
   SHY_CHECK_CUDA(dalloc(&w->dpos, n), "allocate drop slots");
@@ -132,6 +133,8 @@ int alloc_drop_slots(shy_world* w, int n) {
   SHY_CHECK_CUDA(dalloc(&w->dcell, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dctr, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dcmask, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->down, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->dsteep, n), "allocate drop slots");
   w->max_drops = n;
   return SHY_OK;
 }
@@ -147,6 +150,27 @@ int upload_terrains(shy_world* w) {
   SHY_CHECK_CUDA(cudaMemcpyAsync(w->dterrains, w->terrains.data(), sizeof(Terrain) * w->terrains.size(),
                                  cudaMemcpyHostToDevice, w->stream),
                  "upload terrain table");
+  SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
+  return SHY_OK;
+}
+
+// Drop volume after k evaporations, (float)((double)v * (1 - evap)) applied k
+// times from 1 (source/water.h:136): volume depends on nothing else, so the
+// batched kernel looks it up by age.
+int upload_volume_table(shy_world* w) {
+  const int n = (int)w->P.max_age + 3;
+  std::vector<float> v((size_t)n);
+  v[0] = 1.0f;
+  for (int k = 1; k < n; ++k) v[k] = (float)((double)v[k - 1] * (1.0 - (double)w->P.evap_rate));
+  if (n > w->voltab_len) {
+    if (w->voltab) cudaFree(w->voltab);
+    w->voltab = nullptr;
+    w->voltab_len = 0;
+    SHY_CHECK_CUDA(cudaMalloc((void**)&w->voltab, sizeof(float) * n), "allocate volume table");
+    w->voltab_len = n;
+  }
+  SHY_CHECK_CUDA(cudaMemcpyAsync(w->voltab, v.data(), sizeof(float) * n, cudaMemcpyHostToDevice, w->stream),
+                 "upload volume table");
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
   return SHY_OK;
 }
@@ -239,11 +263,8 @@ int create_world(int n, const int* nx, const int* ny, const int* drops, const ui
   if ((e = dalloc(&w->track_f, 3 * N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->rec, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->effd, N)) != cudaSuccess) return fail(e, "allocate maps");
-  if ((e = dalloc(&w->acc, N)) != cudaSuccess) return fail(e, "allocate maps");
-  if ((e = dalloc(&w->casc, N)) != cudaSuccess) return fail(e, "allocate maps");
-  if ((e = dalloc(&w->cnt, 2 * N)) != cudaSuccess) return fail(e, "allocate maps");
-  if ((e = dalloc(&w->cover, N)) != cudaSuccess) return fail(e, "allocate maps");
-  if ((e = dalloc(&w->stamp, N)) != cudaSuccess) return fail(e, "allocate maps");
+  if ((e = dalloc(&w->trk, N)) != cudaSuccess) return fail(e, "allocate maps");
+  if ((e = dalloc(&w->cq, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->scratch, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->relax, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->dterrains, (size_t)n)) != cudaSuccess) return fail(e, "allocate terrain table");
@@ -257,16 +278,17 @@ int create_world(int n, const int* nx, const int* ny, const int* drops, const ui
   cudaMemsetAsync(w->plant, 0, sizeof(float) * N, s);
   cudaMemsetAsync(w->track_f, 0, sizeof(float) * 3 * N, s);
   cudaMemsetAsync(w->rec, 0, sizeof(float4) * N, s);
-  cudaMemsetAsync(w->acc, 0, sizeof(Acc4) * N, s);
-  cudaMemsetAsync(w->casc, 0, sizeof(long long) * N, s);
-  cudaMemsetAsync(w->cnt, 0, sizeof(int) * 2 * N, s);
-  cudaMemsetAsync(w->cover, 0, sizeof(int) * N, s);
-  cudaMemsetAsync(w->stamp, 0xFF, sizeof(unsigned) * N, s);
+  cudaMemsetAsync(w->trk, 0, sizeof(Tracks) * N, s);
+  cudaMemsetAsync(w->cq, 0, sizeof(CellQ) * N, s);
   cudaMemsetAsync(w->stats, 0, sizeof(DevStats), s);
   cudaMemsetAsync(w->bar, 0, sizeof(GridBar), s);
   if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "initialise maps");
   if ((e = launch_rebuild_records(w, -1)) != cudaSuccess) return fail(e, "initialise records");
   w->ceq_source = ERF_DEVICE;
+  if ((rc = upload_volume_table(w)) != SHY_OK) {
+    free_world(w);
+    return rc;
+  }
   rc = upload_terrains(w);
   if (rc != SHY_OK) {
     free_world(w);
@@ -421,7 +443,7 @@ int shy_world_set_params(shy_world* w, const shy_params* p) {
   SHY_CHECK_CUDA(launch_rebuild_records(w, -1), "rebuild records");
   w->ceq_source = ERF_DEVICE;
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
-  return SHY_OK;
+  return upload_volume_table(w);
 }
 
 int shy_world_get_params(shy_world* w, shy_params* out) {
@@ -470,6 +492,7 @@ int shy_terrain_set_field(shy_world* w, int t, int field, const float* host, siz
   const int comp = rec_comp(field);
   float* dst = comp >= 0 ? w->scratch : plain_field(w, t, field);
   SHY_CHECK_CUDA(cudaMemcpyAsync(dst, host, sizeof(float) * n, cudaMemcpyHostToDevice, w->stream), "upload field");
+  if (field == SHY_FIELD_HEIGHT) w->hq_stale = true;
   if (comp >= 0) SHY_CHECK_CUDA(launch_scatter_comp(w, t, comp, w->scratch), "scatter field");
   if (field == SHY_FIELD_DISCHARGE || field == SHY_FIELD_ROOT_DENSITY) {
     SHY_CHECK_CUDA(launch_rebuild_records(w, -1), "rebuild records");
@@ -589,6 +612,18 @@ int shy_world_timing(shy_world* w, shy_timing* out) {
   return SHY_OK;
 }
 
+int shy_world_lockstep_profile(shy_world* w, double* phase_ms, uint64_t* iterations) {
+  int rc = check_world(w);
+  if (rc) return rc;
+  GridBar b;
+  SHY_CHECK_CUDA(cudaMemcpyAsync(&b, w->bar, sizeof(b), cudaMemcpyDeviceToHost, w->stream), "read profile");
+  SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
+  if (phase_ms)
+    for (int i = 0; i < 6; ++i) phase_ms[i] = (double)b.phase_ns[i] * 1e-6;
+  if (iterations) *iterations = b.iterations;
+  return SHY_OK;
+}
+
 int shy_world_set_erf_source(shy_world* w, int source) {
   int rc = check_world(w);
   if (rc) return rc;
@@ -608,6 +643,12 @@ int shy_batch_erode(shy_world* w, int cycles) {
     return SHY_ERR_INVALID_ARG;
   }
   if ((rc = ensure_ceq(w, ERF_DEVICE)) != SHY_OK) return rc;
+  if (w->hq_stale) {
+    SHY_CHECK_CUDA(launch_heights_to_fixed(w), "heights to fixed point");
+    w->hq_stale = false;
+  }
+  if (w->P.cascade_passes > 0 && !w->hq_relax)
+    SHY_CHECK_CUDA(dalloc(&w->hq_relax, (size_t)w->cells), "allocate relax buffer");
   for (int c = 0; c < cycles; ++c) SHY_CHECK_CUDA(launch_batched_cycle(w), "batched cycle");
   return check_device_error(w);
 }
@@ -659,6 +700,7 @@ int shy_terrain_erode_exact(shy_world* w, int t, const int32_t* spawn_xy, int n)
   const long long b = T.cell_base, N = w->cells, cn = (long long)T.nx * T.ny;
   for (int k = 0; k < 3; ++k)  // source/world.h:56-61
     SHY_CHECK_CUDA(cudaMemsetAsync(w->track_f + k * N + b, 0, sizeof(float) * cn, w->stream), "zero tracks");
+  w->hq_stale = true;
   SHY_CHECK_CUDA(launch_exact_erode(w, t, n), "exact erode");
   SHY_CHECK_CUDA(launch_exact_blend(w, t), "exact blend");
   w->ceq_source = ERF_DEVICE;  // the blend rebuilt ceqfac with the device erf
@@ -684,6 +726,7 @@ int shy_drop_descend(shy_world* w, shy_drop* drop, int* more) {
   }
   if ((rc = ensure_ceq(w, w->erf_source)) != SHY_OK) return rc;
   SHY_CHECK_CUDA(cudaMemcpyAsync(w->ddrop, drop, sizeof(shy_drop), cudaMemcpyHostToDevice, w->stream), "upload drop");
+  w->hq_stale = true;
   SHY_CHECK_CUDA(launch_drop_descend(w, 0), "descend");
   SHY_CHECK_CUDA(cudaMemcpyAsync(drop, w->ddrop, sizeof(shy_drop), cudaMemcpyDeviceToHost, w->stream), "download drop");
   int m = 0;
@@ -712,6 +755,7 @@ int shy_drop_run(shy_world* w, float x, float y, float* trace, int max_records, 
     SHY_CHECK_CUDA(dalloc(&w->dtrace, (size_t)max_records * 8), "allocate trace");
     w->dtrace_cap = max_records;
   }
+  w->hq_stale = true;
   SHY_CHECK_CUDA(launch_drop_run(w, 0, x, y, max_records), "drop run");
   int n = 0;
   SHY_CHECK_CUDA(cudaMemcpyAsync(&n, w->dint, sizeof(int), cudaMemcpyDeviceToHost, w->stream), "download count");
@@ -730,6 +774,7 @@ int shy_cascade(shy_world* w, float x, float y) {
     set_error("cascade position must be finite, |pos| < 2^24");
     return SHY_ERR_INVALID_ARG;
   }
+  w->hq_stale = true;
   SHY_CHECK_CUDA(launch_cascade(w, 0, x, y), "cascade");
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
   return SHY_OK;
@@ -747,6 +792,7 @@ int shy_terrain_generate(shy_world* w, int t, uint64_t seed, int octaves) {
   unsigned long long* mm = nullptr;
   SHY_CHECK_CUDA(cudaMallocAsync((void**)&raw, sizeof(double) * n, w->stream), "allocate noise buffer");
   cudaError_t e = cudaMallocAsync((void**)&mm, 2 * sizeof(unsigned long long), w->stream);
+  w->hq_stale = true;
   if (e == cudaSuccess) e = launch_value_noise(w, t, seed, octaves, raw, mm);
   cudaFreeAsync(raw, w->stream);
   if (mm) cudaFreeAsync(mm, w->stream);

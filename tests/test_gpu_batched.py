@@ -83,7 +83,12 @@ def test_empty_and_degenerate(shy, po):
     w.set_field("height", H)
     w.set_field("discharge", np.full((16, 16), 2.0, np.float32))
     w.erode(0, 1)
-    assert np.array_equal(w.get_field("height"), H)
+    m = po.Maps(16, 16, height=H)
+    m.discharge[...] = 2.0
+    po.erode_batched(m, 1, 0, 0, 1)
+    # heights only pass through the 32.32 fixed point of the batched mode
+    assert np.array_equal(bits(w.get_field("height")), bits(m.height))
+    assert np.abs(m.height - H).max() < 2.0 ** -32
     assert np.allclose(w.get_field("discharge"), 1.8)
     # all spawns below 0.1 are skipped
     w.set_field("height", np.full((16, 16), 0.05, np.float32))
@@ -125,3 +130,27 @@ def test_full_size_properties(shy):
     for a, b in zip(outs[0][:3], outs[1][:3]):
         assert np.array_equal(bits(a), bits(b))
     assert outs[0][3] == outs[1][3]
+
+
+def test_consecutive_calls_carry_fixed_point_state(shy, po):
+    """Three shy_erode calls of one cycle each == the oracle carrying its
+    fixed-point heights between calls; a height upload restarts from floats."""
+    nx, ny = 90, 110
+    H = po.value_noise(nx, ny, 31)
+    w = shy.World(nx, ny, seed=8)
+    w.set_field("height", H)
+    m = po.Maps(nx, ny, height=H)
+    hq = np.zeros((nx, ny), np.int64)
+    for c in range(3):
+        w.erode(1500, 1)
+        po.erode_batched(m, 8, c, 1500, 1, hq=hq)
+    compare_all(w.get_field, m, po, "3 calls")
+    # uploading heights makes the float map the state again
+    h2 = w.get_field("height")
+    w.set_field("height", h2)
+    m.f[0][...] = h2
+    m.hq_valid = False
+    w.erode(1500, 1)
+    po.erode_batched(m, 8, 3, 1500, 1, hq=hq)
+    compare_all(w.get_field, m, po, "after upload")
+    w.close()

@@ -50,8 +50,9 @@ def test_batched_is_deterministic_and_cycle_keyed(po):
     a = po.Maps(n, n, height=H)
     b = po.Maps(n, n, height=H)
     po.erode_batched(a, 3, 0, 700, 3)
-    po.erode_batched(b, 3, 0, 700, 1)
-    po.erode_batched(b, 3, 1, 700, 2)  # the cycle index keys the spawns
+    hq = np.zeros((n, n), np.int64)      # the fixed-point heights carry over
+    po.erode_batched(b, 3, 0, 700, 1, hq=hq)
+    po.erode_batched(b, 3, 1, 700, 2, hq=hq)  # the cycle index keys the spawns
     for k in range(8):
         assert np.array_equal(a.f[k].view(np.uint32), b.f[k].view(np.uint32))
 
