@@ -91,3 +91,15 @@ def test_no_device_is_an_error_not_a_fallback(shy):
     assert rc == -4 and not w.value
     with pytest.raises(shy.ShyError):
         shy.World(64, 64)
+
+
+def test_cpp_facade_compiles(shy, tmp_path):
+    """include/shy_world.hpp (the reference's World/Drop names over the C ABI)
+    compiles and links against libshy.so with the host C++ compiler."""
+    exe = tmp_path / "facade_loop"
+    src = os.path.join(ROOT, "tests", "cpp", "facade_loop.cpp")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), src,
+                        "-L" + os.path.dirname(shy._capi.LIB_PATH), "-lshy",
+                        "-Wl,-rpath," + os.path.dirname(shy._capi.LIB_PATH), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
