@@ -27,7 +27,7 @@ int main(int argc, char** argv) {
       }
     shy_stats st;
     shy_ref::check(shy_world_stats(shy_ref::World::map.w, &st));
-    std::printf("{\"frames\": %d, \"drop_steps\": %llu, \"height_sum\": %.9g, \"alpha_sum\": %.9g}\n", frames,
+    std::printf("{\"frames\": %d, \"drop_steps\": %llu, \"height_sum\": %.17g, \"alpha_sum\": %.17g}\n", frames,
                 (unsigned long long)st.drop_steps, hsum, alpha);
     shy_ref::World::shutdown();
   } catch (const shy_ref::Error& e) {
