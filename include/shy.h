@@ -228,6 +228,44 @@ int shy_terrain_erode_exact(shy_world* w, int terrain, const int32_t* spawn_xy, 
  * the workloads' recipe; the normalisation is the reference's (:382-409). */
 int shy_terrain_generate(shy_world* w, int terrain, uint64_t seed, int octaves);
 
+/* ---- batched erosion without allocation ------------------------------------
+ * No counterpart in the reference (which has no GPU path); the library adds
+ * it for callers that cannot allocate device memory themselves or through
+ * the library: a frame loop or plugin running under a host application
+ * that owns all device memory (its own caching allocator has reserved the
+ * GPU, so cudaMalloc fails or is forbidden), or code that must not stall or
+ * fragment the allocator at run time.  Such callers hold the maps in memory
+ * they already own and pass device pointers.
+ *
+ * Runs `cycles` batched cycles (the same lock-step cycles as shy_erode, keyed
+ * by seed and by cycle index cycle0, cycle0 + 1, ...) on one nx-by-ny terrain
+ * whose maps the caller holds in DEVICE memory (nx * ny floats each,
+ * x-major): height, discharge and momentum are read and updated in place,
+ * root_density is read.  Each call starts from the float maps (heights are
+ * rounded into the batched mode's 32.32 fixed point on entry), so a call
+ * equals a fresh world created from the same maps.  `stream` is a
+ * cudaStream_t (NULL for the legacy default stream); the call returns after
+ * the stream finished the work.  `stats` (host, may be NULL) receives the
+ * call's counters.
+ *
+ * It allocates nothing: no cudaMalloc or cudaFree and no allocating library
+ * routine.  Its working memory is one fixed device array of about 8 MiB
+ * inside the library, sized for at most SHY_NOALLOC_MAX_CELLS cells,
+ * SHY_NOALLOC_MAX_DROPS drops per cycle and max_age SHY_NOALLOC_MAX_AGE
+ * (larger requests fail with SHY_ERR_INVALID_ARG), and cascade_passes must be
+ * 0.  Every GPU that loads the library holds that array until the process
+ * exits.  All calls on a device share it: calls that overlap on the GPU (from
+ * other threads or other streams) race and corrupt each other's results, so
+ * serialise them.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before capturing any
+ * stream into a CUDA graph. */
+#define SHY_NOALLOC_MAX_CELLS (256 * 256)
+#define SHY_NOALLOC_MAX_DROPS 16384
+#define SHY_NOALLOC_MAX_AGE 4096
+int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint64_t seed, uint64_t cycle0,
+                      int drops, int cycles, float* height, float* discharge, float* momentum_x,
+                      float* momentum_y, const float* root_density, void* stream, shy_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -151,7 +151,37 @@ struct shy_world {
 
 namespace shy {
 
+// Device buffers of one batched cycle, for launching it on memory the
+// caller laid out (the no-allocation entry point).
+struct CycleBuffers {
+  const Terrain* terrains;
+  int n_terrains;
+  int total_drops;
+  long long cells;
+  float* h;
+  CellQ* cq;
+  float4* rec;
+  const float* effd;
+  const float* voltab;
+  Tracks* trk;
+  float* track_f;
+  float2 *pos, *spd, *vs;
+  int* age;
+  long long* gain;
+  long long* own;
+  int* terr;
+  long long* cell;
+  long long* ctr;
+  int* cmask;
+  SteepCell* steep;
+  DevStats* st;
+  GridBar* bar;
+  shy_params P;
+  int sm_count;
+};
+
 // ---- launchers (defined in the .cu files) --------------------------------
+cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream);
 cudaError_t launch_rebuild_records(shy_world* w, int kind_for_timing);
 cudaError_t launch_exact_erode(shy_world* w, int terrain, int n);
 cudaError_t launch_exact_blend(shy_world* w, int terrain);

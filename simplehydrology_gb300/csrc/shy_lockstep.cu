@@ -767,6 +767,50 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   return cudaSuccess;
 }
 
+// One batched cycle (lock-step kernel + end-of-cycle kernel) on buffers the
+// caller provides; no relax passes.
+cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
+  LockArgs a;
+  a.terrains = b.terrains;
+  a.n_terrains = b.n_terrains;
+  a.total_drops = b.total_drops;
+  a.cells = b.cells;
+  a.h = b.h;
+  a.cq = b.cq;
+  a.rec = b.rec;
+  a.effd = b.effd;
+  a.voltab = b.voltab;
+  a.ev = shy_evap_make(b.P.evap_rate);
+  a.trk = b.trk;
+  a.pos = b.pos;
+  a.spd = b.spd;
+  a.vs = b.vs;
+  a.age = b.age;
+  a.gain = b.gain;
+  a.own = b.own;
+  a.terr = b.terr;
+  a.cell = b.cell;
+  a.ctr = b.ctr;
+  a.cmask = b.cmask;
+  a.steep = b.steep;
+  a.P = b.P;
+  a.st = b.st;
+  a.bar = b.bar;
+  a.max_steps = (int)b.P.max_age + 3;
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lockstep_kernel, kLockBlock, 0);
+  if (e != cudaSuccess) return e;
+  int grid = per_sm * b.sm_count;
+  const int need = (b.total_drops + kLockBlock - 1) / kLockBlock;
+  if (grid > need) grid = need < 1 ? 1 : need;
+  void* args[] = {&a};
+  e = cudaLaunchCooperativeKernel((const void*)lockstep_kernel, dim3(grid), dim3(kLockBlock), args, 0, stream);
+  if (e != cudaSuccess) return e;
+  cycle_end_kernel<<<cells_grid(b.cells), 256, 0, stream>>>(b.trk, b.rec, b.track_f, b.cq, b.h, b.cells, b.P,
+                                                            b.bar, b.st);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_heights_to_fixed(shy_world* w) {
   heights_to_fixed_kernel<<<cells_grid(w->cells), 256, 0, w->stream>>>(w->h, w->cq, w->cells);
   return cudaGetLastError();
