@@ -203,6 +203,21 @@ int shy_drop_run(shy_world* w, float x, float y, float* trace, int max_records,
 /* World::cascade(pos), source/world.h:90-168, on the live heights. */
 int shy_cascade(shy_world* w, float x, float y);
 
+/* Vegetation::grow() (source/vegetation.h:122-188), `steps` times, per cell
+ * and for every terrain of the world: each cell holds at most one plant
+ * (SHY_FIELD_PLANT_SIZE > 0), which grows, dies on discharge, height or a
+ * plant_death_prob draw, and spreads with plant_spread_prob to a cell up to 4
+ * away; empty cells where Plant::spawn allows gain a plant with
+ * plant_spawn_prob.  Plants add and remove root density with the reference's
+ * 3 x 3 weights 1, 0.6, 0.4, which lowers the deposition rate of the batched
+ * and exact erosion (source/water.h:86-87).  Draws come from a counter keyed
+ * by the terrain seed, the step index and the cell; the result is
+ * deterministic.  Equivalent to the reference's plant list in distribution,
+ * not plant by plant. */
+int shy_vegetation_step(shy_world* w, int steps);
+/* Index of the next vegetation step (its random draws). */
+int shy_world_set_vegetation_step(shy_world* w, uint64_t step);
+
 /* quad::map::normal (source/cellpool.h:182-204) of every cell, 3 floats per
  * cell, x-major. */
 int shy_normals(shy_world* w, float* host_xyz, size_t count);

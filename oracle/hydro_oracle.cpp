@@ -594,6 +594,88 @@ struct Lockstep {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Per-cell vegetation: the GPU engine's restatement of Vegetation::grow
+// (source/vegetation.h:122-188).  Every cell holds at most one plant (size
+// > 0); one call is one grow() of every plant, in parallel, against the maps
+// as they were at the start of the call:
+//   grow      size += growRate * (maxSize - size)                  (:63-65)
+//   die       erf(0.4 d) >= maxDischarge, height >= maxTreeHeight,
+//             or a draw below plant_death_prob (1/1000)            (:67-74)
+//             -> root(-1)
+//   spread    with plant_spread_prob (1/20): a target cell offset by
+//             (u9 - 4, u9 - 4); in the map, erf(0.4 d) < maxDischarge, a draw
+//             u1000/1000 above its rootdensity, normal.y > maxSteep, empty
+//             -> new plant, root(+1)                               (:160-183)
+//   spawn     every empty cell with plant_spawn_prob where erf(0.4 d) <
+//             maxDischarge, normal.y >= maxSteep, height < maxTreeHeight
+//             -> new plant, root(+1)                               (:76-85)
+// A new plant has had its first grow (the reference grows a plant in the
+// call that adds it).  A cell that several spawns/spreads reach gets one
+// plant.  root(f) adds f * {1, 0.6, 0.4} over the 3 x 3 block (:87-118),
+// summed in 32.32 fixed point and added once per cell.
+struct VegDraws {
+  uint64_t seed, step;
+  float u(size_t cell, uint32_t what) const { return shy_uniform24(seed, step, cell, what); }
+};
+
+inline float veg_weight(int dx, int dy) {
+  const int n = (dx != 0) + (dy != 0);
+  return n == 0 ? 1.0f : (n == 1 ? 0.6f : 0.4f);
+}
+
+void vegetation_step(Grid<float>& g, float* plant, const shy_params& P, uint64_t seed, uint64_t step) {
+  const size_t N = (size_t)g.nx * g.ny;
+  const VegDraws R = {seed, step};
+  std::vector<float> p0(plant, plant + N);
+  std::vector<int64_t> dq(N, 0);
+  std::vector<unsigned char> taken(N, 0);
+  auto erfd = [&](size_t c) { return shy_erff(0.4f * g.d[c]); };
+  auto root = [&](int x, int y, float f) {
+    for (int dx = -1; dx <= 1; ++dx)
+      for (int dy = -1; dy <= 1; ++dy)
+        if (!g.oob(x + dx, y + dy)) dq[g.at(x + dx, y + dy)] += q32(f * veg_weight(dx, dy));
+  };
+  auto place = [&](int x, int y) {
+    const size_t t = g.at(x, y);
+    if (taken[t]) return;
+    taken[t] = 1;
+    plant[t] = P.plant_grow_rate * (P.plant_max_size - 0.0f);
+    root(x, y, 1.0f);
+  };
+  for (int x = 0; x < g.nx; ++x)
+    for (int y = 0; y < g.ny; ++y) {
+      const size_t c = g.at(x, y);
+      if (p0[c] > 0.0f) {
+        const float s = p0[c] + P.plant_grow_rate * (P.plant_max_size - p0[c]);
+        if (erfd(c) >= P.plant_max_discharge || g.h[c] >= P.plant_max_height ||
+            R.u(c, 0) < P.plant_death_prob) {
+          plant[c] = 0.0f;
+          root(x, y, -1.0f);
+          continue;
+        }
+        plant[c] = s;
+        if (!(R.u(c, 1) < P.plant_spread_prob)) continue;
+        const int tx = x + (int)(R.u(c, 2) * 9.0f) - 4, ty = y + (int)(R.u(c, 3) * 9.0f) - 4;
+        if (g.oob(tx, ty)) continue;
+        const size_t t = g.at(tx, ty);
+        if (erfd(t) >= P.plant_max_discharge) continue;
+        if ((float)(int)(R.u(c, 4) * 1000.0f) / 1000.0f <= g.root[t]) continue;
+        if (!(normal(g, tx, ty, P.map_scale).y > P.plant_max_steep)) continue;
+        if (p0[t] > 0.0f) continue;
+        place(tx, ty);
+      } else {
+        if (!(R.u(c, 5) < P.plant_spawn_prob)) continue;
+        if (erfd(c) >= P.plant_max_discharge) continue;
+        if (normal(g, x, y, P.map_scale).y < P.plant_max_steep) continue;
+        if (g.h[c] >= P.plant_max_height) continue;
+        place(x, y);
+      }
+    }
+  for (size_t i = 0; i < N; ++i)
+    if (dq[i] != 0) g.root[i] = g.root[i] + unq(dq[i]);
+}
+
 }  // namespace
 
 extern "C" {
@@ -717,6 +799,13 @@ int orc_erode_batched_f32(orc_grid_f32* gr, const shy_params* p, uint64_t seed, 
   for (int c = 0; c < cycles; ++c) b.cycle(seed, cycle0 + (uint64_t)c, drops, acc);
   if (hq_io) std::memcpy(hq_io, b.hq.data(), N * sizeof(int64_t));
   return 0;
+}
+
+// One per-cell vegetation step (see vegetation_step); `plant` is nx * ny
+// plant sizes, updated in place with the root-density field.
+void orc_vegetation_step_f32(orc_grid_f32* gr, float* plant, const shy_params* p, uint64_t seed, uint64_t step) {
+  Grid<float> g = make_grid<float>(gr);
+  vegetation_step(g, plant, *p, seed, step);
 }
 
 // Seeded fractal value noise normalised to [0, 1]: the terrain recipe.

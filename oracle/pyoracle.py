@@ -102,6 +102,7 @@ def lib():
         L.orc_erode_batched_f32.argtypes = [P(GridF32), P(Params), C.c_uint64, C.c_uint64, C.c_int,
                                             C.c_int, P(Acc), P(C.c_int64), C.c_int]
         L.orc_value_noise.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_int, P(C.c_float)]
+        L.orc_vegetation_step_f32.argtypes = [P(GridF32), P(C.c_float), P(Params), C.c_uint64, C.c_uint64]
         L.orc_erff_libm.argtypes = [C.c_float]
         L.orc_erff_libm.restype = C.c_float
         L.orc_erff_shy.argtypes = [C.c_float]
@@ -260,6 +261,14 @@ def erode_batched(maps: Maps, seed, cycle0, drops, cycles, params=None, hq=None)
     if hq is not None:
         maps.hq_valid = True
     return acc
+
+
+def vegetation_step(maps: Maps, plant, seed, step, params=None):
+    """One per-cell vegetation step; `plant` (nx, ny) float32 sizes, in place."""
+    params = params or default_params()
+    assert plant.dtype == np.float32 and plant.flags.c_contiguous
+    g = maps.grid()
+    lib().orc_vegetation_step_f32(C.byref(g), fptr(plant), C.byref(params), seed, step)
 
 
 # ---- the compiled reference (512 x 512) -----------------------------------

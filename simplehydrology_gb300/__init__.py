@@ -80,6 +80,10 @@ class _Handle:
         check(lib().shy_world_lockstep_profile(self._w, ph, C.byref(it)))
         return list(ph), it.value
 
+    def vegetation_step(self, steps: int = 1):
+        """Vegetation::grow(), per cell (source/vegetation.h:122-188)."""
+        check(lib().shy_vegetation_step(self._w, steps))
+
     def set_cycle(self, cycle: int):
         check(lib().shy_world_set_cycle(self._w, cycle))
 

@@ -99,6 +99,10 @@ struct shy_world {
   float* h = nullptr;         // height (in batched mode: hq rounded to float)
   float* root = nullptr;      // rootdensity
   float* plant = nullptr;     // per-cell plant size (vegetation)
+  float* plant_next = nullptr;  // second plant buffer of a vegetation step
+  long long* rootq = nullptr;   // root-density sums of a vegetation step, 32.32
+  unsigned* veg_claim = nullptr;  // per-cell new-plant claims (step tags)
+  unsigned long long veg_step = 0;
   float* track_f = nullptr;   // 3 x cells: float tracks (d, mx, my)
   // engine-internal per-cell state
   float4* rec = nullptr;      // {momentumx, momentumy, discharge, 1 + entrainment*erf(0.4 d)}
@@ -191,6 +195,7 @@ cudaError_t launch_cascade(shy_world* w, int terrain, float x, float y);
 cudaError_t launch_normals(shy_world* w, int terrain, float* out3);
 cudaError_t launch_batched_cycle(shy_world* w);
 cudaError_t launch_heights_to_fixed(shy_world* w);
+cudaError_t launch_vegetation_step(shy_world* w);
 cudaError_t launch_value_noise(shy_world* w, int terrain, unsigned long long seed, int octaves,
                                double* raw, unsigned long long* minmax);
 cudaError_t launch_gather_comp(shy_world* w, int terrain, int comp, float* out);

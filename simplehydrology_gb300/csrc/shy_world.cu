@@ -98,7 +98,8 @@ void free_world(shy_world* w) {
   if (w->stream) cudaStreamSynchronize(w->stream);
   void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
                   w->dterr, w->dcell, w->dctr, w->dcmask, w->dterrains, w->stats, w->bar, w->ddrop,
-                  w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down};
+                  w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down,
+                  w->plant_next, w->rootq, w->veg_claim};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (w->graph) cudaGraphExecDestroy(w->graph);
@@ -798,6 +799,35 @@ int shy_terrain_generate(shy_world* w, int t, uint64_t seed, int octaves) {
   if (mm) cudaFreeAsync(mm, w->stream);
   if (e != cudaSuccess) return cuda_fail(e, "generate terrain");
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
+  return SHY_OK;
+}
+
+int shy_vegetation_step(shy_world* w, int steps) {
+  int rc = check_world(w);
+  if (rc) return rc;
+  if (steps < 0) {
+    set_error("negative step count");
+    return SHY_ERR_INVALID_ARG;
+  }
+  if (!w->plant_next) {
+    SHY_CHECK_CUDA(dalloc(&w->plant_next, (size_t)w->cells), "allocate vegetation buffers");
+    SHY_CHECK_CUDA(dalloc(&w->rootq, (size_t)w->cells), "allocate vegetation buffers");
+    SHY_CHECK_CUDA(dalloc(&w->veg_claim, (size_t)w->cells), "allocate vegetation buffers");
+    SHY_CHECK_CUDA(cudaMemsetAsync(w->rootq, 0, sizeof(long long) * w->cells, w->stream), "clear");
+    SHY_CHECK_CUDA(cudaMemsetAsync(w->veg_claim, 0xFF, sizeof(unsigned) * w->cells, w->stream), "clear");
+  }
+  for (int k = 0; k < steps; ++k) {
+    SHY_CHECK_CUDA(launch_vegetation_step(w), "vegetation step");
+    w->veg_step += 1;
+  }
+  SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
+  return SHY_OK;
+}
+
+int shy_world_set_vegetation_step(shy_world* w, uint64_t step) {
+  int rc = check_world(w);
+  if (rc) return rc;
+  w->veg_step = step;
   return SHY_OK;
 }
 
