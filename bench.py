@@ -276,7 +276,7 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": bytes_per_launch},
         "kernel_ms": {"drops": tm.ms[0], "cycle_end": tm.ms[1], "relax": tm.ms[2]},
         "lockstep": {"iterations": it1 - it0,
-                     "phase_ms": dict(zip(["descend", "wait_a", "cascade", "wait_c", "apply_and_wait", "spawn_exit"],
+                     "phase_ms": dict(zip(["descend", "wait_descend", "scan", "wait_scan", "settle", "wait_settle"],
                                           [b - a for a, b in zip(ph0, ph1)]))},
         "drop_steps": steps_total, "wall_s": wall,
     }

@@ -151,8 +151,9 @@ int shy_world_enable_timing(shy_world* w, int on);
 int shy_world_timing(shy_world* w, shy_timing* out);
 /* Where the batched kernel's time goes, as seen by its first CTA, summed
  * over all cycles since creation: phase_ms[6] = {descend phase, barrier
- * wait, cascade phase, barrier wait, apply phase + barrier wait, spawn and
- * exit}; *iterations = lock-step steps run. */
+ * wait, cascade scan phase, barrier wait, settle phase (steep cascades,
+ * height updates, retirements), barrier wait plus spawn and exit};
+ * *iterations = lock-step steps run. */
 int shy_world_lockstep_profile(shy_world* w, double* phase_ms, uint64_t* iterations);
 
 /* Source of erf(0.4 * discharge) (source/cellpool.h:242-244) for the exact

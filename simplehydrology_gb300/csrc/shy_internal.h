@@ -37,7 +37,7 @@ struct alignas(32) Tracks {
 struct alignas(32) CellQ {
   long long hq;   // height, 32.32 fixed point
   long long e;    // erosion / deposition of the current step (phase A sums)
-  long long q;    // cascade transfers of the current step (phase C sums)
+  long long pad;
   int cnt[2];     // drops at the cell at the start of a step, by step parity
 };
 
@@ -48,11 +48,11 @@ struct DevStats {
   double gain_exact, loss_exact;  // exact (sequential) mode
 };
 
-// A cascade of the current step that will move height: its centre, the
-// drop slot that runs it and the nine heights it starts from.
+// A cascade of the current step that will move height: its centre and the
+// nine heights it starts from.
 struct alignas(16) SteepCell {
   long long c2;
-  int d, ti, ix, iy;
+  int ti, ix, iy;
   float h0;
   float v[8];
 };
@@ -65,10 +65,10 @@ struct GridBar {
   unsigned long long live;    // drops still descending in the current cycle
   unsigned long long tick;    // unused
   unsigned long long cycle;   // batched cycle index (spawn RNG)
-  // CTA 0's view of the lock-step phases: A, wait, C, wait, D + wait, other
+  // CTA 0's view of the lock-step phases: descend, wait, scan, wait,
+  // settle, wait
   unsigned long long phase_ns[6];
   unsigned long long iterations;  // lock-step steps run
-  unsigned steep;                 // entries in the steep-cascade queue
 };
 
 enum ErfSource { ERF_DEVICE = 0, ERF_HOST_LIBM = 1 };
@@ -126,7 +126,6 @@ struct shy_world {
   int* dterr = nullptr;       // terrain of the slot
   long long* dcell = nullptr; // cell of this step's exchange, -1 if none
   long long* dctr = nullptr;  // cascade centre this slot runs this step, -1 if none
-  int* dcmask = nullptr;      // cells the centre's cascade changed (bit k: neighbour k, bit 8: centre)
   shy::SteepCell* dsteep = nullptr;  // steep-cascade queue (one entry per drop slot at most)
 
   shy::Terrain* dterrains = nullptr;
@@ -176,7 +175,6 @@ struct CycleBuffers {
   int* terr;
   long long* cell;
   long long* ctr;
-  int* cmask;
   SteepCell* steep;
   DevStats* st;
   GridBar* bar;

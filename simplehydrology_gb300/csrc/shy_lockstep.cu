@@ -1,27 +1,32 @@
 // shy_lockstep.cu -- the batched erosion mode.
 //
 // One batched cycle is World::erode(drops) (source/world.h:54-88) with all
-// drops of every terrain of the world descending at once, one drop per
-// thread slot, in lock step.  Step t is three phases separated by grid-wide
-// barriers:
-//   A  each live drop takes one Drop::descend step (source/water.h:58-156)
-//      against the heights after step t-1.  A drop sharing its cell with n-1
-//      other live drops exchanges sediment at rate effD / n (n = 1 is the
-//      reference).  The height change goes to the cell's pending erosion sum
-//      and the three tracks to its track record, as 32.32 fixed-point integer
-//      atomics.  Each drop registers at its new cell (the count of the next
-//      step); the first to arrive runs that cell's cascade.
-//   C  World::cascade (source/world.h:90-168) at every claimed cell on the
-//      heights as phase A left them; transfers go to the pending records.
-//      Cascades that move nothing are settled by their own thread; the steep
-//      ones are queued and run one per warp after one more barrier.
-//      Where the 3 x 3 blocks of k cascades overlap, a pair's transfer is
-//      divided by k (the larger count of its two cells), so overlapping
-//      cascades together move what one would; the counts come from the
-//      arrivals registered in the 5 x 5 block around the centre.
-//   D  every drop adds its own height change to its cell's fixed-point
-//      height and clears the cell's pending sum and count; each cascade adds
-//      what it moved; finished drops retire.
+// drops of every terrain of the world descending at once, in lock step.  Each
+// CTA owns a contiguous range of drop slots and keeps their state (and its
+// queue of steep cascades) in shared memory when it fits, in the world's
+// global drop arrays otherwise.  Step t is three phases separated by
+// grid-wide barriers:
+//   descend  each live drop takes one Drop::descend step
+//      (source/water.h:58-156) against the heights after step t-1.  A drop
+//      sharing its cell with n-1 other live drops exchanges sediment at rate
+//      effD / n (n = 1 is the reference).  The height change goes to the
+//      cell's pending erosion sum and the three tracks to its track record,
+//      as 32.32 fixed-point integer atomics.  Each drop registers at its new
+//      cell (the count of the next step); the first to arrive runs that
+//      cell's cascade.
+//   scan  World::cascade (source/world.h:90-168) at every claimed cell reads
+//      the nine heights phase descend left (fixed point plus pending sum).
+//      Cascades that move nothing end here; the steep ones are queued in the
+//      CTA with the heights they read.
+//   settle  each queued cascade runs the reference's sequential transfer
+//      loop on one thread and adds its transfers straight to the fixed-point
+//      heights (no height is read in this phase); where the 3 x 3 blocks of k
+//      cascades overlap, a pair's transfer is divided by k (the larger count
+//      of its two cells), so overlapping cascades together move what one
+//      would; the counts come from the arrivals registered in the 5 x 5 block
+//      around the centre.  Every drop adds its own height change to its
+//      cell's fixed-point height and clears the cell's pending sum and count;
+//      finished drops retire.
 // Heights live in 32.32 fixed point for the whole cycle (the float map is
 // rewritten at its end), so every update is an integer addition.
 // Integer sums make every result independent of thread timing: the same
@@ -38,6 +43,8 @@ namespace {
 
 const int kLockBlock = 256;
 const int kSmemTerrains = 128;
+// shared-memory bytes per drop slot: its state plus one steep-queue entry
+const int kSlotBytes = 3 * 8 + 4 * 8 + 2 * 4 + (int)sizeof(SteepCell);
 // A grid barrier gives up (and flags SHY_ERR_TIMEOUT) after this long.
 const unsigned long long kBarrierLimitNs = 2000000000ull;
 
@@ -50,6 +57,11 @@ __device__ __forceinline__ unsigned long long global_ns() {
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
   unsigned long long v;
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
 __device__ __forceinline__ void red_release_add_u64(unsigned long long* p, unsigned long long v) {
@@ -67,9 +79,12 @@ __device__ __forceinline__ void add_i64(long long* p, long long v) {
 
 // Grid-wide barrier over a monotonically increasing arrival counter (reset to
 // zero between launches).  `passed` counts the barriers this CTA has passed.
-// Every wait is bounded: past kBarrierLimitNs the waiter sets bar->abort and
-// every later barrier returns false at once, so the kernel always ends.
-__device__ bool grid_barrier(GridBar* bar, unsigned long long& passed) {
+// Thread 0 reads the live-drop count once the barrier is passed (every CTA
+// added its retirements before arriving) and leaves it in `*live` for the
+// whole CTA.  Every wait is bounded: past kBarrierLimitNs the waiter sets
+// bar->abort and every later barrier returns false at once, so the kernel
+// always ends.
+__device__ bool grid_barrier(GridBar* bar, unsigned long long& passed, unsigned long long* live) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -93,6 +108,7 @@ __device__ bool grid_barrier(GridBar* bar, unsigned long long& passed) {
       }
       __nanosleep(64);
     }
+    if (live) *live = ld_relaxed_u64(&bar->live);
     s_ok = ok;
   }
   __syncthreads();
@@ -112,6 +128,8 @@ struct LockArgs {
   const float* voltab;  // volume after k evaporations (source/water.h:136)
   shy_evap ev;
   Tracks* trk;
+  // global drop slots and steep queue (used when a CTA's range does not fit
+  // in shared memory)
   float2* pos;
   float2* spd;
   float2* vs;
@@ -121,13 +139,57 @@ struct LockArgs {
   int* terr;
   long long* cell;
   long long* ctr;
-  int* cmask;
-  SteepCell* steep;  // this step's steep cascades
+  SteepCell* steep;
+  int smem_slots;   // 1: drop slots and queue live in dynamic shared memory
   shy_params P;
   DevStats* st;
   GridBar* bar;
   int max_steps;
 };
+
+// The drop slots [lo, lo + n) of one CTA.
+struct Slots {
+  float2* pos;
+  float2* spd;
+  float2* vs;  // {volume, sediment}
+  long long* gain;
+  long long* own;
+  long long* cell;  // cell of this step's exchange, -1 if none
+  long long* ctr;   // cascade centre this slot runs this step, -1 if none
+  int* age;         // >= 0 descending, -2 finished this step, -1 idle
+  int* terr;
+  SteepCell* steep;
+};
+
+__device__ __forceinline__ Slots slots_of(const LockArgs& a, unsigned char* smem, long long lo, int cap) {
+  Slots S;
+  if (a.smem_slots) {
+    // 16-byte entries first, then 8-byte, then 4-byte arrays
+    unsigned char* p = smem;
+    S.steep = reinterpret_cast<SteepCell*>(p); p += sizeof(SteepCell) * cap;
+    S.pos = reinterpret_cast<float2*>(p); p += 8 * cap;
+    S.spd = reinterpret_cast<float2*>(p); p += 8 * cap;
+    S.vs = reinterpret_cast<float2*>(p); p += 8 * cap;
+    S.gain = reinterpret_cast<long long*>(p); p += 8 * cap;
+    S.own = reinterpret_cast<long long*>(p); p += 8 * cap;
+    S.cell = reinterpret_cast<long long*>(p); p += 8 * cap;
+    S.ctr = reinterpret_cast<long long*>(p); p += 8 * cap;
+    S.age = reinterpret_cast<int*>(p); p += 4 * cap;
+    S.terr = reinterpret_cast<int*>(p);
+  } else {
+    S.steep = a.steep + lo;
+    S.pos = a.pos + lo;
+    S.spd = a.spd + lo;
+    S.vs = a.vs + lo;
+    S.gain = a.gain + lo;
+    S.own = a.own + lo;
+    S.cell = a.cell + lo;
+    S.ctr = a.ctr + lo;
+    S.age = a.age + lo;
+    S.terr = a.terr + lo;
+  }
+  return S;
+}
 
 __device__ __forceinline__ int find_terrain(const Terrain* T, int n, int d) {
   int lo = 0, hi = n - 1;
@@ -198,16 +260,96 @@ __device__ __forceinline__ longlong2 hq_e(const CellQ* c) {
   return *reinterpret_cast<const longlong2*>(c);
 }
 
+// World::cascade's transfer loop (source/world.h:127-165) for one queued
+// centre: the neighbours in the reference's stable height order, the live
+// centre height, each transfer divided by the overlap count of its pair.
+// Transfers go straight to the fixed-point heights.
+__device__ __forceinline__ void settle_cascade(const SteepCell& qc, const Terrain& T, CellQ* cq, int par,
+                                               const shy_params& P) {
+  const long long c2 = qc.c2;
+  const int ix = qc.ix, iy = qc.iy;
+  // cascade centres of this step in the 5 x 5 block (cells a drop moved to):
+  // bit l for (dx, dy) = (l / 5 - 2, l % 5 - 2); a cell outside the map reads
+  // the centre and is masked out
+  int cv[25];
+#pragma unroll
+  for (int l = 0; l < 25; ++l) {
+    const int dx = l / 5 - 2, dy = l % 5 - 2;
+    const bool in = !oob(ix + dx, iy + dy, T.nx, T.ny);
+    cv[l] = cq[in ? c2 + (long long)dx * T.ny + dy : c2].cnt[par ^ 1];
+  }
+  unsigned cen = 0;
+#pragma unroll
+  for (int l = 0; l < 25; ++l) {
+    const int dx = l / 5 - 2, dy = l % 5 - 2;
+    const bool in = !oob(ix + dx, iy + dy, T.nx, T.ny);
+    cen |= (in && cv[l] > 0) ? (1u << l) : 0u;
+  }
+  // cascades whose 3 x 3 block holds cell (dx, dy): popcount of a window
+  auto cover = [&](int dx, int dy) {
+    const unsigned row = 7u << (dy + 1);  // 3 bits centred on dy
+    const unsigned win = (row << (5 * (dx + 1))) | (row << (5 * (dx + 2))) | (row << (5 * (dx + 3)));
+    return __popc(cen & win);
+  };
+  const int kc = cover(0, 0);
+  float v[8];
+  int sk[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    v[k] = qc.v[k];
+    sk[k] = k;
+  }
+  sort8(v, sk);
+  const float h0 = qc.h0;
+  float hcv = h0;
+  bool moved = false;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    if (!(v[j] < __int_as_float(0x7f800000))) continue;  // outside the map
+    const float diff = hcv - v[j];
+    if (diff == 0.0f) continue;
+    const int k = sk[j];
+    const float dist = (nb_dx(k) != 0 && nb_dy(k) != 0) ? sqrtf(2.0f) : 1.0f;
+    // h > 0.1 in double is h >= 0.1f in float (no float lies between)
+    const float excess = v[j] >= 0.1f ? fabsf(diff) - dist * P.max_diff : fabsf(diff);
+    if (excess <= 0.0f) continue;
+    const int kn = cover(nb_dx(k), nb_dy(k));
+    const int kk = kc > kn ? kc : kn;
+    float transfer = P.settling * excess / 2.0f;
+    if (kk > 1) transfer = transfer / (float)kk;
+    float t;
+    if (diff > 0.0f) {
+      hcv -= transfer;
+      t = transfer;
+    } else {
+      hcv += transfer;
+      t = -transfer;
+    }
+    moved = true;
+    if (t != 0.0f) add_i64(&cq[c2 + (long long)nb_dx(k) * T.ny + nb_dy(k)].hq, shy_q32(t));
+  }
+  if (moved) add_i64(&cq[c2].hq, shy_q32(hcv - h0));
+}
+
 __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
+  extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ Terrain sT[kSmemTerrains];
+  __shared__ int s_nq;                  // steep cascades queued this step
+  __shared__ unsigned long long s_live;  // drops still descending
   const bool smem_t = a.n_terrains <= kSmemTerrains;
   if (smem_t)
     for (int i = threadIdx.x; i < a.n_terrains; i += blockDim.x) sT[i] = a.terrains[i];
+  if (threadIdx.x == 0) s_nq = 0;
   __syncthreads();
   const Terrain* TT = smem_t ? sT : a.terrains;
 
-  const long long G = (long long)gridDim.x * blockDim.x;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // this CTA's drop slots: [lo, hi), at most `cap` of them
+  const long long lo = (long long)blockIdx.x * a.total_drops / gridDim.x;
+  const long long hi = (long long)(blockIdx.x + 1) * a.total_drops / gridDim.x;
+  const int nd = (int)(hi - lo);
+  const int cap = (int)(((long long)a.total_drops + gridDim.x - 1) / gridDim.x);
+  const Slots S = slots_of(a, s_dyn, lo, cap);
+
   const shy_params& P = a.P;
   const unsigned long long cycle = a.bar->cycle;
   const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
@@ -224,58 +366,61 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
   unsigned long long n_steps = 0, n_oob = 0, n_drops = 0, n_skipped = 0;
   long long gain_q = 0, loss_q = 0;
   const shy_evap ev = a.ev;
+  const int vmax = (int)P.max_age + 2;  // last entry of the volume table
 
   // spawn (source/world.h:64-74)
   unsigned long long born = 0;
-  for (long long d = tid; d < a.total_drops; d += G) {
+  for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+    const long long d = lo + j;
     const int t = find_terrain(TT, a.n_terrains, (int)d);
     const Terrain T = TT[t];
     int x, y;
     shy_spawn_xy(T.seed, cycle, (unsigned)(d - T.drop_base), T.nx, T.ny, &x, &y);
     const long long c = T.cell_base + (long long)x * T.ny + y;
-    a.terr[d] = t;
-    a.cell[d] = -1;
-    a.ctr[d] = -1;
+    S.terr[j] = t;
+    S.cell[j] = -1;
+    S.ctr[j] = -1;
     // world.h:71; no float lies between 0.1 and 0.1f, so this is h < 0.1
     if (a.h[c] < 0.1f) {
-      a.age[d] = -1;
+      S.age[j] = -1;
       ++n_skipped;
       continue;
     }
     ++n_drops;
     ++born;
-    a.age[d] = 0;
-    a.pos[d] = make_float2((float)x, (float)y);
-    a.spd[d] = make_float2(0.0f, 0.0f);
-    a.vs[d] = make_float2(1.0f, 0.0f);
-    a.gain[d] = 0;
+    S.age[j] = 0;
+    S.pos[j] = make_float2((float)x, (float)y);
+    S.spd[j] = make_float2(0.0f, 0.0f);
+    S.vs[j] = make_float2(1.0f, 0.0f);
+    S.gain[j] = 0;
     atomicAdd(&a.cq[c].cnt[0], 1);
   }
   {
     const unsigned long long s = block_sum_u64(born);
     if (threadIdx.x == 0 && s) atomicAdd(&a.bar->live, s);
   }
-  bool ok = grid_barrier(a.bar, passed);
+  bool ok = grid_barrier(a.bar, passed, &s_live);
 
   int step = 0;
   for (; ok && step < a.max_steps; ++step) {
-    if (*((volatile unsigned long long*)&a.bar->live) == 0) break;
+    if (s_live == 0) break;
     const int par = step & 1;
     lap(5);
 
-    // ---- phase A: one descend step per live drop ----
-    for (long long d = tid; d < a.total_drops; d += G) {
-      const int ag = a.age[d];
-      const int ti = a.terr[d];
-      float2 p = a.pos[d], s = a.spd[d], v = a.vs[d];
-      long long gn = a.gain[d];
+    // ---- descend: one Drop::descend step per live drop ----
+    if (threadIdx.x == 0) s_nq = 0;  // everyone read it before the last barrier
+    for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+      const int ag = S.age[j];
       if (ag < 0) continue;
+      const int ti = S.terr[j];
+      float2 p = S.pos[j], s = S.spd[j], v = S.vs[j];
+      long long gn = S.gain[j];
       const Terrain T = TT[ti];
       const CellQ* RT = a.cq + T.cell_base;
       const int ix = (int)p.x, iy = (int)p.y;
       const long long lc = (long long)ix * T.ny + iy;
       const long long c = T.cell_base + lc;
-      a.cell[d] = c;
+      S.cell[j] = c;
       // the five heights quad::_normal reads (0 outside the map)
       const bool xp = ix + 1 < T.nx, xm = ix > 0, yp = iy + 1 < T.ny, ym = iy > 0;
       // all loads issued together; a neighbour outside the map reads the
@@ -288,6 +433,7 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
       long long qym = RT[ym ? lc - 1 : lc].hq;
       const float4 r = __ldg(&a.rec[c]);
       const float ed = __ldg(&a.effd[c]);
+      const float vnext = __ldg(&a.voltab[ag + 1 < vmax ? ag + 1 : vmax]);
       qxp = xp ? qxp : 0;
       qxm = xm ? qxm : 0;
       qyp = yp ? qyp : 0;
@@ -298,10 +444,10 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
       if ((float)ag > P.max_age || v.x < P.min_vol) {  // water.h:74-83
         const long long dep = shy_q32(v.y);
         add_i64(&a.cq[c].e, dep);
-        a.own[d] = dep;
+        S.own[j] = dep;
         gain_q += gn;
-        a.age[d] = -2;
-        a.ctr[d] = -1;
+        S.age[j] = -2;
+        S.ctr[j] = -1;
         continue;
       }
       ++n_steps;
@@ -345,52 +491,43 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
       v.y += ex;
       const long long de = -shy_q32(ex);
       add_i64(&a.cq[c].e, de);
-      a.own[d] = de;
+      S.own[j] = de;
       const float s0 = v.y;  // water.h:135-136, without the FP64 unit
       v.y = shy_evap_div(v.y, &ev);
-      v.x = __ldg(&a.voltab[ag + 1]);
+      v.x = vnext;
       gn += shy_q32(v.y - s0);  // exact difference (Sterbenz)
       if (out) {  // water.h:139-142
         ++n_oob;
         loss_q += shy_q32(v.y);
         gain_q += gn;
-        a.age[d] = -2;
-        a.ctr[d] = -1;
+        S.age[j] = -2;
+        S.ctr[j] = -1;
         continue;
       }
-      a.ctr[d] = arrived_before == 0 ? c2 : -1;  // World::cascade(pos), water.h:151
-      a.age[d] = ag + 1;
-      a.pos[d] = p;
-      a.spd[d] = s;
-      a.vs[d] = v;
-      a.gain[d] = gn;
+      S.ctr[j] = arrived_before == 0 ? c2 : -1;  // World::cascade(pos), water.h:151
+      S.age[j] = ag + 1;
+      S.pos[j] = p;
+      S.spd[j] = s;
+      S.vs[j] = v;
+      S.gain[j] = gn;
     }
     lap(0);
-    if (!grid_barrier(a.bar, passed)) { ok = false; break; }
+    if (!grid_barrier(a.bar, passed, nullptr)) { ok = false; break; }
     lap(1);
 
-    // ---- phase C: World::cascade at each claimed cell ----
-    // C1: each cascade computes the nine heights it works on; most move
-    // nothing (no neighbour starts with excess) and are settled here.  The
-    // steep ones go to a queue, which C2 works through one cell per warp after
-    // a barrier, so that no warp carries more than its share of them.
-    long long sq_c2 = 0;
-    int sq_ti = 0, sq_ix = 0, sq_iy = 0;
-    float sq_h0 = 0.0f, sq_v[8];
-    for (long long d0 = tid - (threadIdx.x & 31); d0 < a.total_drops; d0 += G) {
-      // warp-uniform loop, so that the warp can take queue slots together
-      const int lane = threadIdx.x & 31;
-      const long long d = d0 + lane;
-      const long long c2 = d < a.total_drops ? a.ctr[d] : -1;
-      const int ti = d < a.total_drops ? a.terr[d] : 0;
-      bool steep = false;
-      if (c2 >= 0) {
+    // ---- scan: the nine heights of each claimed cascade ----
+    // heights after phase descend: fixed point plus the step's erosion.  All
+    // nine loads are issued together: a neighbour outside the map reads the
+    // centre instead and is masked out.  The centre only changes through a
+    // transfer, so without any excess to begin with the sequential loop moves
+    // nothing and the cascade ends here.
+    for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+      const long long c2 = S.ctr[j];
+      if (c2 < 0) continue;
+      const int ti = S.terr[j];
       const Terrain T = TT[ti];
       const int lc = (int)(c2 - T.cell_base);  // < 2^31 cells per terrain
       const int ix = lc / T.ny, iy = lc - ix * T.ny;
-      // heights after phase A: fixed point plus the step's erosion.  All nine
-      // loads are issued together: a neighbour outside the map reads the
-      // centre instead and is masked out.
       longlong2 nv[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
@@ -404,8 +541,6 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
         sh[k] = oob(ix + nb_dx(k), iy + nb_dy(k), T.nx, T.ny) ? __int_as_float(0x7f800000)  // never used
                                                               : shy_unq(nv[k].x + nv[k].y);
       const float h0 = shy_unq(v0.x + v0.y);
-      // the centre only changes through a transfer, so without any excess to
-      // begin with the sequential loop moves nothing
       bool any = false;
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
@@ -414,155 +549,46 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
         const float excess = sh[k] >= 0.1f ? fabsf(diff) - dist * P.max_diff : fabsf(diff);
         any |= (sh[k] < __int_as_float(0x7f800000)) && diff != 0.0f && excess > 0.0f;
       }
-      a.cmask[d] = 0;
-      steep = any;
       if (any) {
-        // keep what the queue entry needs until the warp has its slots
-        sq_c2 = c2; sq_ti = ti; sq_ix = ix; sq_iy = iy; sq_h0 = h0;
+        // one claim per drop slot, so the queue (cap entries) cannot overflow
+        SteepCell& q = S.steep[atomicAdd(&s_nq, 1)];
+        q.c2 = c2;
+        q.ti = ti;
+        q.ix = ix;
+        q.iy = iy;
+        q.h0 = h0;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) sq_v[k] = sh[k];
-      }
-      }
-      const unsigned bal = __ballot_sync(0xffffffffu, steep);
-      if (bal) {
-        unsigned base = 0;
-        if (lane == __ffs(bal) - 1) base = atomicAdd(&a.bar->steep, (unsigned)__popc(bal));
-        base = __shfl_sync(0xffffffffu, base, __ffs(bal) - 1);
-        if (steep) {
-          SteepCell& q = a.steep[base + __popc(bal & ((1u << lane) - 1u))];
-          q.c2 = sq_c2;
-          q.d = (int)d;
-          q.ti = sq_ti;
-          q.ix = sq_ix;
-          q.iy = sq_iy;
-          q.h0 = sq_h0;
-#pragma unroll
-          for (int k = 0; k < 8; ++k) q.v[k] = sq_v[k];
-        }
+        for (int k = 0; k < 8; ++k) q.v[k] = sh[k];
       }
     }
     lap(2);
-    if (!grid_barrier(a.bar, passed)) { ok = false; break; }
-
-    // C2: the steep cascades, each by one whole warp
-    {
-      const int lane = threadIdx.x & 31;
-      const unsigned nsteep = *((volatile unsigned*)&a.bar->steep);
-      const long long warp = tid >> 5, nwarps = G >> 5;
-      for (long long i = warp; i < nsteep; i += nwarps) {
-        const SteepCell& qc = a.steep[i];
-        const long long sc2 = qc.c2;
-        const int six = qc.ix, siy = qc.iy;
-        const float sh0 = qc.h0;
-        const Terrain T = TT[qc.ti];
-        float v[8];
-        int sk[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          v[k] = qc.v[k];
-          sk[k] = k;
-        }
-        // cascade centres of this step in the 5 x 5 block (cells a drop moved
-        // to): lane l looks at (dx, dy) = (l / 5 - 2, l % 5 - 2); bit l
-        bool is_c = false;
-        {
-          const int dx = lane < 25 ? lane / 5 - 2 : 0, dy = lane < 25 ? lane % 5 - 2 : 0;
-          const bool in = lane < 25 && !oob(six + dx, siy + dy, T.nx, T.ny);
-          const int cv = a.cq[in ? sc2 + (long long)dx * T.ny + dy : sc2].cnt[par ^ 1];
-          is_c = in && cv > 0;
-        }
-        const unsigned cen = __ballot_sync(0xffffffffu, is_c);
-        // cascades whose 3 x 3 block holds cell (dx, dy): popcount of a window
-        auto cover = [&](int dx, int dy) {
-          const unsigned row = 7u << (dy + 1);  // 3 bits centred on dy
-          const unsigned win = (row << (5 * (dx + 1))) | (row << (5 * (dx + 2))) | (row << (5 * (dx + 3)));
-          return __popc(cen & win);
-        };
-        unsigned kv = 0;  // 4 bits per neighbour
-#pragma unroll
-        for (int k = 0; k < 8; ++k) kv |= (unsigned)cover(nb_dx(k), nb_dy(k)) << (4 * k);
-        const int kc = cover(0, 0);
-        sort8(v, sk);
-        // the reference's sequential loop (every lane, same values)
-        float hcv = sh0;
-        float tr[8];
-        int mask = 0;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          tr[j] = 0.0f;
-          if (!(v[j] < __int_as_float(0x7f800000))) continue;
-          const float diff = hcv - v[j];
-          if (diff == 0.0f) continue;
-          const int k = sk[j];
-          const float dist = (nb_dx(k) != 0 && nb_dy(k) != 0) ? sqrtf(2.0f) : 1.0f;
-          // h > 0.1 in double is h >= 0.1f in float (no float lies between)
-          const float excess = v[j] >= 0.1f ? fabsf(diff) - dist * P.max_diff : fabsf(diff);
-          if (excess <= 0.0f) continue;
-          const int kn = (int)((kv >> (4 * k)) & 15u);
-          const int kk = kc > kn ? kc : kn;
-          float transfer = P.settling * excess / 2.0f;
-          if (kk > 1) transfer = transfer / (float)kk;
-          if (diff > 0.0f) {
-            hcv -= transfer;
-            tr[j] = transfer;
-          } else {
-            hcv += transfer;
-            tr[j] = -transfer;
-          }
-          mask |= 1 << k;
-        }
-        if (mask) mask |= 256;
-        // the fixed-point sums: lane j < 8 the j-th sorted neighbour, lane 8
-        // the centre
-        float t = 0.0f;
-        int kt = 0;
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-          if (lane == j) {
-            t = tr[j];
-            kt = sk[j];
-          }
-        if (lane < 8 && t != 0.0f)
-          add_i64(&a.cq[sc2 + (long long)nb_dx(kt) * T.ny + nb_dy(kt)].q, shy_q32(t));
-        if (lane == 8 && mask) add_i64(&a.cq[sc2].q, shy_q32(hcv - sh0));
-        if (lane == 0) a.cmask[qc.d] = mask;
-      }
-    }
-    lap(2);
-    if (!grid_barrier(a.bar, passed)) { ok = false; break; }
+    if (!grid_barrier(a.bar, passed, nullptr)) { ok = false; break; }
     lap(3);
 
-    // ---- phase D: apply, reset counts, retire ----
-    if (tid == 0) a.bar->steep = 0;
-    // Every drop adds its own erosion to its cell's fixed-point height; the
-    // cascades add what they moved.  All integer additions, so the order
-    // does not matter.
+    // ---- settle: steep cascades, each drop's own change, retirements ----
+    // Every addition here is an integer atomic on a fixed-point height that
+    // nobody reads in this phase, so the order does not matter.
+    {
+      const int nq = s_nq;
+      for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+        const SteepCell qc = S.steep[i];
+        settle_cascade(qc, TT[qc.ti], a.cq, par, P);
+      }
+    }
     unsigned long long retired = 0;
-    for (long long d = tid; d < a.total_drops; d += G) {
-      const int ag = a.age[d];
-      const long long c = a.cell[d];
-      const long long c2 = a.ctr[d];
-      const long long own = a.own[d];
-      const int ti = a.terr[d];
-      const int m = c2 >= 0 ? a.cmask[d] : 0;
+    for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+      const int ag = S.age[j];
       if (ag == -1) continue;
+      const long long c = S.cell[j];
       if (c >= 0) {
+        const long long own = S.own[j];
         if (own != 0) add_i64(&a.cq[c].hq, own);
         a.cq[c].e = 0;
         a.cq[c].cnt[par] = 0;
       }
-      if (m) {  // the cells its cascade changed
-        const Terrain T = TT[ti];
-        for (int k = 0; k < 9; ++k) {
-          if (!(m & (1 << (k == 8 ? 8 : k)))) continue;
-          const long long x = k == 8 ? c2 : c2 + (long long)nb_dx(k) * T.ny + nb_dy(k);
-          const long long q = (long long)atomicExch((unsigned long long*)&a.cq[x].q, 0ull);
-          if (q != 0) add_i64(&a.cq[x].hq, q);
-        }
-      }
       if (ag == -2) {
-        a.age[d] = -1;
-        a.cell[d] = -1;
+        S.age[j] = -1;
+        S.cell[j] = -1;
         ++retired;
       }
     }
@@ -571,7 +597,7 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
       if (threadIdx.x == 0 && s) atomicAdd(&a.bar->live, (unsigned long long)(-(long long)s));
     }
     lap(4);
-    if (!grid_barrier(a.bar, passed)) { ok = false; break; }
+    if (!grid_barrier(a.bar, passed, &s_live)) { ok = false; break; }
   }
   lap(5);
 
@@ -625,7 +651,6 @@ __global__ void cycle_end_kernel(Tracks* __restrict__ trk, float4* __restrict__ 
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     bar->arrive = 0;
     bar->live = 0;
-    bar->steep = 0;
     bar->cycle += 1;
     st->cycles += 1;
   }
@@ -702,6 +727,53 @@ int batched_max_grid(shy_world* w, int block) {
   return per_sm * w->sm_count;
 }
 
+namespace {
+
+// Launches one lock-step cycle.  The grid is the resident CTAs per SM times
+// the SMs (fewer for small cycles: at least 32 drops per CTA); each CTA's
+// drop slots go to shared memory when they fit without lowering that
+// occupancy, else to the global arrays in `a`.
+cudaError_t launch_lockstep(LockArgs& a, int sm_count, int grid_hint, cudaStream_t stream) {
+  int dev = 0, optin = 0, per0 = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  if ((e = cudaFuncGetAttributes(&fa, lockstep_kernel)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, lockstep_kernel, kLockBlock, 0)) != cudaSuccess)
+    return e;
+  if (per0 < 1) return cudaErrorLaunchOutOfResources;
+  const long long max_dyn = (long long)optin - (long long)fa.sharedSizeBytes;
+  long long want = ((long long)a.total_drops + 31) / 32;
+  if (want < 1) want = 1;
+  if (grid_hint > 0 && want > grid_hint) want = grid_hint;
+
+  const long long g = (long long)per0 * sm_count < want ? (long long)per0 * sm_count : want;
+  const int grid = (int)g;
+  const long long b = (((long long)a.total_drops + g - 1) / g) * kSlotBytes;
+  size_t bytes = 0;
+  a.smem_slots = 0;
+  if (b <= max_dyn) {
+    if (b > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(lockstep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b)) !=
+            cudaSuccess)
+      return e;
+    int per = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lockstep_kernel, kLockBlock, (size_t)b)) !=
+        cudaSuccess)
+      return e;
+    if ((long long)per * sm_count >= g) {  // the slots fit without costing occupancy
+      a.smem_slots = 1;
+      bytes = (size_t)b;
+    }
+  }
+  void* args[] = {&a};
+  return cudaLaunchCooperativeKernel((const void*)lockstep_kernel, dim3(grid), dim3(kLockBlock), args, bytes,
+                                     stream);
+}
+
+}  // namespace
+
 cudaError_t launch_batched_cycle(shy_world* w) {
   LockArgs a;
   a.terrains = w->dterrains;
@@ -725,25 +797,17 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.terr = w->dterr;
   a.cell = w->dcell;
   a.ctr = w->dctr;
-  a.cmask = w->dcmask;
   a.steep = w->dsteep;
+  a.smem_slots = 0;
   a.P = w->P;
   a.st = w->stats;
   a.bar = w->bar;
   a.max_steps = (int)w->P.max_age + 3;
 
-  int grid = w->batch_grid;
-  const int maxg = batched_max_grid(w, kLockBlock);
-  const int need = (a.total_drops + kLockBlock - 1) / kLockBlock;
-  if (grid <= 0 || grid > maxg) grid = maxg;
-  if (grid > need) grid = need < 1 ? 1 : need;
-  void* args[] = {&a};
   int slot = -1;
   cudaError_t e = timing_begin(w, SHY_KERNEL_DROPS, &slot);
   if (e != cudaSuccess) return e;
-  e = cudaLaunchCooperativeKernel((const void*)lockstep_kernel, dim3(grid), dim3(kLockBlock), args, 0,
-                                  w->stream);
-  if (e != cudaSuccess) return e;
+  if ((e = launch_lockstep(a, w->sm_count, w->batch_grid, w->stream)) != cudaSuccess) return e;
   if ((e = timing_end(w, slot)) != cudaSuccess) return e;
 
   if ((e = timing_begin(w, SHY_KERNEL_APPLY, &slot)) != cudaSuccess) return e;
@@ -791,20 +855,13 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.terr = b.terr;
   a.cell = b.cell;
   a.ctr = b.ctr;
-  a.cmask = b.cmask;
   a.steep = b.steep;
+  a.smem_slots = 0;
   a.P = b.P;
   a.st = b.st;
   a.bar = b.bar;
   a.max_steps = (int)b.P.max_age + 3;
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lockstep_kernel, kLockBlock, 0);
-  if (e != cudaSuccess) return e;
-  int grid = per_sm * b.sm_count;
-  const int need = (b.total_drops + kLockBlock - 1) / kLockBlock;
-  if (grid > need) grid = need < 1 ? 1 : need;
-  void* args[] = {&a};
-  e = cudaLaunchCooperativeKernel((const void*)lockstep_kernel, dim3(grid), dim3(kLockBlock), args, 0, stream);
+  cudaError_t e = launch_lockstep(a, b.sm_count, 0, stream);
   if (e != cudaSuccess) return e;
   cycle_end_kernel<<<cells_grid(b.cells), 256, 0, stream>>>(b.trk, b.rec, b.track_f, b.cq, b.h, b.cells, b.P,
                                                             b.bar, b.st);

@@ -27,7 +27,7 @@ struct NoallocScratch {
   float2 pos[SHY_NOALLOC_MAX_DROPS], spd[SHY_NOALLOC_MAX_DROPS], vs[SHY_NOALLOC_MAX_DROPS];
   long long gain[SHY_NOALLOC_MAX_DROPS], own[SHY_NOALLOC_MAX_DROPS];
   long long cell[SHY_NOALLOC_MAX_DROPS], ctr[SHY_NOALLOC_MAX_DROPS];
-  int age[SHY_NOALLOC_MAX_DROPS], terr[SHY_NOALLOC_MAX_DROPS], cmask[SHY_NOALLOC_MAX_DROPS];
+  int age[SHY_NOALLOC_MAX_DROPS], terr[SHY_NOALLOC_MAX_DROPS];
   Terrain terrain;
   GridBar bar;
   DevStats st;
@@ -86,7 +86,7 @@ __global__ void noalloc_pack_kernel(NoallocScratch* s, int n, float* h, const fl
     CellQ c;
     c.hq = q;
     c.e = 0;
-    c.q = 0;
+    c.pad = 0;
     c.cnt[0] = 0;
     c.cnt[1] = 0;
     s->cq[i] = c;
@@ -186,7 +186,6 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
   b.terr = sc->terr;
   b.cell = sc->cell;
   b.ctr = sc->ctr;
-  b.cmask = sc->cmask;
   b.steep = sc->steep;
   b.st = &sc->st;
   b.bar = &sc->bar;

@@ -97,7 +97,7 @@ void free_world(shy_world* w) {
   if (!w) return;
   if (w->stream) cudaStreamSynchronize(w->stream);
   void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
-                  w->dterr, w->dcell, w->dctr, w->dcmask, w->dterrains, w->stats, w->bar, w->ddrop,
+                  w->dterr, w->dcell, w->dctr, w->dterrains, w->stats, w->bar, w->ddrop,
                   w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down,
                   w->plant_next, w->rootq, w->veg_claim};
   for (void* p : ptrs)
@@ -114,13 +114,13 @@ void free_world(shy_world* w) {
 
 int alloc_drop_slots(shy_world* w, int n) {
   if (n <= w->max_drops) return SHY_OK;
-  void* ptrs[] = {w->dpos, w->dspd, w->dvs, w->dage, w->dgain, w->dterr, w->dcell, w->dctr, w->dcmask, w->down,
+  void* ptrs[] = {w->dpos, w->dspd, w->dvs, w->dage, w->dgain, w->dterr, w->dcell, w->dctr, w->down,
                   w->dsteep};
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
   for (void* p : ptrs)
     if (p) cudaFree(p);
   w->dpos = w->dspd = w->dvs = nullptr;
-  w->dage = w->dterr = w->dcmask = nullptr;
+  w->dage = w->dterr = nullptr;
   w->dgain = w->down = nullptr;
   w->dsteep = nullptr;
   w->dcell = w->dctr = nullptr;
@@ -133,7 +133,6 @@ int alloc_drop_slots(shy_world* w, int n) {
   SHY_CHECK_CUDA(dalloc(&w->dterr, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dcell, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dctr, n), "allocate drop slots");
-  SHY_CHECK_CUDA(dalloc(&w->dcmask, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->down, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dsteep, n), "allocate drop slots");
   w->max_drops = n;
