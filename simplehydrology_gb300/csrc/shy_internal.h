@@ -48,13 +48,17 @@ struct DevStats {
   double gain_exact, loss_exact;  // exact (sequential) mode
 };
 
-// A cascade of the current step that will move height: its centre and the
-// nine heights it starts from.
+// A cascade of the current step that will move height: its centre, the
+// nine heights it starts from and the overlap counts of its 3 x 3 block
+// (cascades of the step whose blocks hold the cell: the centre's, and 4 bits
+// per neighbour).
 struct alignas(16) SteepCell {
   long long c2;
-  int ti, ix, iy;
+  int ti;
   float h0;
   float v[8];
+  unsigned kv;
+  int kc;
 };
 
 // Grid barrier state of the persistent lock-step kernel.

@@ -84,11 +84,11 @@ __device__ __forceinline__ void add_i64(long long* p, long long v) {
 // whole CTA.  Every wait is bounded: past kBarrierLimitNs the waiter sets
 // bar->abort and every later barrier returns false at once, so the kernel
 // always ends.
-__device__ bool grid_barrier(GridBar* bar, unsigned long long& passed, unsigned long long* live) {
+__device__ bool grid_barrier(GridBar* bar, unsigned& passed, unsigned long long* live) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned long long target = (passed + 1) * (unsigned long long)gridDim.x;
+    const unsigned long long target = (unsigned long long)(passed + 1) * gridDim.x;
     red_release_add_u64(&bar->arrive, 1ull);
     int ok = 1;
     unsigned long long t0 = 0;
@@ -260,24 +260,13 @@ __device__ __forceinline__ longlong2 hq_e(const CellQ* c) {
   return *reinterpret_cast<const longlong2*>(c);
 }
 
-// World::cascade's transfer loop (source/world.h:127-165) for one queued
-// centre: the neighbours in the reference's stable height order, the live
-// centre height, each transfer divided by the overlap count of its pair.
-// Transfers go straight to the fixed-point heights.
-__device__ __forceinline__ void settle_cascade(const SteepCell& qc, const Terrain& T, CellQ* cq, int par,
-                                               const shy_params& P) {
-  const long long c2 = qc.c2;
-  const int ix = qc.ix, iy = qc.iy;
-  // cascade centres of this step in the 5 x 5 block (cells a drop moved to):
-  // bit l for (dx, dy) = (l / 5 - 2, l % 5 - 2); a cell outside the map reads
-  // the centre and is masked out
-  int cv[25];
-#pragma unroll
-  for (int l = 0; l < 25; ++l) {
-    const int dx = l / 5 - 2, dy = l % 5 - 2;
-    const bool in = !oob(ix + dx, iy + dy, T.nx, T.ny);
-    cv[l] = cq[in ? c2 + (long long)dx * T.ny + dy : c2].cnt[par ^ 1];
-  }
+// Overlap counts of a claimed cascade: the cascade centres of this step in the
+// 5 x 5 block around it (cells a drop moved to) give, for the centre and each
+// of its 8 neighbours, how many cascades' 3 x 3 blocks hold that cell.  The
+// arrivals are loaded by the caller (cv[l] for (dx, dy) = (l / 5 - 2,
+// l % 5 - 2), any value outside the map).
+__device__ __forceinline__ void overlap_counts(const int* cv, int ix, int iy, const Terrain& T, unsigned& kv,
+                                               int& kc) {
   unsigned cen = 0;
 #pragma unroll
   for (int l = 0; l < 25; ++l) {
@@ -289,9 +278,23 @@ __device__ __forceinline__ void settle_cascade(const SteepCell& qc, const Terrai
   auto cover = [&](int dx, int dy) {
     const unsigned row = 7u << (dy + 1);  // 3 bits centred on dy
     const unsigned win = (row << (5 * (dx + 1))) | (row << (5 * (dx + 2))) | (row << (5 * (dx + 3)));
-    return __popc(cen & win);
+    return (unsigned)__popc(cen & win);
   };
-  const int kc = cover(0, 0);
+  kv = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) kv |= cover(nb_dx(k), nb_dy(k)) << (4 * k);
+  kc = (int)cover(0, 0);
+}
+
+// World::cascade's transfer loop (source/world.h:127-165) for one queued
+// centre: the neighbours in the reference's stable height order, the live
+// centre height, each transfer divided by the overlap count of its pair.
+// Everything that does not depend on the live centre height is computed
+// before the sequential loop.  Transfers go straight to the fixed-point
+// heights.
+__device__ __forceinline__ void settle_cascade(const SteepCell& qc, const Terrain& T, CellQ* cq,
+                                               const shy_params& P) {
+  const long long c2 = qc.c2;
   float v[8];
   int sk[8];
 #pragma unroll
@@ -300,38 +303,51 @@ __device__ __forceinline__ void settle_cascade(const SteepCell& qc, const Terrai
     sk[k] = k;
   }
   sort8(v, sk);
+  // per sorted neighbour: in the map, excess threshold, overlap divisor
+  float thr[8];
+  int kk[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int k = sk[j];
+    const float dist = (nb_dx(k) != 0 && nb_dy(k) != 0) ? sqrtf(2.0f) : 1.0f;
+    // h > 0.1 in double is h >= 0.1f in float (no float lies between);
+    // |diff| - 0 is |diff| exactly
+    thr[j] = v[j] >= 0.1f ? dist * P.max_diff : 0.0f;
+    const int kn = (int)((qc.kv >> (4 * k)) & 15u);
+    kk[j] = qc.kc > kn ? qc.kc : kn;
+  }
   const float h0 = qc.h0;
   float hcv = h0;
+  float tr[8];
   bool moved = false;
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
+    tr[j] = 0.0f;
     if (!(v[j] < __int_as_float(0x7f800000))) continue;  // outside the map
     const float diff = hcv - v[j];
     if (diff == 0.0f) continue;
-    const int k = sk[j];
-    const float dist = (nb_dx(k) != 0 && nb_dy(k) != 0) ? sqrtf(2.0f) : 1.0f;
-    // h > 0.1 in double is h >= 0.1f in float (no float lies between)
-    const float excess = v[j] >= 0.1f ? fabsf(diff) - dist * P.max_diff : fabsf(diff);
+    const float excess = fabsf(diff) - thr[j];
     if (excess <= 0.0f) continue;
-    const int kn = cover(nb_dx(k), nb_dy(k));
-    const int kk = kc > kn ? kc : kn;
     float transfer = P.settling * excess / 2.0f;
-    if (kk > 1) transfer = transfer / (float)kk;
-    float t;
+    if (kk[j] > 1) transfer = transfer / (float)kk[j];
     if (diff > 0.0f) {
       hcv -= transfer;
-      t = transfer;
+      tr[j] = transfer;
     } else {
       hcv += transfer;
-      t = -transfer;
+      tr[j] = -transfer;
     }
     moved = true;
-    if (t != 0.0f) add_i64(&cq[c2 + (long long)nb_dx(k) * T.ny + nb_dy(k)].hq, shy_q32(t));
   }
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    if (tr[j] != 0.0f)
+      add_i64(&cq[c2 + (long long)nb_dx(sk[j]) * T.ny + nb_dy(sk[j])].hq, shy_q32(tr[j]));
   if (moved) add_i64(&cq[c2].hq, shy_q32(hcv - h0));
 }
 
-__global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
+// 128 registers: two 256-thread CTAs per SM
+__global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ Terrain sT[kSmemTerrains];
   __shared__ int s_nq;                  // steep cascades queued this step
@@ -352,18 +368,23 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
 
   const shy_params& P = a.P;
   const unsigned long long cycle = a.bar->cycle;
+  // phase clock of CTA 0's thread 0, kept in shared memory so that the other
+  // threads hold no registers for it
+  __shared__ unsigned long long s_ph[7];  // 6 phases + the last stamp
   const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
-  unsigned long long ph[6] = {0, 0, 0, 0, 0, 0};
-  unsigned long long tprev = timer ? global_ns() : 0;
+  if (timer) {
+    for (int i = 0; i < 6; ++i) s_ph[i] = 0;
+    s_ph[6] = global_ns();
+  }
   auto lap = [&](int i) {
     if (timer) {
       const unsigned long long t = global_ns();
-      ph[i] += t - tprev;
-      tprev = t;
+      s_ph[i] += t - s_ph[6];
+      s_ph[6] = t;
     }
   };
-  unsigned long long passed = 0;
-  unsigned long long n_steps = 0, n_oob = 0, n_drops = 0, n_skipped = 0;
+  unsigned passed = 0;
+  unsigned n_steps = 0, n_oob = 0, n_drops = 0, n_skipped = 0;  // this thread's, per cycle
   long long gain_q = 0, loss_q = 0;
   const shy_evap ev = a.ev;
   const int vmax = (int)P.max_age + 2;  // last entry of the volume table
@@ -515,7 +536,7 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
     if (!grid_barrier(a.bar, passed, nullptr)) { ok = false; break; }
     lap(1);
 
-    // ---- scan: the nine heights of each claimed cascade ----
+    // ---- scan: the nine heights and the overlap counts of each claimed cascade ----
     // heights after phase descend: fixed point plus the step's erosion.  All
     // nine loads are issued together: a neighbour outside the map reads the
     // centre instead and is masked out.  The centre only changes through a
@@ -535,6 +556,15 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
         nv[k] = hq_e(&a.cq[in ? c2 + (long long)nb_dx(k) * T.ny + nb_dy(k) : c2]);
       }
       const longlong2 v0 = hq_e(&a.cq[c2]);
+      // this step's arrivals in the 5 x 5 block, loaded with the heights so
+      // that a steep cascade needs no further load (most are not steep)
+      int cv[25];
+#pragma unroll
+      for (int l = 0; l < 25; ++l) {
+        const int dx = l / 5 - 2, dy = l % 5 - 2;
+        const bool in = !oob(ix + dx, iy + dy, T.nx, T.ny);
+        cv[l] = a.cq[in ? c2 + (long long)dx * T.ny + dy : c2].cnt[par ^ 1];
+      }
       float sh[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k)
@@ -551,14 +581,17 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
       }
       if (any) {
         // one claim per drop slot, so the queue (cap entries) cannot overflow
+        unsigned kv;
+        int kc;
+        overlap_counts(cv, ix, iy, T, kv, kc);
         SteepCell& q = S.steep[atomicAdd(&s_nq, 1)];
         q.c2 = c2;
         q.ti = ti;
-        q.ix = ix;
-        q.iy = iy;
         q.h0 = h0;
 #pragma unroll
         for (int k = 0; k < 8; ++k) q.v[k] = sh[k];
+        q.kv = kv;
+        q.kc = kc;
       }
     }
     lap(2);
@@ -572,7 +605,7 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
       const int nq = s_nq;
       for (int i = threadIdx.x; i < nq; i += blockDim.x) {
         const SteepCell qc = S.steep[i];
-        settle_cascade(qc, TT[qc.ti], a.cq, par, P);
+        settle_cascade(qc, TT[qc.ti], a.cq, P);
       }
     }
     unsigned long long retired = 0;
@@ -614,7 +647,7 @@ __global__ void __launch_bounds__(kLockBlock) lockstep_kernel(LockArgs a) {
     if (threadIdx.x == 0 && v) atomicAdd((unsigned long long*)&a.st->loss_q, v);
   }
   if (timer) {
-    for (int i = 0; i < 6; ++i) a.bar->phase_ns[i] += ph[i];
+    for (int i = 0; i < 6; ++i) a.bar->phase_ns[i] += s_ph[i];
     a.bar->iterations += (unsigned long long)step;
     if (ok && a.bar->live != 0) atomicCAS(&a.bar->error, 0, SHY_ERR_STATE);
   }
