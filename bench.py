@@ -9,12 +9,25 @@ scatter, lrate blend and cascade.  One step = one erosion cycle
 dataset; the terrain recipe stands in for the reference's FastNoiseLite map.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload plain|batch]
 
 `value` is device throughput with the maps resident in HBM; between timed
 steps the L2 is flushed by writing a 256 MiB buffer (untimed).  `e2e` is the
 same metric through the C ABI with the world state (height, discharge,
 momentum) copied in from pinned host memory and back out every step.  The
 reference arm runs the reference's sequential erosion on the host cores.
+
+`roofline` takes the lock-step kernel's algorithmic bytes (72 B per
+drop-step) against the HBM copy peak; `roofline_l2` takes the same bytes, and
+4 integer atomics per drop-step, against the L2 peaks the library measures
+on the GPU at hand (shy_measure_l2), which bound the kernel while a
+terrain's cell state fits in L2.  `cycle_gbs` adds the 80 B per cell of the
+end-of-cycle pass over the whole step time.
+
+`--workload batch` runs the batched-terrain configuration instead: 64
+terrains, sides log-uniform in [128, 1024], 0.25 drops per cell per cycle,
+one lock-step launch per cycle; with N ranks each erodes a disjoint share of
+whole terrains.
 """
 from __future__ import annotations
 
@@ -157,33 +170,125 @@ def cpu_baseline_sample(seconds=10.0):
             "sample": f"{drops} drops of World::erode on the 1024^2 terrain ({steps} drop-steps, {dt:.1f} s, 1 thread)"}
 
 
+class PlainWorkload:
+    """One terrain: the 1024^2 / 65,536-drop configuration (or a smaller
+    profiling case).  One step = one World::erode(drops) cycle."""
+
+    def __init__(self, shy, n, drops):
+        self.w = shy.World(n, n, seed=SEED)
+        self.w.generate(SEED, 8)
+        self.h0 = self.w.get_field("height")
+        self.zero = self.h0 * 0.0
+        self.drops = drops
+        self.cells = n * n
+        self.config = {"workload": WORKLOAD if (n, drops) == (1024, 65536) else
+                       f"profiling case: {n}x{n} value-noise terrain, {drops} drops/cycle",
+                       "map": [n, n], "drops_per_cycle": drops}
+
+    def erode(self):
+        self.w.erode(self.drops)
+
+    def reset(self):
+        self.w.set_field("height", self.h0)
+        for f in ("discharge", "momentum_x", "momentum_y"):
+            self.w.set_field(f, self.zero)
+        self.w.set_cycle(0)
+
+    def host_buffers(self, torch):
+        bufs = {}
+        for f in FIELDS:
+            b = torch.empty(self.h0.shape, dtype=torch.float32, pin_memory=True).numpy()
+            b[...] = self.h0 if f == "height" else 0.0
+            bufs[f] = b
+        return bufs
+
+    def upload(self, bufs):
+        for f in FIELDS:
+            self.w.set_field(f, bufs[f])
+
+    def download(self, bufs):
+        for f in FIELDS:
+            self.w.get_field(f, out=bufs[f])
+
+
+class BatchWorkload:
+    """This rank's share of the batched-terrain configuration: 64 terrains
+    with sides log-uniform in [128, 1024], 0.25 drops per cell per cycle, all
+    eroded by one lock-step launch per cycle.  Terrains are split over ranks
+    whole (no exchange).  One step = one cycle of every terrain."""
+
+    def __init__(self, shy, rank, world_size, n_terrains):
+        from simplehydrology_gb300 import sharding
+        self.specs = sharding.rank_terrains(sharding.batch_workload(n_terrains), world_size, rank)
+        self.w = shy.Batch([(t.nx, t.ny) for t in self.specs], [t.drops for t in self.specs],
+                           [t.seed for t in self.specs])
+        self.h0 = []
+        for i, t in enumerate(self.specs):
+            self.w.generate(i, t.seed, 8)
+            self.h0.append(self.w.get_field(i, "height"))
+        self.cells = sum(t.cells for t in self.specs)
+        self.config = {"workload": f"batched terrains: {n_terrains} value-noise terrains, sides log-uniform in "
+                                   f"[128, 1024], 0.25 drops/cell/cycle, one launch per cycle",
+                       "terrains_this_rank": len(self.specs), "cells_this_rank": self.cells,
+                       "drops_per_cycle_this_rank": sum(t.drops for t in self.specs)}
+
+    def erode(self):
+        self.w.erode(1)
+
+    def reset(self):
+        for i, t in enumerate(self.specs):
+            self.w.set_field(i, "height", self.h0[i])
+            z = self.h0[i] * 0.0
+            for f in ("discharge", "momentum_x", "momentum_y"):
+                self.w.set_field(i, f, z)
+        self.w.set_cycle(0)
+
+    def host_buffers(self, torch):
+        bufs = []
+        for i, h in enumerate(self.h0):
+            d = {}
+            for f in FIELDS:
+                b = torch.empty(h.shape, dtype=torch.float32, pin_memory=True).numpy()
+                b[...] = h if f == "height" else 0.0
+                d[f] = b
+            bufs.append(d)
+        return bufs
+
+    def upload(self, bufs):
+        for i, d in enumerate(bufs):
+            for f in FIELDS:
+                self.w.set_field(i, f, d[f])
+
+    def download(self, bufs):
+        for i, d in enumerate(bufs):
+            for f in FIELDS:
+                self.w.get_field(i, f, out=d[f])
+
+
+FIELDS = ("height", "discharge", "momentum_x", "momentum_y")
+
+
 def run_ours(args):
-    import numpy as np
     import torch
 
     import simplehydrology_gb300 as shy
     from simplehydrology_gb300 import build as shybuild
+    from simplehydrology_gb300 import sharding
 
     shybuild.build()
     rank, world_size, dist = dist_setup(args.gpus)
     dev = torch.cuda.current_device()
 
-    NX, NY, DROPS = args.map, args.map, args.drops
-    w = shy.World(NX, NY, seed=SEED)
-    w.generate(SEED, 8)
-    h0 = w.get_field("height")
-    zero = np.zeros_like(h0)
-
-    def reset():
-        w.set_field("height", h0)
-        for f in ("discharge", "momentum_x", "momentum_y"):
-            w.set_field(f, zero)
-        w.set_cycle(0)
+    if args.workload == "batch":
+        wl = BatchWorkload(shy, rank, world_size, args.terrains)
+    else:
+        wl = PlainWorkload(shy, args.map, args.drops)
+    w = wl.w
 
     # warm-up on the same workload, then restart from the initial terrain
     for _ in range(args.warmup):
-        w.erode(DROPS)
-    reset()
+        wl.erode()
+    wl.reset()
     w.reset_stats()
 
     stream = torch.cuda.ExternalStream(w.stream())
@@ -201,7 +306,7 @@ def run_ours(args):
             with torch.cuda.stream(stream):
                 flush.fill_(k & 0xFF)        # untimed L2 flush
                 starts[k].record(stream)
-            w.erode(DROPS)
+            wl.erode()
             with torch.cuda.stream(stream):
                 stops[k].record(stream)
         torch.cuda.synchronize()
@@ -213,60 +318,54 @@ def run_ours(args):
     ph1, it1 = w.lockstep_profile()
     w.enable_timing(False)
     steps_total = st.drop_steps
-    if dist:
-        t = torch.tensor([dev_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s = float(t.item())
-        s = torch.tensor([float(steps_total)], dtype=torch.float64, device=dev)
-        dist.all_reduce(s)
-        steps_all = float(s.item())
-    else:
-        steps_all = float(steps_total)
-    value = steps_all / dev_s
+    steps_all, dev_s_max = sharding.aggregate(steps_total, dev_s, dist)
+    value = steps_all / dev_s_max
 
-    # roofline of the dominant kernel (the lock-step drops kernel)
+    # roofline of the dominant kernel (the lock-step drops kernel): the
+    # algorithmic bytes against the HBM copy peak, and against the L2 peaks
+    # that bound it when the cell state fits in L2
     n_launch = max(1, tm.launches[0])
     avg_ms = tm.ms[0] / n_launch
     bytes_per_launch = BYTES_PER_STEP * steps_total / n_launch
     achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
     # the committed capture covers the default 1024^2 / 65,536-drop workload only
-    traffic = profiled_traffic() if (NX, NY, DROPS) == (1024, 1024, 65536) else None
+    plain_default = args.workload == "plain" and (args.map, args.drops) == (1024, 65536)
+    traffic = profiled_traffic() if plain_default else None
+    l2 = shy.measure_l2(dev)
+    kernel_s = tm.ms[0] / 1e3
+    atomics = 4.0 * steps_total / kernel_s
+    cycle_bytes = BYTES_PER_STEP * steps_total + BYTES_PER_CELL_CYCLE * wl.cells * args.steps
 
-    # end to end through the C ABI with pinned host buffers
-    fields = ("height", "discharge", "momentum_x", "momentum_y")
-    if args.no_e2e:
-        fields = ()
-    host = {f: torch.empty((NX, NY), dtype=torch.float32, pin_memory=True).numpy() for f in fields}
-    if fields:
-        host["height"][...] = h0
-        for f in fields[1:]:
-            host[f][...] = 0.0
-    reset()
-    w.reset_stats()
-    e2e_steps = min(args.steps, 50) if fields else 0
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for k in range(e2e_steps):
-        for f in fields:
-            w.set_field(f, host[f])
-        w.erode(DROPS)
-        for f in fields:
-            w.get_field(f, out=host[f])
-    e2e_s = time.perf_counter() - t0
-    e2e_value = w.stats().drop_steps * world_size / e2e_s if e2e_steps else None
-    nbytes = NX * NY * 4 * len(fields)
+    # end to end through the C ABI with pinned host buffers: each step copies
+    # the world state in, erodes one cycle and copies it back out
+    e2e_steps = 0 if args.no_e2e else min(args.steps, 50)
+    e2e_value, nbytes = None, 0
+    if e2e_steps:
+        bufs = wl.host_buffers(torch)
+        wl.reset()
+        w.reset_stats()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            wl.upload(bufs)
+            wl.erode()
+            wl.download(bufs)
+        e2e_s = time.perf_counter() - t0
+        e2e_units, e2e_s = sharding.aggregate(w.stats().drop_steps, e2e_s, dist)
+        e2e_value = e2e_units / e2e_s
+        nbytes = wl.cells * 4 * len(FIELDS)
 
+    config = dict(wl.config)
+    config.update({"step": "one erosion cycle", "l2": "flushed between steps (256 MiB write, untimed)",
+                   "parallelism": (("terrain shards" if args.workload == "batch" else "replicas") +
+                                   f" x{world_size}") if world_size > 1 else "single GPU"})
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world_size,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s_max * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded value-noise terrain, counter-based spawns)",
-        "config": {"workload": WORKLOAD if (NX, DROPS) == (1024, 65536) else
-                   f"profiling case: {NX}x{NY} value-noise terrain, {DROPS} drops/cycle",
-                   "map": [NX, NY], "drops_per_cycle": DROPS,
-                   "step": "one erosion cycle", "l2": "flushed between steps (256 MiB write, untimed)",
-                   "parallelism": f"replicas x{world_size}" if world_size > 1 else "single GPU"},
+        "config": config,
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "steps": e2e_steps},
         "gpu_launches": int(sum(tm.launches)),
@@ -274,6 +373,13 @@ def run_ours(args):
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "kernel": "lockstep_kernel", "avg_launch_ms": avg_ms,
                      "algorithmic_bytes_per_launch": bytes_per_launch},
+        "roofline_l2": {"achieved_gbs": achieved, "read_peak_gbs": l2["read_gbs"],
+                        "frac": achieved / l2["read_gbs"],
+                        "atomics_per_s": atomics, "red_peak_per_s": l2["red_per_s"],
+                        "atomic_frac": atomics / l2["red_per_s"],
+                        "random_sector_reads_peak_per_s": l2["random_sector_reads_per_s"],
+                        "l2_bytes": l2["l2_bytes"], "peak_source": "shy_measure_l2 on this GPU"},
+        "cycle_gbs": cycle_bytes / dev_s / 1e9,
         "kernel_ms": {"drops": tm.ms[0], "cycle_end": tm.ms[1], "relax": tm.ms[2]},
         "lockstep": {"iterations": it1 - it0,
                      "phase_ms": dict(zip(["descend", "wait_descend", "scan", "wait_scan", "settle", "wait_settle"],
@@ -354,6 +460,9 @@ def main():
     ap.add_argument("--map", type=int, default=NX)
     ap.add_argument("--drops", type=int, default=DROPS)
     ap.add_argument("--no-e2e", action="store_true")
+    # the batched-terrain configuration (not the default bench line)
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch"])
+    ap.add_argument("--terrains", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -282,6 +282,21 @@ int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint64_t seed, u
                       int drops, int cycles, float* height, float* discharge, float* momentum_x,
                       float* momentum_y, const float* root_density, void* stream, shy_stats* stats);
 
+/* ---- Measurement ----------------------------------------------------------
+ * L2 peaks of one device, measured by the library's own microbenchmarks (no
+ * counterpart in the reference, which has no GPU path).  They are the
+ * roofline of the batched kernel when a terrain's cell state fits in L2.
+ * Allocates about 40 MiB of device memory for the duration of the call and
+ * takes well under a second. */
+typedef struct shy_l2_probe {
+  uint64_t l2_bytes;                  /* L2 capacity (cudaDevAttrL2CacheSize) */
+  uint64_t buffer_bytes;              /* probe buffer, a quarter of L2 at most */
+  double read_gbs;                    /* streaming 16-byte loads that bypass L1 */
+  double random_sector_reads_per_s;   /* 8-byte loads, one per random 32-byte sector */
+  double red_per_s;                   /* 64-bit atomic adds without return, random addresses */
+} shy_l2_probe;
+int shy_measure_l2(int device, shy_l2_probe* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,11 +18,18 @@ import ctypes as C
 import numpy as np
 
 from . import _capi
-from ._capi import (ERF_DEVICE, ERF_HOST_LIBM, FIELD_NAMES, DropState, Params, ShyError, Stats,
+from ._capi import (ERF_DEVICE, ERF_HOST_LIBM, FIELD_NAMES, DropState, L2Probe, Params, ShyError, Stats,
                     Timing, check, default_params, lib)
 
 __all__ = ["World", "Batch", "Drop", "Params", "Stats", "Timing", "ShyError", "default_params",
-           "lib", "ERF_DEVICE", "ERF_HOST_LIBM", "FIELD_NAMES"]
+           "lib", "measure_l2", "ERF_DEVICE", "ERF_HOST_LIBM", "FIELD_NAMES"]
+
+
+def measure_l2(device: int = 0) -> dict:
+    """L2 peaks of one device from the library's microbenchmarks (shy_measure_l2)."""
+    out = L2Probe()
+    check(lib().shy_measure_l2(int(device), C.byref(out)))
+    return out.as_dict()
 
 
 def _fptr(a):
@@ -234,9 +241,12 @@ class Batch(_Handle):
         a = np.ascontiguousarray(values, dtype=np.float32).reshape(nx, ny)
         check(lib().shy_terrain_set_field(self._w, t, _field_index(field), _fptr(a), a.size))
 
-    def get_field(self, t, field):
+    def get_field(self, t, field, out=None):
         nx, ny = self.sizes[t]
-        out = np.empty((nx, ny), np.float32)
+        if out is None:
+            out = np.empty((nx, ny), np.float32)
+        elif out.dtype != np.float32 or out.shape != (nx, ny) or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float32 array of the terrain's shape")
         check(lib().shy_terrain_get_field(self._w, t, _field_index(field), _fptr(out), out.size))
         return out
 

@@ -71,6 +71,14 @@ class Timing(C.Structure):
     _fields_ = [("ms", C.c_double * 4), ("launches", C.c_uint64 * 4), ("steps_timed", C.c_uint64)]
 
 
+class L2Probe(C.Structure):
+    _fields_ = [("l2_bytes", C.c_uint64), ("buffer_bytes", C.c_uint64), ("read_gbs", C.c_double),
+                ("random_sector_reads_per_s", C.c_double), ("red_per_s", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class ShyError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"shy error {code}: {msg}")
@@ -122,6 +130,7 @@ SIGNATURES = {
     "shy_erode_noalloc": (C.c_int, [C.c_int, C.c_int, P(Params), C.c_uint64, C.c_uint64, C.c_int, C.c_int,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     P(Stats)]),
+    "shy_measure_l2": (C.c_int, [C.c_int, P(L2Probe)]),
 }
 
 _lib = None

@@ -210,4 +210,11 @@ int batched_max_grid(shy_world* w, int block);
 void set_error(const char* fmt, ...);
 int cuda_fail(cudaError_t e, const char* what);
 
+// return the C ABI's error status when a CUDA call fails
+#define SHY_CHECK_CUDA(expr, what)                         \
+  do {                                                     \
+    cudaError_t e_ = (expr);                               \
+    if (e_ != cudaSuccess) return shy::cuda_fail(e_, what); \
+  } while (0)
+
 }  // namespace shy

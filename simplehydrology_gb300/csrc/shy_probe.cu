@@ -1,0 +1,176 @@
+// shy_probe.cu -- L2 peaks of this device, measured by the library itself.
+//
+// The batched erosion kernel keeps a 1024^2 terrain's cell state in L2, so
+// its roofline is the L2's, not HBM's.  shy_measure_l2 measures the figures
+// that roofline needs on the device at hand:
+//   read_gbs                   streaming 16-byte loads that bypass L1, over a
+//                              buffer a quarter of the L2 (at most 32 MiB)
+//   random_sector_reads_per_s  8-byte loads, each to a different 32-byte
+//                              sector picked at random in that buffer (the
+//                              access pattern of a drop-step's cell loads)
+//   red_per_s                  64-bit integer atomic additions without return
+//                              to random addresses of an 8 MiB table (the
+//                              drop-step's scatter)
+// Each is timed with CUDA events after one untimed pass that brings the
+// buffer into L2.
+#include "shy_device.cuh"
+
+namespace shy {
+
+namespace {
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__global__ void stream_read_kernel(const uint4* __restrict__ buf, long long n, int passes,
+                                   unsigned* __restrict__ sink) {
+  unsigned acc = 0;
+  const long long G = (long long)gridDim.x * blockDim.x;
+  for (int p = 0; p < passes; ++p)
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += G) {
+      const uint4 v = __ldcg(buf + i);
+      acc ^= v.x ^ v.y ^ v.z ^ v.w;
+    }
+  if (acc == 0x9E3779B9u) sink[0] = acc;  // keeps the loads
+}
+
+// kLoads independent loads in flight per thread and round
+__global__ void random_sector_kernel(const unsigned long long* __restrict__ buf, long long sectors, int rounds,
+                                     unsigned long long* __restrict__ sink) {
+  const int kLoads = 8;
+  const unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  unsigned long long acc = 0;
+  for (int r = 0; r < rounds; ++r) {
+    unsigned long long v[kLoads];
+#pragma unroll
+    for (int k = 0; k < kLoads; ++k) {
+      const unsigned long long s = mix64(t * 0x100000001B3ull + (unsigned long long)(r * kLoads + k)) % sectors;
+      v[k] = __ldcg(buf + s * 4);  // one 8-byte word of sector s
+    }
+#pragma unroll
+    for (int k = 0; k < kLoads; ++k) acc += v[k];
+  }
+  if (acc == 0x9E3779B97F4A7C15ull) sink[0] = acc;
+}
+
+__global__ void random_red_kernel(unsigned long long* __restrict__ table, long long n, int per_thread) {
+  const unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  for (int k = 0; k < per_thread; ++k) {
+    const unsigned long long s = mix64(t * 0x100000001B3ull + (unsigned long long)k) % (unsigned long long)n;
+    atomicAdd(table + s, 1ull);
+  }
+}
+
+struct ProbeBuffers {
+  void* buf = nullptr;
+  void* table = nullptr;
+  void* sink = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  ~ProbeBuffers() {
+    if (stream) cudaStreamSynchronize(stream);
+    if (buf) cudaFree(buf);
+    if (table) cudaFree(table);
+    if (sink) cudaFree(sink);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+// milliseconds of `launch` (enqueued on pb.stream) between two events
+template <class F>
+cudaError_t timed(ProbeBuffers& pb, F launch, float* ms) {
+  cudaError_t e;
+  if ((e = cudaEventRecord(pb.a, pb.stream)) != cudaSuccess) return e;
+  launch();
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(pb.b, pb.stream)) != cudaSuccess) return e;
+  if ((e = cudaEventSynchronize(pb.b)) != cudaSuccess) return e;
+  return cudaEventElapsedTime(ms, pb.a, pb.b);
+}
+
+int measure(int device, shy_l2_probe* out) {
+  int sms = 0, l2 = 0;
+  SHY_CHECK_CUDA(cudaSetDevice(device), "select device");
+  SHY_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "query SMs");
+  SHY_CHECK_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device), "query L2 size");
+  long long bytes = (long long)l2 / 4;
+  if (bytes > (32ll << 20)) bytes = 32ll << 20;
+  bytes &= ~255ll;
+  if (bytes < (1 << 20)) bytes = 1 << 20;
+  const long long table_n = (8ll << 20) / 8;
+  ProbeBuffers pb;
+  SHY_CHECK_CUDA(cudaStreamCreateWithFlags(&pb.stream, cudaStreamNonBlocking), "create stream");
+  SHY_CHECK_CUDA(cudaEventCreate(&pb.a), "create event");
+  SHY_CHECK_CUDA(cudaEventCreate(&pb.b), "create event");
+  SHY_CHECK_CUDA(cudaMalloc(&pb.buf, (size_t)bytes), "allocate probe buffer");
+  SHY_CHECK_CUDA(cudaMalloc(&pb.table, (size_t)table_n * 8), "allocate probe table");
+  SHY_CHECK_CUDA(cudaMalloc(&pb.sink, 64), "allocate probe sink");
+  SHY_CHECK_CUDA(cudaMemsetAsync(pb.buf, 1, (size_t)bytes, pb.stream), "fill probe buffer");
+  SHY_CHECK_CUDA(cudaMemsetAsync(pb.table, 0, (size_t)table_n * 8, pb.stream), "clear probe table");
+
+  const int grid = sms * 8, block = 256;
+  const long long n16 = bytes / 16;
+  const int passes = 20;
+  float ms = 0.0f;
+  auto stream_run = [&](int p) {
+    stream_read_kernel<<<grid, block, 0, pb.stream>>>((const uint4*)pb.buf, n16, p, (unsigned*)pb.sink);
+  };
+  SHY_CHECK_CUDA(timed(pb, [&] { stream_run(1); }, &ms), "L2 read probe");
+  SHY_CHECK_CUDA(timed(pb, [&] { stream_run(passes); }, &ms), "L2 read probe");
+  out->read_gbs = (double)bytes * passes / (ms * 1e-3) / 1e9;
+
+  const long long sectors = bytes / 32;
+  const int rounds = 64;
+  auto sector_run = [&](int r) {
+    random_sector_kernel<<<grid, block, 0, pb.stream>>>((const unsigned long long*)pb.buf, sectors, r,
+                                                         (unsigned long long*)pb.sink);
+  };
+  SHY_CHECK_CUDA(timed(pb, [&] { sector_run(4); }, &ms), "L2 sector probe");
+  SHY_CHECK_CUDA(timed(pb, [&] { sector_run(rounds); }, &ms), "L2 sector probe");
+  out->random_sector_reads_per_s = (double)grid * block * rounds * 8 / (ms * 1e-3);
+
+  const int per_thread = 64;
+  auto red_run = [&](int k) {
+    random_red_kernel<<<grid, block, 0, pb.stream>>>((unsigned long long*)pb.table, table_n, k);
+  };
+  SHY_CHECK_CUDA(timed(pb, [&] { red_run(4); }, &ms), "L2 atomic probe");
+  SHY_CHECK_CUDA(timed(pb, [&] { red_run(per_thread); }, &ms), "L2 atomic probe");
+  out->red_per_s = (double)grid * block * per_thread / (ms * 1e-3);
+  out->l2_bytes = (uint64_t)l2;
+  out->buffer_bytes = (uint64_t)bytes;
+  return SHY_OK;
+}
+
+}  // namespace
+
+}  // namespace shy
+
+using namespace shy;
+
+extern "C" int shy_measure_l2(int device, shy_l2_probe* out) {
+  if (!out) {
+    set_error("shy_measure_l2: null output");
+    return SHY_ERR_INVALID_ARG;
+  }
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    set_error("shy_measure_l2: no CUDA device");
+    return SHY_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) {
+    set_error("shy_measure_l2: device %d out of range (%d devices)", device, n);
+    return SHY_ERR_INVALID_ARG;
+  }
+  int prev = 0;
+  cudaGetDevice(&prev);
+  const int rc = measure(device, out);
+  cudaSetDevice(prev);
+  return rc;
+}

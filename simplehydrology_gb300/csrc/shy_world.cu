@@ -75,12 +75,6 @@ static cudaError_t timing_collect(shy_world* w) {
 
 using namespace shy;
 
-#define SHY_CHECK_CUDA(expr, what)                \
-  do {                                            \
-    cudaError_t e_ = (expr);                      \
-    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
-  } while (0)
-
 namespace {
 
 bool params_valid(const shy_params* p) {
