@@ -21,8 +21,8 @@ int blocks_for(long long n, int block = kBlock) {
 // 1 + entrainment * erf(0.4 d) (source/water.h:127, source/cellpool.h:242-244)
 // and max(0, depositionRate * (1 - rootdensity)) (source/water.h:86-87).
 __global__ void rebuild_records_kernel(float4* __restrict__ rec, float* __restrict__ effd,
-                                       const float* __restrict__ root, long long cells,
-                                       shy_params P) {
+                                       CellQ* __restrict__ cq, const float* __restrict__ root,
+                                       long long cells, shy_params P) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells;
        i += (long long)gridDim.x * blockDim.x) {
     float4 r = rec[i];
@@ -30,6 +30,7 @@ __global__ void rebuild_records_kernel(float4* __restrict__ rec, float* __restri
     rec[i] = r;
     const float e = P.deposition_rate * (1.0f - root[i]);
     effd[i] = e < 0.0f ? 0.0f : e;
+    cq[i].effd = e < 0.0f ? 0.0f : e;  // the batched mode's copy
   }
 }
 
@@ -171,7 +172,7 @@ __global__ void scatter_rec_kernel(float4* rec, const float* in, long long n, in
 }  // namespace
 
 cudaError_t launch_rebuild_records(shy_world* w, int) {
-  rebuild_records_kernel<<<blocks_for(w->cells), kBlock, 0, w->stream>>>(w->rec, w->effd, w->root,
+  rebuild_records_kernel<<<blocks_for(w->cells), kBlock, 0, w->stream>>>(w->rec, w->effd, w->cq, w->root,
                                                                          w->cells, w->P);
   return cudaGetLastError();
 }

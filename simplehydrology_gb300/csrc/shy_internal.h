@@ -17,6 +17,7 @@ namespace shy {
 // math::flatten, source/include/math.h:11-14).
 struct Terrain {
   long long cell_base;
+  long long arr_base;  // first word of this terrain's arrivals bitmap
   int nx, ny;
   int drop_base;   // first drop slot of this terrain in a batched cycle
   int drops;       // drops per batched cycle
@@ -37,9 +38,18 @@ struct alignas(32) Tracks {
 struct alignas(32) CellQ {
   long long hq;   // height, 32.32 fixed point
   long long e;    // erosion / deposition of the current step (phase A sums)
-  long long pad;
+  float effd;     // max(0, depositionRate * (1 - rootdensity)), a copy of the map
+  int spare;
   int cnt[2];     // drops at the cell at the start of a step, by step parity
 };
+
+// Arrivals bitmap of the batched mode: one bit per cell, set while a
+// cascade is claimed at the cell in the current step.  Cells are grouped in
+// 8 x 8 tiles, one 64-bit word each (bit (x % 8) * 8 + y % 8), so that the
+// 5 x 5 block around any cell lies in at most 2 x 2 words.
+__host__ __device__ inline long long arr_words(int nx, int ny) {
+  return (long long)((nx + 7) >> 3) * ((ny + 7) >> 3);
+}
 
 // Device-side counters (see shy_stats).
 struct DevStats {
@@ -131,6 +141,7 @@ struct shy_world {
   long long* dcell = nullptr; // cell of this step's exchange, -1 if none
   long long* dctr = nullptr;  // cascade centre this slot runs this step, -1 if none
   shy::SteepCell* dsteep = nullptr;  // steep-cascade queue (one entry per drop slot at most)
+  unsigned long long* arr = nullptr;  // arrivals bitmap, all terrains
 
   shy::Terrain* dterrains = nullptr;
   shy::DevStats* stats = nullptr;
@@ -168,7 +179,6 @@ struct CycleBuffers {
   float* h;
   CellQ* cq;
   float4* rec;
-  const float* effd;
   const float* voltab;
   Tracks* trk;
   float* track_f;
@@ -180,6 +190,7 @@ struct CycleBuffers {
   long long* cell;
   long long* ctr;
   SteepCell* steep;
+  unsigned long long* arr;
   DevStats* st;
   GridBar* bar;
   shy_params P;

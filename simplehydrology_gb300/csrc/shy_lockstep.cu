@@ -16,17 +16,18 @@
 //      cell's cascade.
 //   scan  World::cascade (source/world.h:90-168) at every claimed cell reads
 //      the nine heights phase descend left (fixed point plus pending sum).
-//      Cascades that move nothing end here; the steep ones are queued in the
-//      CTA with the heights they read.
+//      Cascades that move nothing end here.  The steep ones read this step's
+//      claimed centres in the 5 x 5 block around theirs (an arrivals bitmap
+//      in 8 x 8-cell words, loaded with the heights) and are queued in the
+//      CTA with the heights they read and their overlap counts: where the
+//      3 x 3 blocks of k cascades overlap, a pair's transfer is divided by k
+//      (the larger count of its two cells), so overlapping cascades together
+//      move what one would.
 //   settle  each queued cascade runs the reference's sequential transfer
 //      loop on one thread and adds its transfers straight to the fixed-point
-//      heights (no height is read in this phase); where the 3 x 3 blocks of k
-//      cascades overlap, a pair's transfer is divided by k (the larger count
-//      of its two cells), so overlapping cascades together move what one
-//      would; the counts come from the arrivals registered in the 5 x 5 block
-//      around the centre.  Every drop adds its own height change to its
-//      cell's fixed-point height and clears the cell's pending sum and count;
-//      finished drops retire.
+//      heights (no height is read in this phase).  Every drop adds its own
+//      height change to its cell's fixed-point height and clears the cell's
+//      pending sum and count; finished drops retire.
 // Heights live in 32.32 fixed point for the whole cycle (the float map is
 // rewritten at its end), so every update is an integer addition.
 // Integer sums make every result independent of thread timing: the same
@@ -77,6 +78,42 @@ __device__ __forceinline__ void add_i64(long long* p, long long v) {
   atomicAdd((unsigned long long*)p, (unsigned long long)v);
 }
 
+// A cell's whole 32-byte record in one load: fixed-point height, deposition
+// rate and the two step-parity drop counts.
+struct CellView {
+  long long hq;
+  float effd;
+  int cnt0, cnt1;  // drop counts by step parity
+};
+__device__ __forceinline__ CellView load_cell(const CellQ* p) {
+  unsigned long long w0, w1, w2, w3;
+  asm volatile("ld.global.v4.u64 {%0, %1, %2, %3}, [%4];"
+               : "=l"(w0), "=l"(w1), "=l"(w2), "=l"(w3)
+               : "l"(p));
+  CellView v;
+  v.hq = (long long)w0;
+  v.effd = __uint_as_float((unsigned)(w2 & 0xffffffffull));
+  v.cnt0 = (int)(unsigned)(w3 & 0xffffffffull);
+  v.cnt1 = (int)(unsigned)(w3 >> 32);
+  return v;
+}
+
+// an arrivals word, loaded where it stands in the program (not moved into
+// the branch that uses it)
+__device__ __forceinline__ unsigned long long load_arr(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.global.u64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
+}
+
+// word and bit of cell (x, y) in a terrain's arrivals bitmap
+__device__ __forceinline__ long long arr_word(const Terrain& T, int x, int y) {
+  return T.arr_base + (long long)(x >> 3) * ((T.ny + 7) >> 3) + (y >> 3);
+}
+__device__ __forceinline__ unsigned long long arr_bit(int x, int y) {
+  return 1ull << (((x & 7) << 3) | (y & 7));
+}
+
 // Grid-wide barrier over a monotonically increasing arrival counter (reset to
 // zero between launches).  `passed` counts the barriers this CTA has passed.
 // Thread 0 reads the live-drop count once the barrier is passed (every CTA
@@ -124,7 +161,6 @@ struct LockArgs {
   const float* h;  // heights rounded to float at cycle start (spawn test)
   CellQ* cq;       // fixed-point heights, pending changes, drop counts
   const float4* rec;
-  const float* effd;
   const float* voltab;  // volume after k evaporations (source/water.h:136)
   shy_evap ev;
   Tracks* trk;
@@ -140,6 +176,7 @@ struct LockArgs {
   long long* cell;
   long long* ctr;
   SteepCell* steep;
+  unsigned long long* arr;  // arrivals bitmap
   int smem_slots;   // 1: drop slots and queue live in dynamic shared memory
   shy_params P;
   DevStats* st;
@@ -261,18 +298,21 @@ __device__ __forceinline__ longlong2 hq_e(const CellQ* c) {
 }
 
 // Overlap counts of a claimed cascade: the cascade centres of this step in the
-// 5 x 5 block around it (cells a drop moved to) give, for the centre and each
-// of its 8 neighbours, how many cascades' 3 x 3 blocks hold that cell.  The
-// arrivals are loaded by the caller (cv[l] for (dx, dy) = (l / 5 - 2,
-// l % 5 - 2), any value outside the map).
-__device__ __forceinline__ void overlap_counts(const int* cv, int ix, int iy, const Terrain& T, unsigned& kv,
-                                               int& kc) {
+// 5 x 5 block around (ix, iy) give, for the centre and each of its 8
+// neighbours, how many cascades' 3 x 3 blocks hold that cell.  wij is the
+// arrivals word of tile column tx0 + i, tile row ty0 + j (the block spans at
+// most two of each).
+__device__ __forceinline__ void overlap_counts(unsigned long long w00, unsigned long long w01,
+                                               unsigned long long w10, unsigned long long w11, int tx0, int ty0,
+                                               int ix, int iy, const Terrain& T, unsigned& kv, int& kc) {
   unsigned cen = 0;
 #pragma unroll
   for (int l = 0; l < 25; ++l) {
-    const int dx = l / 5 - 2, dy = l % 5 - 2;
-    const bool in = !oob(ix + dx, iy + dy, T.nx, T.ny);
-    cen |= (in && cv[l] > 0) ? (1u << l) : 0u;
+    const int x = ix + l / 5 - 2, y = iy + l % 5 - 2;
+    const bool in = !oob(x, y, T.nx, T.ny);
+    const bool i = in && (x >> 3) != tx0, j = in && (y >> 3) != ty0;
+    const unsigned long long word = i ? (j ? w11 : w10) : (j ? w01 : w00);
+    cen |= (in && (word & arr_bit(x, y))) ? (1u << l) : 0u;
   }
   // cascades whose 3 x 3 block holds cell (dx, dy): popcount of a window
   auto cover = [&](int dx, int dy) {
@@ -446,14 +486,15 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       const bool xp = ix + 1 < T.nx, xm = ix > 0, yp = iy + 1 < T.ny, ym = iy > 0;
       // all loads issued together; a neighbour outside the map reads the
       // centre and is masked to height 0
-      const long long q0 = RT[lc].hq;
-      const int nhere = RT[lc].cnt[par];
+      const CellView own = load_cell(RT + lc);
+      const long long q0 = own.hq;
+      const int nhere = par ? own.cnt1 : own.cnt0;
       long long qxp = RT[xp ? lc + T.ny : lc].hq;
       long long qxm = RT[xm ? lc - T.ny : lc].hq;
       long long qyp = RT[yp ? lc + 1 : lc].hq;
       long long qym = RT[ym ? lc - 1 : lc].hq;
       const float4 r = __ldg(&a.rec[c]);
-      const float ed = __ldg(&a.effd[c]);
+      const float ed = own.effd;
       const float vnext = __ldg(&a.voltab[ag + 1 < vmax ? ag + 1 : vmax]);
       qxp = xp ? qxp : 0;
       qxm = xm ? qxm : 0;
@@ -526,6 +567,8 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         continue;
       }
       S.ctr[j] = arrived_before == 0 ? c2 : -1;  // World::cascade(pos), water.h:151
+      if (arrived_before == 0)
+        atomicOr(&a.arr[arr_word(T, jx, jy)], arr_bit(jx, jy));
       S.age[j] = ag + 1;
       S.pos[j] = p;
       S.spd[j] = s;
@@ -536,7 +579,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     if (!grid_barrier(a.bar, passed, nullptr)) { ok = false; break; }
     lap(1);
 
-    // ---- scan: the nine heights and the overlap counts of each claimed cascade ----
+    // ---- scan: the nine heights of each claimed cascade; overlap counts of the steep ones ----
     // heights after phase descend: fixed point plus the step's erosion.  All
     // nine loads are issued together: a neighbour outside the map reads the
     // centre instead and is masked out.  The centre only changes through a
@@ -556,15 +599,16 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         nv[k] = hq_e(&a.cq[in ? c2 + (long long)nb_dx(k) * T.ny + nb_dy(k) : c2]);
       }
       const longlong2 v0 = hq_e(&a.cq[c2]);
-      // this step's arrivals in the 5 x 5 block, loaded with the heights so
-      // that a steep cascade needs no further load (most are not steep)
-      int cv[25];
-#pragma unroll
-      for (int l = 0; l < 25; ++l) {
-        const int dx = l / 5 - 2, dy = l % 5 - 2;
-        const bool in = !oob(ix + dx, iy + dy, T.nx, T.ny);
-        cv[l] = a.cq[in ? c2 + (long long)dx * T.ny + dy : c2].cnt[par ^ 1];
-      }
+      // the arrivals of the 5 x 5 block: at most 2 x 2 bitmap words, loaded
+      // with the heights
+      const int tx0 = (ix >= 2 ? ix - 2 : 0) >> 3, tx1 = (ix + 2 < T.nx ? ix + 2 : T.nx - 1) >> 3;
+      const int ty0 = (iy >= 2 ? iy - 2 : 0) >> 3, ty1 = (iy + 2 < T.ny ? iy + 2 : T.ny - 1) >> 3;
+      const long long tyn = (T.ny + 7) >> 3;
+      const unsigned long long* AW = a.arr + T.arr_base;
+      const unsigned long long aw00 = load_arr(AW + tx0 * tyn + ty0);
+      const unsigned long long aw01 = load_arr(AW + tx0 * tyn + ty1);
+      const unsigned long long aw10 = load_arr(AW + tx1 * tyn + ty0);
+      const unsigned long long aw11 = load_arr(AW + tx1 * tyn + ty1);
       float sh[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k)
@@ -580,10 +624,10 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         any |= (sh[k] < __int_as_float(0x7f800000)) && diff != 0.0f && excess > 0.0f;
       }
       if (any) {
-        // one claim per drop slot, so the queue (cap entries) cannot overflow
         unsigned kv;
         int kc;
-        overlap_counts(cv, ix, iy, T, kv, kc);
+        overlap_counts(aw00, aw01, aw10, aw11, tx0, ty0, ix, iy, T, kv, kc);
+        // one claim per drop slot, so the queue (cap entries) cannot overflow
         SteepCell& q = S.steep[atomicAdd(&s_nq, 1)];
         q.c2 = c2;
         q.ti = ti;
@@ -613,6 +657,13 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       const int ag = S.age[j];
       if (ag == -1) continue;
       const long long c = S.cell[j];
+      const long long c2 = S.ctr[j];
+      if (c2 >= 0) {  // the claim of this step ends
+        const Terrain T = TT[S.terr[j]];
+        const int lc = (int)(c2 - T.cell_base);
+        const int x = lc / T.ny, y = lc - x * T.ny;
+        atomicAnd(&a.arr[arr_word(T, x, y)], ~arr_bit(x, y));
+      }
       if (c >= 0) {
         const long long own = S.own[j];
         if (own != 0) add_i64(&a.cq[c].hq, own);
@@ -817,7 +868,6 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.h = w->h;
   a.cq = w->cq;
   a.rec = w->rec;
-  a.effd = w->effd;
   a.voltab = w->voltab;
   a.ev = shy_evap_make(w->P.evap_rate);
   a.trk = w->trk;
@@ -831,6 +881,7 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.cell = w->dcell;
   a.ctr = w->dctr;
   a.steep = w->dsteep;
+  a.arr = w->arr;
   a.smem_slots = 0;
   a.P = w->P;
   a.st = w->stats;
@@ -875,7 +926,6 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.h = b.h;
   a.cq = b.cq;
   a.rec = b.rec;
-  a.effd = b.effd;
   a.voltab = b.voltab;
   a.ev = shy_evap_make(b.P.evap_rate);
   a.trk = b.trk;
@@ -889,6 +939,7 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.cell = b.cell;
   a.ctr = b.ctr;
   a.steep = b.steep;
+  a.arr = b.arr;
   a.smem_slots = 0;
   a.P = b.P;
   a.st = b.st;

@@ -24,6 +24,8 @@ struct NoallocScratch {
   float track_f[3 * SHY_NOALLOC_MAX_CELLS];
   float voltab[SHY_NOALLOC_MAX_AGE + 3];
   SteepCell steep[SHY_NOALLOC_MAX_DROPS];
+  // arrivals bitmap: ceil(nx / 8) * ceil(ny / 8) <= cells / 64 + (nx + ny) / 8 + 1 words
+  unsigned long long arr[SHY_NOALLOC_MAX_CELLS / 64 + (SHY_NOALLOC_MAX_CELLS + 1) / 8 + 2];
   float2 pos[SHY_NOALLOC_MAX_DROPS], spd[SHY_NOALLOC_MAX_DROPS], vs[SHY_NOALLOC_MAX_DROPS];
   long long gain[SHY_NOALLOC_MAX_DROPS], own[SHY_NOALLOC_MAX_DROPS];
   long long cell[SHY_NOALLOC_MAX_DROPS], ctr[SHY_NOALLOC_MAX_DROPS];
@@ -79,25 +81,29 @@ __global__ void noalloc_init_kernel(NoallocScratch* s, Terrain T, unsigned long 
 // The caller's maps into the batched mode's state: heights to 32.32 fixed
 // point (and re-rounded), per-cell records (source/water.h:86-87,127), track
 // sums and pending sums cleared.
-__global__ void noalloc_pack_kernel(NoallocScratch* s, int n, float* h, const float* d, const float* mx,
-                                    const float* my, const float* root, shy_params P) {
+__global__ void noalloc_pack_kernel(NoallocScratch* s, int n, long long words, float* h, const float* d,
+                                    const float* mx, const float* my, const float* root, shy_params P) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const long long q = shy_q32(h[i]);
     CellQ c;
     c.hq = q;
     c.e = 0;
-    c.pad = 0;
+    const float e = P.deposition_rate * (1.0f - root[i]);
+    c.effd = e < 0.0f ? 0.0f : e;
+    c.spare = 0;
     c.cnt[0] = 0;
     c.cnt[1] = 0;
     s->cq[i] = c;
     h[i] = shy_unq(q);
     s->rec[i] = make_float4(mx[i], my[i], d[i], 1.0f + P.entrainment * shy_erff(0.4f * d[i]));
-    const float e = P.deposition_rate * (1.0f - root[i]);
-    s->effd[i] = e < 0.0f ? 0.0f : e;
+    s->effd[i] = c.effd;
     Tracks t;
     t.td = t.tmx = t.tmy = t.pad = 0;
     s->trk[i] = t;
   }
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < words;
+       i += (long long)gridDim.x * blockDim.x)
+    s->arr[i] = 0;
 }
 
 // Discharge and momentum back to the caller's maps.
@@ -128,6 +134,10 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
               SHY_NOALLOC_MAX_CELLS);
     return SHY_ERR_INVALID_ARG;
   }
+  if (arr_words(nx, ny) > (long long)(sizeof(((NoallocScratch*)nullptr)->arr) / sizeof(unsigned long long))) {
+    set_error("shy_erode_noalloc: %d x %d map exceeds the fixed arrivals bitmap", nx, ny);
+    return SHY_ERR_INVALID_ARG;
+  }
   if (drops < 0 || drops > SHY_NOALLOC_MAX_DROPS || cycles < 0) {
     set_error("shy_erode_noalloc: %d drops per cycle exceeds the fixed scratch of %d (or cycles < 0)", drops,
               SHY_NOALLOC_MAX_DROPS);
@@ -154,6 +164,7 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
   const int n = nx * ny;
   Terrain T;
   T.cell_base = 0;
+  T.arr_base = 0;
   T.nx = nx;
   T.ny = ny;
   T.drop_base = 0;
@@ -161,8 +172,8 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
   T.seed = seed;
   const int blocks = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
   noalloc_init_kernel<<<1, 32, 0, s>>>(sc, T, cycle0, params->evap_rate, (int)params->max_age + 3);
-  noalloc_pack_kernel<<<blocks, 256, 0, s>>>(sc, n, height, discharge, momentum_x, momentum_y, root_density,
-                                             *params);
+  noalloc_pack_kernel<<<blocks, 256, 0, s>>>(sc, n, arr_words(nx, ny), height, discharge, momentum_x,
+                                             momentum_y, root_density, *params);
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "shy_erode_noalloc: set-up kernels");
 
   CycleBuffers b;
@@ -173,7 +184,6 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
   b.h = height;
   b.cq = sc->cq;
   b.rec = sc->rec;
-  b.effd = sc->effd;
   b.voltab = sc->voltab;
   b.trk = sc->trk;
   b.track_f = sc->track_f;
@@ -187,6 +197,7 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
   b.cell = sc->cell;
   b.ctr = sc->ctr;
   b.steep = sc->steep;
+  b.arr = sc->arr;
   b.st = &sc->st;
   b.bar = &sc->bar;
   b.P = *params;

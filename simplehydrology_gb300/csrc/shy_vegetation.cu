@@ -93,7 +93,7 @@ __global__ void veg_step_kernel(const Terrain* __restrict__ terrains, int n_terr
 
 // root density += the step's sums; deposition records follow.
 __global__ void veg_apply_kernel(long long cells, float* __restrict__ root, long long* __restrict__ rootq,
-                                 float* __restrict__ effd, shy_params P) {
+                                 float* __restrict__ effd, CellQ* __restrict__ cq, shy_params P) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells;
        i += (long long)gridDim.x * blockDim.x) {
     const long long q = rootq[i];
@@ -105,6 +105,7 @@ __global__ void veg_apply_kernel(long long cells, float* __restrict__ root, long
     }
     const float e = P.deposition_rate * (1.0f - r);  // source/water.h:86-87
     effd[i] = e < 0.0f ? 0.0f : e;
+    cq[i].effd = e < 0.0f ? 0.0f : e;  // the batched mode's copy
   }
 }
 
@@ -124,7 +125,8 @@ cudaError_t launch_vegetation_step(shy_world* w) {
                                                               w->h, w->rec, w->root, w->plant, w->plant_next,
                                                               w->rootq, w->veg_claim, tag, w->P, w->veg_step);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  veg_apply_kernel<<<grid_for(w->cells), 256, 0, w->stream>>>(w->cells, w->root, w->rootq, w->effd, w->P);
+  veg_apply_kernel<<<grid_for(w->cells), 256, 0, w->stream>>>(w->cells, w->root, w->rootq, w->effd, w->cq,
+                                                                  w->P);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   float* t = w->plant;
   w->plant = w->plant_next;

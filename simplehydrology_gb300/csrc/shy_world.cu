@@ -93,7 +93,7 @@ void free_world(shy_world* w) {
   void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
                   w->dterr, w->dcell, w->dctr, w->dterrains, w->stats, w->bar, w->ddrop,
                   w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down,
-                  w->plant_next, w->rootq, w->veg_claim};
+                  w->plant_next, w->rootq, w->veg_claim, w->arr};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (w->graph) cudaGraphExecDestroy(w->graph);
@@ -203,6 +203,7 @@ int create_world(int n, const int* nx, const int* ny, const int* drops, const ui
     shy_params_default(&P);
   }
   long long cells = 0;
+  long long words = 0;  // arrivals bitmap
   long long total_drops = 0;
   std::vector<Terrain> terr(n);
   for (int i = 0; i < n; ++i) {
@@ -216,12 +217,14 @@ int create_world(int n, const int* nx, const int* ny, const int* drops, const ui
       return SHY_ERR_INVALID_ARG;
     }
     terr[i].cell_base = cells;
+    terr[i].arr_base = words;
     terr[i].nx = nx[i];
     terr[i].ny = ny[i];
     terr[i].drops = dn;
     terr[i].drop_base = 0;
     terr[i].seed = seeds[i];
     cells += (long long)nx[i] * ny[i];
+    words += arr_words(nx[i], ny[i]);
     total_drops += dn;
   }
   if (total_drops > (1ll << 30)) {
@@ -261,6 +264,7 @@ int create_world(int n, const int* nx, const int* ny, const int* drops, const ui
   if ((e = dalloc(&w->cq, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->scratch, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->relax, N)) != cudaSuccess) return fail(e, "allocate maps");
+  if ((e = dalloc(&w->arr, (size_t)words)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->dterrains, (size_t)n)) != cudaSuccess) return fail(e, "allocate terrain table");
   if ((e = dalloc(&w->stats, 1)) != cudaSuccess) return fail(e, "allocate counters");
   if ((e = dalloc(&w->bar, 1)) != cudaSuccess) return fail(e, "allocate counters");
@@ -274,6 +278,7 @@ int create_world(int n, const int* nx, const int* ny, const int* drops, const ui
   cudaMemsetAsync(w->rec, 0, sizeof(float4) * N, s);
   cudaMemsetAsync(w->trk, 0, sizeof(Tracks) * N, s);
   cudaMemsetAsync(w->cq, 0, sizeof(CellQ) * N, s);
+  cudaMemsetAsync(w->arr, 0, sizeof(unsigned long long) * (size_t)words, s);
   cudaMemsetAsync(w->stats, 0, sizeof(DevStats), s);
   cudaMemsetAsync(w->bar, 0, sizeof(GridBar), s);
   if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "initialise maps");
