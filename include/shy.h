@@ -39,6 +39,7 @@ typedef struct shy_world shy_world;
 #define SHY_ERR_NO_DEVICE (-4)
 #define SHY_ERR_TIMEOUT (-5)   /* a bounded device-side wait gave up */
 #define SHY_ERR_STATE (-6)     /* call not valid in the world's current state */
+#define SHY_ERR_IO (-7)        /* a checkpoint file could not be read or written */
 
 /* Per-cell fields, in the order of quad::cell (source/cellpool.h:207-220). */
 #define SHY_FIELD_HEIGHT 0
@@ -281,6 +282,40 @@ int shy_terrain_generate(shy_world* w, int terrain, uint64_t seed, int octaves);
 int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint64_t seed, uint64_t cycle0,
                       int drops, int cycles, float* height, float* discharge, float* momentum_x,
                       float* momentum_y, const float* root_density, void* stream, shy_stats* stats);
+
+/* ---- Checkpoint and resume (no reference counterpart: the reference keeps
+ *      its state in process memory only) ---------------------------------
+ * shy_world_save writes a world's state between calls -- terrains,
+ * parameters, maps, fixed-point heights, cycle and vegetation-step counters,
+ * counters -- to `path` (through a temporary file renamed into place).
+ * shy_world_load creates a new world on the current device from such a file;
+ * it continues bit for bit as the saved world would have.  The format is
+ * versioned and ends in a hash of its contents; a damaged or foreign file
+ * fails with SHY_ERR_IO. */
+int shy_world_save(shy_world* w, const char* path);
+int shy_world_load(const char* path, shy_world** out);
+
+/* ---- Front-end data feed ---------------------------------------------------
+ * What the reference's front end rebuilds from the maps after every erosion
+ * frame and uploads to OpenGL (SimpleHydrology.cpp:322-355; updatenode,
+ * source/cellpool.h:286-317), written into a plain buffer instead, one record
+ * per cell of terrain `terrain`, cells x-major (x * ny + y):
+ *   SHY_FEED_DISCHARGE_RGBA  4 floats: waterColor (92, 133, 142) / 255
+ *                            (source/model.h:22) and erf(0.4 discharge)
+ *   SHY_FEED_MOMENTUM_RGBA   4 floats: 0.5 (1 + erf(mx)), 0.5 (1 + erf(my)),
+ *                            0.5, 1
+ *   SHY_FEED_VERTICES        12 floats: position (x, mapscale h, y), normal
+ *                            (quad::_normal), tangent T - P and bitangent
+ *                            B - P toward the points at x + 1 and y + 1
+ *                            (heights 0 outside the map)
+ * count must be cells x floats per record.  out_is_device = 1: `out` is a
+ * 16-byte aligned device pointer, written on the world's stream (order with
+ * shy_world_stream or shy_world_sync); 0: `out` is host memory, filled before
+ * the call returns.  erf is the library's correctly rounded erf. */
+#define SHY_FEED_DISCHARGE_RGBA 0
+#define SHY_FEED_MOMENTUM_RGBA 1
+#define SHY_FEED_VERTICES 2
+int shy_feed(shy_world* w, int terrain, int kind, float* out, size_t count, int out_is_device);
 
 /* ---- Measurement ----------------------------------------------------------
  * L2 peaks of one device, measured by the library's own microbenchmarks (no

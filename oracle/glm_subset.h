@@ -2,7 +2,7 @@
 //
 // The reference (SimpleHydrology, source/*.h) is written against glm, which is
 // not installed here. This header supplies the small part of glm's surface that
-// the erosion headers use (vec2, ivec2, vec3, and the free functions length,
+// the erosion headers use (vec2, ivec2, vec3, vec4, and the free functions length,
 // normalize, dot, cross), written from glm's documented semantics:
 //   * component-wise arithmetic, each component rounded to its own type;
 //   * dot(a, b)      = sum of the component products, summed left to right;
@@ -88,8 +88,20 @@ template <typename T> inline tvec3<T> cross(tvec3<T> x, tvec3<T> y) {
   return tvec3<T>(x.y * y.z - y.y * x.z, x.z * y.x - y.z * x.x, x.x * y.y - y.x * x.y);
 }
 
+// vec4 as the front end builds its texels: from four scalars, or from a vec3
+// and a scalar, each converted to the component type
+template <typename T> struct tvec4 {
+  T x, y, z, w;
+  template <typename A, typename B, typename C, typename D>
+  constexpr tvec4(A a, B b, C c, D d)
+      : x(static_cast<T>(a)), y(static_cast<T>(b)), z(static_cast<T>(c)), w(static_cast<T>(d)) {}
+  template <typename S>
+  constexpr tvec4(tvec3<T> v, S s) : x(v.x), y(v.y), z(v.z), w(static_cast<T>(s)) {}
+};
+
 typedef tvec2<float> vec2;
 typedef tvec2<int> ivec2;
 typedef tvec3<float> vec3;
+typedef tvec4<float> vec4;
 
 }  // namespace glm

@@ -766,6 +766,45 @@ void orc_normals_f32(orc_grid_f32* gr, const shy_params* p, float* out3) {
     }
 }
 
+// The front end's per-frame buffers (SimpleHydrology.cpp:341-354; updatenode,
+// source/cellpool.h:286-317): kind 0 the discharge texture
+// vec4(waterColor, erf(0.4 d)) with waterColor = vec3(92, 133, 142) / 255
+// (source/model.h:22), kind 1 the momentum texture
+// vec4(0.5 (1 + erf(mx)), 0.5 (1 + erf(my)), 0.5, 1), kind 2 the mesh
+// vertex of each cell: P = (x, mapscale h, y), quad::_normal, T - P, B - P.
+void orc_feed_f32(orc_grid_f32* gr, const shy_params* p, int kind, int erf_mode, float* out) {
+  Grid<float> g = make_grid<float>(gr);
+  const float ms = p->map_scale;
+  for (int x = 0; x < g.nx; ++x)
+    for (int y = 0; y < g.ny; ++y) {
+      const size_t c = g.at(x, y);
+      if (kind == 0) {
+        float* o = out + 4 * c;
+        o[0] = 92.0f / 255.0f;
+        o[1] = 133.0f / 255.0f;
+        o[2] = 142.0f / 255.0f;
+        o[3] = (float)(double)erf_of(0.4f * g.d[c], erf_mode);  // map.discharge, stored via double
+      } else if (kind == 1) {
+        float* o = out + 4 * c;
+        o[0] = 0.5f * (1.0f + erf_of(g.mx[c], erf_mode));
+        o[1] = 0.5f * (1.0f + erf_of(g.my[c], erf_mode));
+        o[2] = 0.5f;
+        o[3] = 1.0f;
+      } else {
+        float* o = out + 12 * c;
+        const float px = (float)x, py = (float)y;
+        const float hp = ms * g.height(x, y);
+        const V3<float> n = normal(g, x, y, ms);
+        const float tx = (float)(x + 1), ty = ms * g.height(x + 1, y);
+        const float bx = (float)x, by = ms * g.height(x, y + 1), bz = (float)(y + 1);
+        o[0] = px; o[1] = hp; o[2] = py;
+        o[3] = n.x; o[4] = n.y; o[5] = n.z;
+        o[6] = tx - px; o[7] = ty - hp; o[8] = py - py;
+        o[9] = bx - px; o[10] = by - hp; o[11] = bz - py;
+      }
+    }
+}
+
 // Spawn positions as World::erode draws them (source/world.h:69):
 // srand(seed), then two rand() per drop; `order` 0 gives the first draw to x,
 // 1 gives it to y (the compiler picks the argument evaluation order).

@@ -98,6 +98,7 @@ def lib():
         L.orc_drop_descend_f32.argtypes = [P(GridF32), P(Params), P(Drop), C.c_int, P(Acc)]
         L.orc_cascade_f32.argtypes = [P(GridF32), P(Params), C.c_float, C.c_float]
         L.orc_normals_f32.argtypes = [P(GridF32), P(Params), P(C.c_float)]
+        L.orc_feed_f32.argtypes = [P(GridF32), P(Params), C.c_int, C.c_int, P(C.c_float)]
         L.orc_rand_spawns.argtypes = [C.c_uint, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int32)]
         L.orc_erode_batched_f32.argtypes = [P(GridF32), P(Params), C.c_uint64, C.c_uint64, C.c_int,
                                             C.c_int, P(Acc), P(C.c_int64), C.c_int]
@@ -132,6 +133,7 @@ def ref():
         R.ref_normal.argtypes = [C.c_int, C.c_int, P(C.c_float)]
         R.ref_descend_trace.argtypes = [C.c_float, C.c_float, P(C.c_float), C.c_int]
         R.ref_veg_get.argtypes = [P(C.c_float), C.c_int]
+        R.ref_frame.argtypes = [P(C.c_float), P(C.c_float), P(C.c_float)]
         R.ref_init(1)
         _ref = R
     return _ref
@@ -233,6 +235,16 @@ def normals(maps: Maps, params=None):
     out = np.zeros((maps.nx, maps.ny, 3), np.float32)
     g = maps.grid()
     lib().orc_normals_f32(C.byref(g), C.byref(params), fptr(out))
+    return out
+
+
+def feed(maps: Maps, kind, erf_mode=ERF_SHY, params=None):
+    """The front end's per-frame buffer: kind 0 discharge texture, 1 momentum
+    texture (4 floats per cell), 2 mesh vertices (12 floats per cell)."""
+    params = params or default_params()
+    out = np.zeros((maps.nx, maps.ny, 12 if kind == 2 else 4), np.float32)
+    g = maps.grid()
+    lib().orc_feed_f32(C.byref(g), C.byref(params), kind, erf_mode, fptr(out))
     return out
 
 

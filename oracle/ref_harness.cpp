@@ -25,11 +25,15 @@
 using namespace std;
 using namespace glm;
 
-// No-op stand-ins for the render-side types that source/cellpool.h:252-340
-// calls while building its map (the reference gets these from TinyEngine).
+// Stand-ins for the render-side types that source/cellpool.h:252-340 calls
+// while building its map (the reference gets these from TinyEngine).  fill()
+// records the vertex that updatenode (source/cellpool.h:286-317) writes, 12
+// floats per vertex index, when a recording buffer is set.
 struct Vertex {
   Vertex(vec3, vec3, vec3, vec3) {}
 };
+float* g_fill_out = nullptr;
+int g_fill_max = 0;
 template <typename T> struct Vertexpool {
   std::vector<uint> indices;
   uint slot = 0;
@@ -37,7 +41,16 @@ template <typename T> struct Vertexpool {
   void resize(uint*, size_t) {}
   void index() {}
   void update() {}
-  void fill(uint*, int, vec3, vec3, vec3, vec3) {}
+  void fill(uint*, int i, vec3 p, vec3 n, vec3 t, vec3 b) {
+    if (!g_fill_out || i < 0 || i >= g_fill_max) return;
+    float* o = g_fill_out + 12 * (size_t)i;
+    const vec3 v[4] = {p, n, t, b};
+    for (int k = 0; k < 4; ++k) {
+      o[3 * k] = v[k].x;
+      o[3 * k + 1] = v[k].y;
+      o[3 * k + 2] = v[k].z;
+    }
+  }
 };
 
 #include "world.h"
@@ -164,6 +177,35 @@ int ref_veg_get(float* out, int max_plants) {
     out[3 * i + 2] = Vegetation::plants[i].size;
   }
   return n;
+}
+
+// The front end's per-frame data (SimpleHydrology.cpp:322-355): the mesh
+// through the reference's own updatenode (its vertex index is
+// math::flatten(pos, tileres), x-major like the maps), and the two texture
+// lambdas of SimpleHydrology.cpp:341-354 (which need TinyEngine to compile)
+// restated over the reference's map accessors, with waterColor of
+// source/model.h:22.
+void ref_frame(float* vert12, float* dis4, float* mom4) {
+  const int n = quad::tilesize * quad::tilesize;
+  g_fill_out = vert12;
+  g_fill_max = n;
+  for (auto& node : World::map.nodes) updatenode(g_vertexpool, node);
+  g_fill_out = nullptr;
+  const vec3 waterColor = vec3(92, 133, 142) / 255.0f;
+  for (int x = 0; x < quad::tilesize; ++x)
+    for (int y = 0; y < quad::tilesize; ++y) {
+      const ivec2 p(x, y);
+      const size_t i = (size_t)x * quad::tilesize + y;
+      double d = World::map.discharge(p);
+      const vec4 dc = vec4(waterColor, d);
+      auto node = World::map.get(p);
+      auto cell = node->get(p);
+      float mx = cell->momentumx;
+      float my = cell->momentumy;
+      const vec4 mc = vec4(0.5f * (1.0f + erf(mx)), 0.5f * (1.0f + erf(my)), 0.5f, 1.0);
+      dis4[4 * i] = dc.x; dis4[4 * i + 1] = dc.y; dis4[4 * i + 2] = dc.z; dis4[4 * i + 3] = dc.w;
+      mom4[4 * i] = mc.x; mom4[4 * i + 1] = mc.y; mom4[4 * i + 2] = mc.z; mom4[4 * i + 3] = mc.w;
+    }
 }
 
 }  // extern "C"

@@ -18,11 +18,11 @@ import ctypes as C
 import numpy as np
 
 from . import _capi
-from ._capi import (ERF_DEVICE, ERF_HOST_LIBM, FIELD_NAMES, DropState, L2Probe, Params, ShyError, Stats,
-                    Timing, check, default_params, lib)
+from ._capi import (ERF_DEVICE, ERF_HOST_LIBM, FEED_KINDS, FIELD_NAMES, DropState, L2Probe, Params, ShyError,
+                    Stats, Timing, check, default_params, lib)
 
 __all__ = ["World", "Batch", "Drop", "Params", "Stats", "Timing", "ShyError", "default_params",
-           "lib", "measure_l2", "ERF_DEVICE", "ERF_HOST_LIBM", "FIELD_NAMES"]
+           "lib", "load", "measure_l2", "ERF_DEVICE", "ERF_HOST_LIBM", "FIELD_NAMES"]
 
 
 def measure_l2(device: int = 0) -> dict:
@@ -101,6 +101,31 @@ class _Handle:
         s = C.c_void_p()
         check(lib().shy_world_stream(self._w, C.byref(s)))
         return s.value or 0
+
+    def save(self, path):
+        """Write the world's state to a checkpoint file (shy_world_save)."""
+        check(lib().shy_world_save(self._w, str(path).encode()))
+
+    def feed(self, kind: str, terrain: int = 0, out=None):
+        """The front end's per-frame buffer `kind` (discharge_rgba, momentum_rgba
+        or vertices) of one terrain, as a numpy array (nx, ny, 4 or 12).  `out`
+        may be a torch CUDA tensor of that shape (float32, contiguous), which
+        is filled on the device."""
+        k, per = FEED_KINDS[kind]
+        nx, ny = self._terrain_shape(terrain)
+        if out is not None and hasattr(out, "data_ptr"):
+            if tuple(out.shape) != (nx, ny, per) or not out.is_contiguous() or out.element_size() != 4:
+                raise ValueError("out must be a contiguous float32 tensor of shape (nx, ny, %d)" % per)
+            check(lib().shy_feed(self._w, terrain, k, C.c_void_p(out.data_ptr()), nx * ny * per, 1))
+            return out
+        a = np.empty((nx, ny, per), np.float32)
+        check(lib().shy_feed(self._w, terrain, k, a.ctypes.data_as(C.c_void_p), a.size, 0))
+        return a
+
+    def _terrain_shape(self, terrain):
+        nx, ny, d = C.c_int(), C.c_int(), C.c_int()
+        check(lib().shy_terrain_size(self._w, terrain, C.byref(nx), C.byref(ny), C.byref(d)))
+        return nx.value, ny.value
 
     @property
     def params(self) -> Params:
@@ -255,3 +280,27 @@ class Batch(_Handle):
 
     def erode(self, cycles: int = 1):
         check(lib().shy_batch_erode(self._w, cycles))
+
+
+def load(path):
+    """A world resumed from a checkpoint file (shy_world_load): a World for a
+    single terrain, a Batch otherwise."""
+    h = C.c_void_p()
+    check(lib().shy_world_load(str(path).encode(), C.byref(h)))
+    n = C.c_int()
+    check(lib().shy_batch_size(h, C.byref(n)))
+    sizes = []
+    for t in range(n.value):
+        nx, ny, d = C.c_int(), C.c_int(), C.c_int()
+        check(lib().shy_terrain_size(h, t, C.byref(nx), C.byref(ny), C.byref(d)))
+        sizes.append((nx.value, ny.value))
+    if n.value == 1:
+        obj = World.__new__(World)
+        _Handle.__init__(obj)
+        obj.nx, obj.ny = sizes[0]
+    else:
+        obj = Batch.__new__(Batch)
+        _Handle.__init__(obj)
+        obj.sizes = sizes
+    obj._w = h
+    return obj

@@ -37,6 +37,8 @@ KERNEL_DROPS, KERNEL_APPLY, KERNEL_CASCADE, KERNEL_OTHER = 0, 1, 2, 3
 
 ERF_DEVICE = 0
 ERF_HOST_LIBM = 1
+# shy_feed kinds and floats per cell
+FEED_KINDS = {"discharge_rgba": (0, 4), "momentum_rgba": (1, 4), "vertices": (2, 12)}
 
 
 class Params(C.Structure):
@@ -131,6 +133,9 @@ SIGNATURES = {
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     P(Stats)]),
     "shy_measure_l2": (C.c_int, [C.c_int, P(L2Probe)]),
+    "shy_feed": (C.c_int, [W, C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
+    "shy_world_save": (C.c_int, [W, C.c_char_p]),
+    "shy_world_load": (C.c_int, [C.c_char_p, P(W)]),
 }
 
 _lib = None

@@ -142,6 +142,8 @@ struct shy_world {
   long long* dctr = nullptr;  // cascade centre this slot runs this step, -1 if none
   shy::SteepCell* dsteep = nullptr;  // steep-cascade queue (one entry per drop slot at most)
   unsigned long long* arr = nullptr;  // arrivals bitmap, all terrains
+  float* feed = nullptr;              // staging buffer of shy_feed for host output
+  size_t feed_len = 0;
 
   shy::Terrain* dterrains = nullptr;
   shy::DevStats* stats = nullptr;
@@ -200,6 +202,9 @@ struct CycleBuffers {
 // ---- launchers (defined in the .cu files) --------------------------------
 cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream);
 cudaError_t launch_rebuild_records(shy_world* w, int kind_for_timing);
+int world_create(int n, const int* nx, const int* ny, const int* drops, const uint64_t* seeds,
+                 const shy_params* params, shy_world** out);
+void world_free(shy_world* w);
 cudaError_t launch_exact_erode(shy_world* w, int terrain, int n);
 cudaError_t launch_exact_blend(shy_world* w, int terrain);
 cudaError_t launch_drop_descend(shy_world* w, int terrain);

@@ -93,7 +93,7 @@ void free_world(shy_world* w) {
   void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
                   w->dterr, w->dcell, w->dctr, w->dterrains, w->stats, w->bar, w->ddrop,
                   w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down,
-                  w->plant_next, w->rootq, w->veg_claim, w->arr};
+                  w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (w->graph) cudaGraphExecDestroy(w->graph);
@@ -374,6 +374,15 @@ int check_terrain(shy_world* w, int t) {
 }
 
 }  // namespace
+
+namespace shy {
+// world construction and teardown for the other translation units
+int world_create(int n, const int* nx, const int* ny, const int* drops, const uint64_t* seeds,
+                 const shy_params* params, shy_world** out) {
+  return create_world(n, nx, ny, drops, seeds, params, out);
+}
+void world_free(shy_world* w) { free_world(w); }
+}  // namespace shy
 
 extern "C" {
 
