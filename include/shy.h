@@ -283,11 +283,36 @@ int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint64_t seed, u
                       int drops, int cycles, float* height, float* discharge, float* momentum_x,
                       float* momentum_y, const float* root_density, void* stream, shy_stats* stats);
 
+/* ---- The reference's frame loop in its own random sequence ----------------
+ * The reference draws World::erode's spawn positions (source/world.h:69) and
+ * Vegetation::grow's plant events (source/vegetation.h:122-188) from one
+ * C-library rand() stream.  A world carries that generator (the GNU C
+ * library's default rand(), restated) on the device:
+ *   shy_world_srand(w, s)        srand(s) for the world's stream (a stream
+ *                                never seeded behaves as srand(1))
+ *   shy_erode_rand(w, drops)     World::erode(drops) of terrain 0 in the exact
+ *                                (sequential) mode, spawns drawn from the stream
+ *   shy_vegetation_grow(w)       Vegetation::grow() on the world's plant list
+ *   shy_plants(w, out, max, &n)  the plant list, (x, y, size) per plant in
+ *                                list order (at most max copied, n = its size)
+ * so that srand(s) followed by frames of World::erode(n); Vegetation::grow();
+ * is reproduced with the reference's maps and plant list.
+ * shy_world_set_rand_order selects which of the two rand() arguments of one
+ * vector constructor is drawn first: 1 (default) the second one, as g++
+ * evaluates them; 0 the first one.  These are parity paths run by one device
+ * thread, like shy_erode_exact. */
+int shy_world_srand(shy_world* w, uint32_t seed);
+int shy_world_set_rand_order(shy_world* w, int order);
+int shy_erode_rand(shy_world* w, int drops);
+int shy_vegetation_grow(shy_world* w);
+int shy_plants(shy_world* w, float* out, int max_plants, int* count);
+
 /* ---- Checkpoint and resume (no reference counterpart: the reference keeps
  *      its state in process memory only) ---------------------------------
  * shy_world_save writes a world's state between calls -- terrains,
  * parameters, maps, fixed-point heights, cycle and vegetation-step counters,
- * counters -- to `path` (through a temporary file renamed into place).
+ * counters, the C-library random stream and the plant list -- to `path`
+ * (through a temporary file renamed into place).
  * shy_world_load creates a new world on the current device from such a file;
  * it continues bit for bit as the saved world would have.  The format is
  * versioned and ends in a hash of its contents; a damaged or foreign file

@@ -9,6 +9,9 @@
 //   shy_ref::World::cascade({x, y});               // World::cascade, source/world.h:90-168
 //   shy_ref::Drop d({x, y}); while (d.descend());  // source/water.h:58-156
 //   float h = shy_ref::World::map.height({x, y});  // quad::map::height, source/cellpool.h:433-437
+//   shy_ref::World::srand(s);                      // the reference's own sequence:
+//   shy_ref::World::erode_sequential(512);         //   World::erode with rand() spawns
+//   shy_ref::Vegetation::grow();                   //   Vegetation::grow, plant agents
 //
 // World::erode runs the batched GPU mode (all drops of the call at once);
 // World::erode_exact runs the reference's sequential semantics on the GPU.
@@ -110,6 +113,32 @@ class World {
   }
   // World::cascade(vec2 pos)
   static void cascade(vec2 pos) { check(shy_cascade(map.w, pos.x, pos.y)); }
+  // srand(seed) and World::erode(n) in the reference's own sequence: spawns
+  // drawn from the world's C-library rand() stream, drops run one after
+  // another (source/world.h:64-78)
+  static void srand(unsigned seed) { check(shy_world_srand(map.w, seed)); }
+  static void erode_sequential(int drops) { check(shy_erode_rand(map.w, drops)); }
+};
+
+// struct Plant (source/vegetation.h:12-36), as the plant list returns it.
+struct Plant {
+  vec2 pos;
+  float size;
+};
+
+// struct Vegetation (source/vegetation.h:45-50): grow() runs the reference's
+// plant agents on the world's rand() stream; plants() reads the list.
+struct Vegetation {
+  static void grow() { check(shy_vegetation_grow(World::map.w)); }
+  static std::vector<Plant> plants() {
+    int n = 0;
+    check(shy_plants(World::map.w, nullptr, 0, &n));
+    std::vector<float> buf(3 * (size_t)n);
+    if (n) check(shy_plants(World::map.w, buf.data(), n, &n));
+    std::vector<Plant> out((size_t)n);
+    for (int i = 0; i < n; ++i) out[i] = {{buf[3 * i], buf[3 * i + 1]}, buf[3 * i + 2]};
+    return out;
+  }
 };
 
 // struct Drop, source/water.h:12-39.

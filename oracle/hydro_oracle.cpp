@@ -595,6 +595,77 @@ struct Lockstep {
 };
 
 // ---------------------------------------------------------------------------
+// The reference's plant agents (source/vegetation.h:12-188) and its frame
+// loop's random stream.  Vegetation::grow draws from the same C-library
+// rand() as World::erode's spawns (source/world.h:69), so a frame
+// `World::erode(n); Vegetation::grow();` after srand(seed) is one sequence of
+// draws; shy_crand (shy_math.h) restates that generator.  `order` is the
+// evaluation order of the two rand() arguments of one vector constructor
+// (world.h:69 and vegetation.h:162): 0 left to right, 1 right to left (g++).
+
+struct PlantA {
+  float x, y, size;
+};
+
+// Plant::root(f), source/vegetation.h:87-118: the 3 x 3 kernel in the
+// reference's order, skipping cells outside the map.
+template <class T> void plant_root(Grid<T>& g, const PlantA& p, float f) {
+  static const int off[9][2] = {{0, 0}, {1, 0}, {-1, 0}, {0, 1}, {0, -1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1}};
+  static const float wgt[9] = {1.0f, 0.6f, 0.6f, 0.6f, 0.6f, 0.4f, 0.4f, 0.4f, 0.4f};
+  for (int k = 0; k < 9; ++k) {
+    const int x = (int)(p.x + (float)off[k][0]), y = (int)(p.y + (float)off[k][1]);
+    if (g.oob(x, y)) continue;
+    g.root[g.at(x, y)] += f * wgt[k];
+  }
+}
+
+// quad::map::discharge (source/cellpool.h:439-443): erf(0.4 d), 0 outside
+template <class T> float map_discharge(const Grid<T>& g, int x, int y, int erf_mode) {
+  return g.oob(x, y) ? 0.0f : erf_of(0.4f * (float)g.d[g.at(x, y)], erf_mode);
+}
+
+// Vegetation::grow, source/vegetation.h:122-188.
+template <class T>
+void vegetation_grow(Grid<T>& g, const shy_params& P, shy_crand* rnd, std::vector<PlantA>& plants, int order,
+                     int erf_mode) {
+  {  // :126-139, a random position
+    const int x = shy_crand_next(rnd) % g.nx;
+    const int y = shy_crand_next(rnd) % g.ny;
+    // Plant::spawn, :76-85
+    if (!(map_discharge(g, x, y, erf_mode) >= P.plant_max_discharge) &&
+        !(normal(g, x, y, P.map_scale).y < P.plant_max_steep) && !(g.height(x, y) >= P.plant_max_height)) {
+      plants.push_back({(float)x, (float)y, 0.0f});
+      plant_root(g, plants.back(), 1.0f);
+    }
+  }
+  for (size_t i = 0; i < plants.size(); ++i) {  // :143-183
+    PlantA& p = plants[i];
+    p.size = p.size + P.plant_grow_rate * (P.plant_max_size - p.size);  // Plant::grow, :63-65
+    const int cx = (int)p.x, cy = (int)p.y;
+    // Plant::die, :67-74 (short-circuit: rand() only when both tests pass)
+    const bool die = map_discharge(g, cx, cy, erf_mode) >= P.plant_max_discharge ||
+                     g.height(cx, cy) >= P.plant_max_height || shy_crand_next(rnd) % 1000 == 0;
+    if (die) {
+      plant_root(g, p, -1.0f);
+      plants.erase(plants.begin() + (long)i);
+      --i;
+      continue;
+    }
+    if (shy_crand_next(rnd) % 20 != 0) continue;  // :160
+    const int r1 = shy_crand_next(rnd), r2 = shy_crand_next(rnd);
+    const int dx = (order == 0 ? r1 : r2) % 9 - 4, dy = (order == 0 ? r2 : r1) % 9 - 4;  // :162
+    const float nx = p.x + (float)dx, ny = p.y + (float)dy;
+    const int ix = (int)nx, iy = (int)ny;
+    if (g.oob(ix, iy)) continue;                                                    // :165
+    if (map_discharge(g, ix, iy, erf_mode) >= P.plant_max_discharge) continue;      // :168
+    if ((double)(float)(shy_crand_next(rnd) % 1000) / 1000.0 <= (double)g.root[g.at(ix, iy)]) continue;  // :171
+    if (normal(g, ix, iy, P.map_scale).y <= P.plant_max_steep) continue;            // :174-177
+    plants.push_back({nx, ny, 0.0f});
+    plant_root(g, plants.back(), 1.0f);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Per-cell vegetation: the GPU engine's restatement of Vegetation::grow
 // (source/vegetation.h:122-188).  Every cell holds at most one plant (size
 // > 0); one call is one grow() of every plant, in parallel, against the maps
@@ -803,6 +874,41 @@ void orc_feed_f32(orc_grid_f32* gr, const shy_params* p, int kind, int erf_mode,
         o[9] = bx - px; o[10] = by - hp; o[11] = bz - py;
       }
     }
+}
+
+// The restated C-library generator: n outputs after seeding.
+void orc_crand(unsigned seed, int n, int* out) {
+  shy_crand g;
+  shy_crand_seed(&g, seed);
+  for (int i = 0; i < n; ++i) out[i] = shy_crand_next(&g);
+}
+
+// The reference's frame loop from srand(seed): `frames` times
+// World::erode(drops) with spawns from the stream (source/world.h:64-78),
+// then Vegetation::grow().  The plant list starts empty; it comes back as
+// (x, y, size) triples in list order (at most max_plants); returns its size.
+int orc_frames_f32(orc_grid_f32* gr, const shy_params* p, unsigned seed, int frames, int drops, int order,
+                   int erf_mode, float* plants_out, int max_plants, orc_acc* acc) {
+  Grid<float> g = make_grid<float>(gr);
+  shy_crand rnd;
+  shy_crand_seed(&rnd, seed);
+  std::vector<PlantA> plants;
+  std::vector<int32_t> sp((size_t)2 * (drops > 0 ? drops : 0));
+  for (int f = 0; f < frames; ++f) {
+    for (int i = 0; i < drops; ++i) {
+      const int r1 = shy_crand_next(&rnd), r2 = shy_crand_next(&rnd);
+      sp[2 * i] = (order == 0 ? r1 : r2) % g.nx;
+      sp[2 * i + 1] = (order == 0 ? r2 : r1) % g.ny;
+    }
+    erode_seq(g, *p, sp.data(), drops, erf_mode, acc);
+    vegetation_grow(g, *p, &rnd, plants, order, erf_mode);
+  }
+  for (size_t i = 0; i < plants.size() && (int)i < max_plants; ++i) {
+    plants_out[3 * i] = plants[i].x;
+    plants_out[3 * i + 1] = plants[i].y;
+    plants_out[3 * i + 2] = plants[i].size;
+  }
+  return (int)plants.size();
 }
 
 // Spawn positions as World::erode draws them (source/world.h:69):

@@ -99,6 +99,10 @@ def lib():
         L.orc_cascade_f32.argtypes = [P(GridF32), P(Params), C.c_float, C.c_float]
         L.orc_normals_f32.argtypes = [P(GridF32), P(Params), P(C.c_float)]
         L.orc_feed_f32.argtypes = [P(GridF32), P(Params), C.c_int, C.c_int, P(C.c_float)]
+        L.orc_crand.argtypes = [C.c_uint, C.c_int, P(C.c_int)]
+        L.orc_frames_f32.argtypes = [P(GridF32), P(Params), C.c_uint, C.c_int, C.c_int, C.c_int, C.c_int,
+                                     P(C.c_float), C.c_int, P(Acc)]
+        L.orc_frames_f32.restype = C.c_int
         L.orc_rand_spawns.argtypes = [C.c_uint, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int32)]
         L.orc_erode_batched_f32.argtypes = [P(GridF32), P(Params), C.c_uint64, C.c_uint64, C.c_int,
                                             C.c_int, P(Acc), P(C.c_int64), C.c_int]
@@ -246,6 +250,25 @@ def feed(maps: Maps, kind, erf_mode=ERF_SHY, params=None):
     g = maps.grid()
     lib().orc_feed_f32(C.byref(g), C.byref(params), kind, erf_mode, fptr(out))
     return out
+
+
+def crand(seed, n):
+    """n outputs of the restated C-library rand() after srand(seed)."""
+    out = np.zeros(n, np.int32)
+    lib().orc_crand(seed, n, out.ctypes.data_as(C.POINTER(C.c_int)))
+    return out
+
+
+def frames(maps: Maps, seed, n_frames, drops, order=1, erf_mode=ERF_LIBM, params=None, max_plants=1 << 20):
+    """The reference's frame loop (World::erode(drops); Vegetation::grow()) from
+    srand(seed); returns the plant list (n, 3) and the counters."""
+    params = params or default_params()
+    out = np.zeros((max_plants, 3), np.float32)
+    acc = Acc()
+    g = maps.grid()
+    n = lib().orc_frames_f32(C.byref(g), C.byref(params), seed, n_frames, drops, order, erf_mode, fptr(out),
+                             max_plants, C.byref(acc))
+    return out[:min(n, max_plants)].copy(), acc
 
 
 def rand_spawns(seed, n, nx, ny, order):

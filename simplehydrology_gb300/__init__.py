@@ -174,6 +174,28 @@ class World(_Handle):
         sp = np.ascontiguousarray(np.asarray(spawns, np.int32).reshape(-1, 2))
         check(lib().shy_erode_exact(self._w, sp.ctypes.data_as(C.POINTER(C.c_int32)), len(sp)))
 
+    # ---- the reference's frame loop in its own random sequence ----
+    def srand(self, seed: int):
+        """srand(seed) for the world's C-library random stream."""
+        check(lib().shy_world_srand(self._w, seed))
+
+    def erode_rand(self, drops: int):
+        """World::erode(drops), sequential, spawns from the world's stream."""
+        check(lib().shy_erode_rand(self._w, drops))
+
+    def grow(self):
+        """Vegetation::grow() on the world's plant list."""
+        check(lib().shy_vegetation_grow(self._w))
+
+    def plants(self):
+        """The plant list as (n, 3) float32: x, y, size."""
+        n = C.c_int()
+        check(lib().shy_plants(self._w, None, 0, C.byref(n)))
+        out = np.zeros((n.value, 3), np.float32)
+        if n.value:
+            check(lib().shy_plants(self._w, _fptr(out), n.value, C.byref(n)))
+        return out
+
     def cascade(self, pos):
         check(lib().shy_cascade(self._w, float(pos[0]), float(pos[1])))
 

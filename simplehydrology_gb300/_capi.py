@@ -135,6 +135,11 @@ SIGNATURES = {
     "shy_measure_l2": (C.c_int, [C.c_int, P(L2Probe)]),
     "shy_feed": (C.c_int, [W, C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
     "shy_world_save": (C.c_int, [W, C.c_char_p]),
+    "shy_world_srand": (C.c_int, [W, C.c_uint32]),
+    "shy_world_set_rand_order": (C.c_int, [W, C.c_int]),
+    "shy_erode_rand": (C.c_int, [W, C.c_int]),
+    "shy_vegetation_grow": (C.c_int, [W]),
+    "shy_plants": (C.c_int, [W, FP, C.c_int, P(C.c_int)]),
     "shy_world_load": (C.c_int, [C.c_char_p, P(W)]),
 }
 

@@ -10,7 +10,7 @@
 //             u32 n_terrains; u32 flags (bit 0: fixed-point heights valid);
 //             u64 cycle; u64 vegetation step; i32 erf source; i32 erf source
 //             of the records; i32 track mode; u32 sizeof(shy_params);
-//             u32 sizeof(cell record); u32 reserved; u64 cells
+//             u32 sizeof(cell record); i32 rand() argument order; u64 cells
 //   params    shy_params as in shy.h
 //   terrains  per terrain: i32 nx, i32 ny, i32 drops per cycle, u32 0,
 //             u64 seed
@@ -21,7 +21,9 @@
 //             size f32, 4 tracks 3 x f32, 5 records 4 x f32 (momentum x, y,
 //             discharge, 1 + entrainment erf(0.4 d)), 6 deposition rate f32,
 //             7 cell records (i64 fixed-point height, i64 0, f32 deposition
-//             rate, i32 0, i32 0, i32 0)
+//             rate, i32 0, i32 0, i32 0); then 8 the C-library random stream
+//             (31 x i32 state, i32 front, i32 back; 0 bytes if never used) and
+//             9 the plant agents (x, y, size) x f32 in list order
 //   trailer   u64 FNV-1a hash of every byte before it
 #include <cstdio>
 #include <cstring>
@@ -42,7 +44,8 @@ struct Header {
   uint32_t version, abi, n_terrains, flags;
   uint64_t cycle, veg_step;
   int32_t erf_source, ceq_source, track_mode;
-  uint32_t params_size, cellq_size, reserved;
+  uint32_t params_size, cellq_size;
+  int32_t rand_order;
   uint64_t cells;
 };
 struct TerrainRec {
@@ -84,7 +87,7 @@ struct Reader {
   }
 };
 
-enum ArrayId : uint32_t { A_H = 1, A_ROOT, A_PLANT, A_TRACKS, A_REC, A_EFFD, A_CELLQ };
+enum ArrayId : uint32_t { A_H = 1, A_ROOT, A_PLANT, A_TRACKS, A_REC, A_EFFD, A_CELLQ, A_CRAND, A_AGENTS };
 
 struct ArrayDesc {
   uint32_t id;
@@ -127,6 +130,7 @@ extern "C" int shy_world_save(shy_world* w, const char* path) {
   h.track_mode = w->track_mode;
   h.params_size = sizeof(shy_params);
   h.cellq_size = sizeof(CellQ);
+  h.rand_order = w->rand_order;
   h.cells = (uint64_t)w->cells;
   Writer out;
   out.put(&h, sizeof(h));
@@ -157,6 +161,26 @@ extern "C" int shy_world_save(shy_world* w, const char* path) {
     out.put(id, sizeof(id));
     out.put(&bytes, sizeof(bytes));
     out.put(tmp.data(), a.bytes);
+  }
+  {  // the random stream and the plant agents
+    const uint32_t id[2] = {A_CRAND, 0u};
+    const uint64_t bytes = w->crand ? sizeof(shy_crand) : 0;
+    out.put(id, sizeof(id));
+    out.put(&bytes, sizeof(bytes));
+    if (bytes) {
+      shy_crand g;
+      SHY_CHECK_CUDA(cudaMemcpy(&g, w->crand, sizeof(g), cudaMemcpyDeviceToHost), "shy_world_save: read stream");
+      out.put(&g, sizeof(g));
+    }
+    const uint32_t id2[2] = {A_AGENTS, 0u};
+    const uint64_t pbytes = sizeof(float3) * (uint64_t)w->plant_count;
+    out.put(id2, sizeof(id2));
+    out.put(&pbytes, sizeof(pbytes));
+    if (pbytes) {
+      tmp.resize(pbytes);
+      SHY_CHECK_CUDA(cudaMemcpy(tmp.data(), w->plants, pbytes, cudaMemcpyDeviceToHost), "shy_world_save: read plants");
+      out.put(tmp.data(), pbytes);
+    }
   }
   const uint64_t hash = fnv1a(1469598103934665603ull, out.buf.data(), out.buf.size());
   out.put(&hash, sizeof(hash));
@@ -250,6 +274,32 @@ extern "C" int shy_world_load(const char* path, shy_world** out) {
     if (e != cudaSuccess) return fail(cuda_fail(e, "shy_world_load: upload"), cudaGetErrorString(e));
     r.off += a.bytes;
   }
+  {  // the random stream and the plant agents
+    uint32_t id[2];
+    uint64_t bytes;
+    if (!r.get(id, sizeof(id)) || !r.get(&bytes, sizeof(bytes)) || id[0] != A_CRAND ||
+        (bytes != 0 && bytes != sizeof(shy_crand)) || bytes > r.n - r.off)
+      return fail(SHY_ERR_IO, "random stream record damaged");
+    if (bytes) {
+      cudaError_t e = cudaMalloc((void**)&w->crand, sizeof(shy_crand));
+      if (e == cudaSuccess) e = cudaMemcpy(w->crand, buf.data() + r.off, sizeof(shy_crand), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return fail(cuda_fail(e, "shy_world_load: upload"), cudaGetErrorString(e));
+      r.off += bytes;
+    }
+    if (!r.get(id, sizeof(id)) || !r.get(&bytes, sizeof(bytes)) || id[0] != A_AGENTS ||
+        bytes % sizeof(float3) != 0 || bytes > r.n - r.off || bytes / sizeof(float3) > (1u << 30))
+      return fail(SHY_ERR_IO, "plant list record damaged");
+    const long long np = (long long)(bytes / sizeof(float3));
+    if (np > 0) {
+      const long long cap = 4 * (np + 1) + 4096;
+      cudaError_t e = cudaMalloc((void**)&w->plants, sizeof(float3) * (size_t)cap);
+      if (e == cudaSuccess) e = cudaMemcpy(w->plants, buf.data() + r.off, bytes, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return fail(cuda_fail(e, "shy_world_load: upload"), cudaGetErrorString(e));
+      w->plant_cap = (int)cap;
+      w->plant_count = (int)np;
+      r.off += bytes;
+    }
+  }
   if (r.off != r.n) return fail(SHY_ERR_IO, "trailing bytes");
   GridBar bar;
   std::memset(&bar, 0, sizeof(bar));
@@ -272,6 +322,7 @@ extern "C" int shy_world_load(const char* path, shy_world** out) {
   w->erf_source = h.erf_source;
   w->ceq_source = h.ceq_source;
   w->track_mode = h.track_mode;
+  w->rand_order = h.rand_order == 0 ? 0 : 1;
   w->hq_stale = (h.flags & 1u) == 0;
   *out = w;
   return SHY_OK;

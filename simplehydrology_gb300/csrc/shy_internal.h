@@ -9,6 +9,8 @@
 
 #include "../../include/shy.h"
 
+struct shy_crand;  // the C-library generator state (shy_math.h)
+
 namespace shy {
 
 // One terrain of a world, as the kernels see it.  A world holds one or more
@@ -144,6 +146,12 @@ struct shy_world {
   unsigned long long* arr = nullptr;  // arrivals bitmap, all terrains
   float* feed = nullptr;              // staging buffer of shy_feed for host output
   size_t feed_len = 0;
+  // the reference's frame loop: C-library random stream and plant agents
+  shy_crand* crand = nullptr;         // device generator state (seeded lazily with 1)
+  int rand_order = 1;                 // evaluation order of two rand() arguments (1: g++'s)
+  float3* plants = nullptr;           // (x, y, size) per plant, list order
+  int plant_cap = 0;
+  int plant_count = 0;
 
   shy::Terrain* dterrains = nullptr;
   shy::DevStats* stats = nullptr;
@@ -205,6 +213,10 @@ cudaError_t launch_rebuild_records(shy_world* w, int kind_for_timing);
 int world_create(int n, const int* nx, const int* ny, const int* drops, const uint64_t* seeds,
                  const shy_params* params, shy_world** out);
 void world_free(shy_world* w);
+int world_check(shy_world* w);
+// exact-mode World::erode of terrain t with the n spawns already in w->dspawn
+int ensure_spawn_capacity(shy_world* w, int n);
+int exact_erode_device_spawns(shy_world* w, int t, int n);
 cudaError_t launch_exact_erode(shy_world* w, int terrain, int n);
 cudaError_t launch_exact_blend(shy_world* w, int terrain);
 cudaError_t launch_drop_descend(shy_world* w, int terrain);

@@ -283,3 +283,39 @@ SHY_HD float shy_evap_div(float s, const shy_evap* E) {
   const uint64_t mant = x >> (lead - 23);
   return SHY_AS_FLOAT(((uint32_t)be << 23) | ((uint32_t)mant & 0x7FFFFFu));
 }
+
+// The C library's rand() as the reference's process draws it (spawn
+// positions, source/world.h:69; plant events, source/vegetation.h:67-182):
+// the GNU C library's default generator, an additive lagged-Fibonacci
+// generator of degree 31 with lags 3 and 31 (its "TYPE_3" random_r).
+// srand(seed): r[0] = seed (1 if 0), r[i] = 16807 r[i-1] mod (2^31 - 1) by
+// Schrage's method for i = 1..30, then 310 outputs are discarded.  Each
+// output adds the word 31 places back into the word 3 places back (32-bit
+// wrap-around), stores the sum and returns it shifted right by one bit.
+typedef struct shy_crand {
+  int32_t r[31];
+  int32_t f, b;  // front (r[f] += r[b]) and back indices
+} shy_crand;
+
+SHY_HD int shy_crand_next(shy_crand* g) {
+  const uint32_t v = (uint32_t)g->r[g->f] + (uint32_t)g->r[g->b];
+  g->r[g->f] = (int32_t)v;
+  g->f = g->f == 30 ? 0 : g->f + 1;
+  g->b = g->b == 30 ? 0 : g->b + 1;
+  return (int)(v >> 1);
+}
+
+SHY_HD void shy_crand_seed(shy_crand* g, uint32_t seed) {
+  if (seed == 0) seed = 1;
+  int32_t word = (int32_t)seed;  // the seed as a signed 32-bit word
+  g->r[0] = word;
+  for (int i = 1; i < 31; ++i) {
+    const int64_t hi = word / 127773, lo = word % 127773;
+    word = (int32_t)(16807 * lo - 2836 * hi);
+    if (word < 0) word += 2147483647;
+    g->r[i] = word;
+  }
+  g->f = 3;
+  g->b = 0;
+  for (int i = 0; i < 310; ++i) (void)shy_crand_next(g);
+}

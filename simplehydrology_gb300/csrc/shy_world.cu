@@ -93,7 +93,7 @@ void free_world(shy_world* w) {
   void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
                   w->dterr, w->dcell, w->dctr, w->dterrains, w->stats, w->bar, w->ddrop,
                   w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down,
-                  w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed};
+                  w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed, w->crand, w->plants};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (w->graph) cudaGraphExecDestroy(w->graph);
@@ -382,6 +382,7 @@ int world_create(int n, const int* nx, const int* ny, const int* drops, const ui
   return create_world(n, nx, ny, drops, seeds, params, out);
 }
 void world_free(shy_world* w) { free_world(w); }
+int world_check(shy_world* w) { return check_world(w); }
 }  // namespace shy
 
 extern "C" {
@@ -694,17 +695,31 @@ int shy_terrain_erode_exact(shy_world* w, int t, const int32_t* spawn_xy, int n)
                 T.nx, T.ny);
       return SHY_ERR_INVALID_ARG;
     }
-  if ((rc = ensure_ceq(w, w->erf_source)) != SHY_OK) return rc;
-  if (n > w->dspawn_cap) {
-    if (w->dspawn) cudaFree(w->dspawn);
-    w->dspawn = nullptr;
-    w->dspawn_cap = 0;
-    SHY_CHECK_CUDA(dalloc(&w->dspawn, (size_t)n), "allocate spawn list");
-    w->dspawn_cap = n;
-  }
+  if ((rc = ensure_spawn_capacity(w, n)) != SHY_OK) return rc;
   if (n > 0)
     SHY_CHECK_CUDA(cudaMemcpyAsync(w->dspawn, spawn_xy, sizeof(int2) * n, cudaMemcpyHostToDevice, w->stream),
                    "upload spawns");
+  return exact_erode_device_spawns(w, t, n);
+}
+
+}  // extern "C"
+
+namespace shy {
+
+int ensure_spawn_capacity(shy_world* w, int n) {
+  if (n <= w->dspawn_cap) return SHY_OK;
+  if (w->dspawn) cudaFree(w->dspawn);
+  w->dspawn = nullptr;
+  w->dspawn_cap = 0;
+  SHY_CHECK_CUDA(dalloc(&w->dspawn, (size_t)n), "allocate spawn list");
+  w->dspawn_cap = n;
+  return SHY_OK;
+}
+
+int exact_erode_device_spawns(shy_world* w, int t, int n) {
+  int rc;
+  if ((rc = ensure_ceq(w, w->erf_source)) != SHY_OK) return rc;
+  const Terrain& T = w->terrains[t];
   const long long b = T.cell_base, N = w->cells, cn = (long long)T.nx * T.ny;
   for (int k = 0; k < 3; ++k)  // source/world.h:56-61
     SHY_CHECK_CUDA(cudaMemsetAsync(w->track_f + k * N + b, 0, sizeof(float) * cn, w->stream), "zero tracks");
@@ -715,6 +730,10 @@ int shy_terrain_erode_exact(shy_world* w, int t, const int32_t* spawn_xy, int n)
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
   return SHY_OK;
 }
+
+}  // namespace shy
+
+extern "C" {
 
 int shy_erode_exact(shy_world* w, const int32_t* spawn_xy, int n) {
   return shy_terrain_erode_exact(w, 0, spawn_xy, n);

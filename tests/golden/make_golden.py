@@ -15,6 +15,13 @@ Drop::descend, World::cascade, quad::map::normal -- on the reference's
                    cell fields after every call, field sums, the budget
   ref_cascade.json World::cascade at 10 positions of a rough map
   ref_normals.json SHA-256 of quad::map::normal over the whole terrain
+  ref_frames.json  the front end's frame loop: srand(5), then 40 times
+                   World::erode(512); Vegetation::grow(); -- SHA-256 of all 8
+                   cell fields and of the plant list (x, y, size per plant),
+                   and the plant count
+  ref_feed.json    the per-frame buffers on the map after those frames: the
+                   mesh written by the reference's updatenode and the two
+                   textures over its map accessors (SHA-256 each)
 
 The input terrain is the workloads' value noise (seed 1) written over the
 reference's own map after World::map.init.  Values that go through erf (the
@@ -108,6 +115,30 @@ def main():
             nm[x, y] = out
     normals = {"sha": sha(nm)}
 
+    # the frame loop: erosion and plant agents from one rand() stream
+    frames = {"seed": 5, "frames": 40, "drops": 512, "terrain_seed": 11, "order": order}
+    fm = po.Maps(N, N, height=po.value_noise(N, N, frames["terrain_seed"]))
+    po.ref_set_maps(fm)
+    R.ref_veg_clear()
+    R.ref_srand(frames["seed"])
+    for _ in range(frames["frames"]):
+        R.ref_erode(frames["drops"])
+        R.ref_veg_grow()
+    fmaps = po.ref_get_maps()
+    pl = np.zeros((1 << 16, 3), np.float32)
+    n_pl = R.ref_veg_get(po.fptr(pl), 1 << 16)
+    frames["field_sha"] = {f: sha(fmaps.f[k]) for k, f in enumerate(po.FIELDS)}
+    frames["plants"] = n_pl
+    frames["plants_sha"] = sha(pl[:n_pl])
+    R.ref_veg_clear()
+
+    v = np.zeros((N, N, 12), np.float32)
+    d4 = np.zeros((N, N, 4), np.float32)
+    m4 = np.zeros((N, N, 4), np.float32)
+    R.ref_frame(po.fptr(v), po.fptr(d4), po.fptr(m4))
+    feed = {"on": "the map after the frame loop of ref_frames.json", "vertices_sha": sha(v),
+            "discharge_rgba_sha": sha(d4), "momentum_rgba_sha": sha(m4)}
+
     meta = {"generator": "tests/golden/make_golden.py", "map": N, "terrain_seed": SEED,
             "machine": platform.machine(), "libc": " ".join(platform.libc_ver())}
     np.savez_compressed(os.path.join(HERE, "ref_traces.npz"),
@@ -121,6 +152,10 @@ def main():
         json.dump({"meta": meta, **cascade}, f, indent=1)
     with open(os.path.join(HERE, "ref_normals.json"), "w") as f:
         json.dump({"meta": meta, **normals}, f, indent=1)
+    with open(os.path.join(HERE, "ref_frames.json"), "w") as f:
+        json.dump({"meta": meta, **frames}, f, indent=1)
+    with open(os.path.join(HERE, "ref_feed.json"), "w") as f:
+        json.dump({"meta": meta, **feed}, f, indent=1)
     print("wrote fixtures:", sorted(os.listdir(HERE)))
 
 
