@@ -9,7 +9,7 @@ scatter, lrate blend and cascade.  One step = one erosion cycle
 dataset; the terrain recipe stands in for the reference's FastNoiseLite map.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload plain|batch]
+                  [--workload plain|batch|converge]
 
 `value` is device throughput with the maps resident in HBM; between timed
 steps the L2 is flushed by writing a 256 MiB buffer (untimed).  `e2e` is the
@@ -23,6 +23,9 @@ drop-step) against the HBM copy peak; `roofline_l2` takes the same bytes, and
 on the GPU at hand (shy_measure_l2), which bound the kernel while a
 terrain's cell state fits in L2.  `cycle_gbs` adds the 80 B per cell of the
 end-of-cycle pass over the whole step time.
+
+`--workload converge` measures the plain method's time to converged
+discharge (within 5 % log-L2 of the discharge after 4 x 500 cycles).
 
 `--workload batch` runs the batched-terrain configuration instead: 64
 terrains, sides log-uniform in [128, 1024], 0.25 drops per cell per cycle,
@@ -448,6 +451,69 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_converge(args):
+    """Time to converged discharge of the plain method: the discharge map
+    after k cycles against the one after `--ref-cycles` cycles (4 x the
+    500-cycle workload by default), distance ||log1p(D_k) - log1p(D*)|| /
+    ||log1p(D*)||; converged at the first k where it is at most 5 %.  The
+    batched mode is deterministic, so one run gives D* and every D_k; the
+    time is the device time of the first k cycles (CUDA events)."""
+    import numpy as np
+    import torch
+
+    import simplehydrology_gb300 as shy
+    from simplehydrology_gb300 import build as shybuild
+    shybuild.build()
+    dev = torch.cuda.current_device()
+    n, drops = args.map, args.drops
+    w = shy.World(n, n, seed=SEED)
+    w.generate(SEED, 8)
+    stream = torch.cuda.ExternalStream(w.stream())
+    snaps, ms, diag = [], [], []
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    every = args.check_every
+    steps0 = 0
+    for c0 in range(0, args.ref_cycles, every):
+        k = min(every, args.ref_cycles - c0)
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+        w.erode(drops, k)
+        with torch.cuda.stream(stream):
+            ev[1].record(stream)
+        torch.cuda.synchronize()
+        ms.append(ev[0].elapsed_time(ev[1]))
+        d = w.get_field("discharge").astype(np.float64)
+        snaps.append(np.log1p(d))
+        h = w.get_field("height")
+        st = w.stats()
+        diag.append({"cycle": c0 + k, "height_mean": round(float(h.mean()), 5),
+                     "cells_ge_0.1": round(float((h >= 0.1).mean()), 4), "discharge_mean": float(d.mean()),
+                     "drop_steps_per_cycle": (st.drop_steps - steps0) / k})
+        steps0 = st.drop_steps
+    ref = snaps[-1]
+    norm = float(np.linalg.norm(ref))
+    # D* is meaningless once the terrain has worn below the spawn threshold
+    # everywhere (source/world.h:71): no drop spawns and discharge decays to 0
+    degenerate = diag[-1]["cells_ge_0.1"] == 0.0 or diag[-1]["drop_steps_per_cycle"] == 0
+    dist = [float(np.linalg.norm(s - ref)) / norm if norm > 0 else float("inf") for s in snaps[:-1]]
+    k_conv = None if degenerate else next((i for i, d in enumerate(dist) if d <= 0.05), None)
+    cycles = (k_conv + 1) * every if k_conv is not None else None
+    t = sum(ms[:k_conv + 1]) / 1e3 if k_conv is not None else None
+    out = {"metric": "time to converged discharge (<=5% log-L2), plain method", "value": t, "unit": "s",
+           "higher_is_better": False, "cycles_to_converge": cycles, "reference_cycles": args.ref_cycles,
+           "log_l2_at_checks": [round(d, 5) for d in dist[:: max(1, len(dist) // 20)]],
+           "diagnostics": diag[:: max(1, len(diag) // 20)],
+           "ms_per_cycle": sum(ms) / args.ref_cycles, "n_gpus": 1, "dtype": "f32",
+           "data": "synthetic (seeded value-noise terrain, counter-based spawns)",
+           "config": {"workload": f"plain method, GPU batched: {n}x{n} value-noise terrain, {drops} drops/cycle",
+                      "check_every_cycles": every},
+           "surrogate": "not built (no reference counterpart)"}
+    if degenerate:
+        out["degenerate"] = ("after %d cycles no cell is at height >= 0.1, so every spawn is skipped "
+                             "(source/world.h:71) and the reference discharge D* has decayed to ~0" % args.ref_cycles)
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -461,13 +527,17 @@ def main():
     ap.add_argument("--drops", type=int, default=DROPS)
     ap.add_argument("--no-e2e", action="store_true")
     # the batched-terrain configuration (not the default bench line)
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "converge"])
+    ap.add_argument("--ref-cycles", type=int, default=2000)
+    ap.add_argument("--check-every", type=int, default=10)
     ap.add_argument("--terrains", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "converge":
+        run_converge(args)
     else:
         run_ours(args)
 
