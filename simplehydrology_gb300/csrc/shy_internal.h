@@ -61,16 +61,16 @@ struct DevStats {
 };
 
 // A cascade of the current step that will move height: its centre, the
-// nine heights it starts from and the overlap counts of its 3 x 3 block
-// (cascades of the step whose blocks hold the cell: the centre's, and 4 bits
-// per neighbour).
+// nine heights it starts from, and the arrivals-bitmap words around it from
+// which its overlap counts are taken (aw[2 * i + j]: tile column tx0 + i,
+// tile row ty0 + j).
 struct alignas(16) SteepCell {
   long long c2;
   int ti;
   float h0;
   float v[8];
-  unsigned kv;
-  int kc;
+  unsigned long long aw[4];
+  int tx0, ty0, ix, iy;
 };
 
 // Grid barrier state of the persistent lock-step kernel.

@@ -16,18 +16,18 @@
 //      cell's cascade.
 //   scan  World::cascade (source/world.h:90-168) at every claimed cell reads
 //      the nine heights phase descend left (fixed point plus pending sum).
-//      Cascades that move nothing end here.  The steep ones read this step's
-//      claimed centres in the 5 x 5 block around theirs (an arrivals bitmap
-//      in 8 x 8-cell words, loaded with the heights) and are queued in the
-//      CTA with the heights they read and their overlap counts: where the
-//      3 x 3 blocks of k cascades overlap, a pair's transfer is divided by k
-//      (the larger count of its two cells), so overlapping cascades together
-//      move what one would.
-//   settle  each queued cascade runs the reference's sequential transfer
-//      loop on one thread and adds its transfers straight to the fixed-point
-//      heights (no height is read in this phase).  Every drop adds its own
-//      height change to its cell's fixed-point height and clears the cell's
-//      pending sum and count; finished drops retire.
+//      Cascades that move nothing end here.  The steep ones are queued in the
+//      CTA with the heights they read and the words of an arrivals bitmap
+//      (8 x 8 cells per word, loaded with the heights) that hold the claimed
+//      centres of the 5 x 5 block around theirs.
+//   settle  each queued cascade takes its overlap counts from those words:
+//      where the 3 x 3 blocks of k cascades overlap, a pair's transfer is
+//      divided by k (the larger count of its two cells), so overlapping
+//      cascades together move what one would.  It then runs the reference's
+//      sequential transfer loop on one thread and adds its transfers straight
+//      to the fixed-point heights (no height is read in this phase).  Every
+//      drop adds its own height change to its cell's fixed-point height and
+//      clears the cell's pending sum and count; finished drops retire.
 // Heights live in 32.32 fixed point for the whole cycle (the float map is
 // rewritten at its end), so every update is an integer addition.
 // Integer sums make every result independent of thread timing: the same
@@ -283,8 +283,10 @@ __device__ __forceinline__ float3 normal5(float hp, float hxp, float hxm, float 
   if (mm) add(make_float3(0.0f, hym - hp, -1.0f), make_float3(-1.0f, hxm - hp, 0.0f));
   if (pm) add(make_float3(1.0f, hxp - hp, 0.0f), make_float3(0.0f, hym - hp, -1.0f));
   if (mp) add(make_float3(-1.0f, hxm - hp, 0.0f), make_float3(0.0f, hyp - hp, 1.0f));
+  // length(n) > 0 (IEEE sqrt is +0 only at +0, so this is dd > 0, without
+  // the square root on the critical path)
   const float dd = n.x * n.x + n.y * n.y + n.z * n.z;
-  if (sqrtf(dd) > 0.0f) {
+  if (dd > 0.0f) {
     const float r = 1.0f / sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
     n = make_float3(n.x * r, n.y * r, n.z * r);
   }
@@ -335,6 +337,9 @@ __device__ __forceinline__ void overlap_counts(unsigned long long w00, unsigned 
 __device__ __forceinline__ void settle_cascade(const SteepCell& qc, const Terrain& T, CellQ* cq,
                                                const shy_params& P) {
   const long long c2 = qc.c2;
+  unsigned kv;
+  int kc;
+  overlap_counts(qc.aw[0], qc.aw[1], qc.aw[2], qc.aw[3], qc.tx0, qc.ty0, qc.ix, qc.iy, T, kv, kc);
   float v[8];
   int sk[8];
 #pragma unroll
@@ -353,8 +358,8 @@ __device__ __forceinline__ void settle_cascade(const SteepCell& qc, const Terrai
     // h > 0.1 in double is h >= 0.1f in float (no float lies between);
     // |diff| - 0 is |diff| exactly
     thr[j] = v[j] >= 0.1f ? dist * P.max_diff : 0.0f;
-    const int kn = (int)((qc.kv >> (4 * k)) & 15u);
-    kk[j] = qc.kc > kn ? qc.kc : kn;
+    const int kn = (int)((kv >> (4 * k)) & 15u);
+    kk[j] = kc > kn ? kc : kn;
   }
   const float h0 = qc.h0;
   float hcv = h0;
@@ -515,14 +520,15 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       ++n_steps;
       s.x = s.x + (P.gravity * n.x) / v.x;  // water.h:95
       s.y = s.y + (P.gravity * n.z) / v.x;
-      if (len2(r.x, r.y) > 0.0f && len2(s.x, s.y) > 0.0f) {  // water.h:97-99
+      // length(v) > 0 is dot(v, v) > 0: IEEE sqrt is +0 only at +0
+      if (dot2(r.x, r.y, r.x, r.y) > 0.0f && dot2(s.x, s.y, s.x, s.y) > 0.0f) {  // water.h:97-99
         const float rf = 1.0f / sqrtf(dot2(r.x, r.y, r.x, r.y));
         const float rs = 1.0f / sqrtf(dot2(s.x, s.y, s.x, s.y));
         const float k = (P.momentum_transfer * dot2(r.x * rf, r.y * rf, s.x * rs, s.y * rs)) / (v.x + r.z);
         s.x = s.x + k * r.x;
         s.y = s.y + k * r.y;
       }
-      if (len2(s.x, s.y) > 0.0f) {  // water.h:108-109
+      if (dot2(s.x, s.y, s.x, s.y) > 0.0f) {  // water.h:108-109
         const float root2 = sqrtf(2.0f);
         const float rs = 1.0f / sqrtf(dot2(s.x, s.y, s.x, s.y));
         const float ux = s.x * rs, uy = s.y * rs;
@@ -624,18 +630,22 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         any |= (sh[k] < __int_as_float(0x7f800000)) && diff != 0.0f && excess > 0.0f;
       }
       if (any) {
-        unsigned kv;
-        int kc;
-        overlap_counts(aw00, aw01, aw10, aw11, tx0, ty0, ix, iy, T, kv, kc);
-        // one claim per drop slot, so the queue (cap entries) cannot overflow
+        // one claim per drop slot, so the queue (cap entries) cannot overflow;
+        // the overlap counts are worked out in settle, off this phase's tail
         SteepCell& q = S.steep[atomicAdd(&s_nq, 1)];
         q.c2 = c2;
         q.ti = ti;
         q.h0 = h0;
 #pragma unroll
         for (int k = 0; k < 8; ++k) q.v[k] = sh[k];
-        q.kv = kv;
-        q.kc = kc;
+        q.aw[0] = aw00;
+        q.aw[1] = aw01;
+        q.aw[2] = aw10;
+        q.aw[3] = aw11;
+        q.tx0 = tx0;
+        q.ty0 = ty0;
+        q.ix = ix;
+        q.iy = iy;
       }
     }
     lap(2);
@@ -646,8 +656,10 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     // Every addition here is an integer atomic on a fixed-point height that
     // nobody reads in this phase, so the order does not matter.
     {
+      // queued cascades go to the highest threads first: those past the
+      // CTA's last drop slot have no drop of their own to settle
       const int nq = s_nq;
-      for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+      for (int i = (int)blockDim.x - 1 - (int)threadIdx.x; i < nq; i += blockDim.x) {
         const SteepCell qc = S.steep[i];
         settle_cascade(qc, TT[qc.ti], a.cq, P);
       }
