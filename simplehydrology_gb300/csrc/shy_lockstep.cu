@@ -307,14 +307,22 @@ __device__ __forceinline__ longlong2 hq_e(const CellQ* c) {
 __device__ __forceinline__ void overlap_counts(unsigned long long w00, unsigned long long w01,
                                                unsigned long long w10, unsigned long long w11, int tx0, int ty0,
                                                int ix, int iy, const Terrain& T, unsigned& kv, int& kc) {
+  // row by row: row dx of the block is byte (x % 8) of the word(s) of its
+  // tile column, the two tile rows side by side as 16 bits; cells outside
+  // the map never have their bit set, rows outside it are skipped
+  const bool two_rows = ((iy + 2 < T.ny ? iy + 2 : T.ny - 1) >> 3) != ty0;
+  const int o = iy - 2 - 8 * ty0;  // bit of the 16 for dy = -2 (-2 .. 7)
   unsigned cen = 0;
 #pragma unroll
-  for (int l = 0; l < 25; ++l) {
-    const int x = ix + l / 5 - 2, y = iy + l % 5 - 2;
-    const bool in = !oob(x, y, T.nx, T.ny);
-    const bool i = in && (x >> 3) != tx0, j = in && (y >> 3) != ty0;
-    const unsigned long long word = i ? (j ? w11 : w10) : (j ? w01 : w00);
-    cen |= (in && (word & arr_bit(x, y))) ? (1u << l) : 0u;
+  for (int r = 0; r < 5; ++r) {
+    const int x = ix + r - 2;
+    if (x < 0 || x >= T.nx) continue;
+    const bool second = (x >> 3) != tx0;
+    const int sh = (x & 7) * 8;
+    unsigned row = (unsigned)(((second ? w10 : w00) >> sh) & 0xFFull);
+    if (two_rows) row |= (unsigned)(((second ? w11 : w01) >> sh) & 0xFFull) << 8;
+    const unsigned bits = (o >= 0 ? row >> o : row << (-o)) & 31u;
+    cen |= bits << (5 * r);
   }
   // cascades whose 3 x 3 block holds cell (dx, dy): popcount of a window
   auto cover = [&](int dx, int dy) {
