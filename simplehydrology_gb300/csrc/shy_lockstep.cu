@@ -548,6 +548,10 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       const int jx = (int)p.x, jy = (int)p.y;
       const bool out = oob(jx, jy, T.nx, T.ny);
       const long long c2 = T.cell_base + (long long)jx * T.ny + jy;
+      // the tracks need nothing from the next cell: out before its loads
+      add_i64(&a.trk[c].td, shy_q32(v.x));  // water.h:115-117
+      add_i64(&a.trk[c].tmx, shy_q32(v.x * s.x));
+      add_i64(&a.trk[c].tmy, shy_q32(v.x * s.y));
       // the next cell's height and the drop's registration there travel
       // together; the first drop to arrive runs the cell's cascade
       int arrived_before = 1;
@@ -556,9 +560,6 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         qn = a.cq[c2].hq;
         arrived_before = atomicAdd(&a.cq[c2].cnt[par ^ 1], 1);
       }
-      add_i64(&a.trk[c].td, shy_q32(v.x));  // water.h:115-117
-      add_i64(&a.trk[c].tmx, shy_q32(v.x * s.x));
-      add_i64(&a.trk[c].tmy, shy_q32(v.x * s.y));
       const float h2 = out ? __double2float_rn((double)hp - 0.002) : shy_unq(qn);  // water.h:120-124
       float ceq = r.w * (hp - h2);  // water.h:127-128
       if (ceq < 0.0f) ceq = 0.0f;
