@@ -9,7 +9,7 @@ scatter, lrate blend and cascade.  One step = one erosion cycle
 dataset; the terrain recipe stands in for the reference's FastNoiseLite map.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload plain|batch|converge]
+                  [--workload plain|batch|converge|large]
 
 `value` is device throughput with the maps resident in HBM; between timed
 steps the L2 is flushed by writing a 256 MiB buffer (untimed).  `e2e` is the
@@ -26,6 +26,9 @@ end-of-cycle pass over the whole step time.
 
 `--workload converge` measures the plain method's time to converged
 discharge (within 5 % log-L2 of the discharge after 4 x 500 cycles).
+
+`--workload large` runs the large-scale configuration: 8192^2, 4,194,304
+drops per cycle, per-cell vegetation every cycle.
 
 `--workload batch` runs the batched-terrain configuration instead: 64
 terrains, sides log-uniform in [128, 1024], 0.25 drops per cell per cycle,
@@ -214,6 +217,27 @@ class PlainWorkload:
             self.w.get_field(f, out=bufs[f])
 
 
+class LargeWorkload(PlainWorkload):
+    """The large-scale configuration: an 8192^2 terrain, 4,194,304 drops per
+    cycle, per-cell vegetation (spawn probability 1e-4 per cell per cycle)
+    coupled to erosion through the root density.  One step = one erosion
+    cycle followed by one vegetation step."""
+
+    def __init__(self, shy, n, drops):
+        super().__init__(shy, n, drops)
+        self.config = {"workload": f"large scale: {n}x{n} value-noise terrain, {drops} drops/cycle, "
+                                   "per-cell vegetation each cycle", "map": [n, n], "drops_per_cycle": drops}
+
+    def erode(self):
+        self.w.erode(self.drops)
+        self.w.vegetation_step(1)
+
+    def reset(self):
+        super().reset()
+        self.w.set_field("root_density", self.zero)
+        self.w.set_field("plant_size", self.zero)
+
+
 class BatchWorkload:
     """This rank's share of the batched-terrain configuration: 64 terrains
     with sides log-uniform in [128, 1024], 0.25 drops per cell per cycle, all
@@ -284,6 +308,9 @@ def run_ours(args):
 
     if args.workload == "batch":
         wl = BatchWorkload(shy, rank, world_size, args.terrains)
+    elif args.workload == "large":
+        wl = LargeWorkload(shy, 8192 if args.map == NX else args.map,
+                           4194304 if args.drops == DROPS else args.drops)
     else:
         wl = PlainWorkload(shy, args.map, args.drops)
     w = wl.w
@@ -390,7 +417,7 @@ def run_ours(args):
         "drop_steps": steps_total, "wall_s": wall,
     }
     out["clocks"] = clk.summary()
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
     if dist:
         dist.barrier()
@@ -527,7 +554,7 @@ def main():
     ap.add_argument("--drops", type=int, default=DROPS)
     ap.add_argument("--no-e2e", action="store_true")
     # the batched-terrain configuration (not the default bench line)
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "converge"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "converge", "large"])
     ap.add_argument("--ref-cycles", type=int, default=2000)
     ap.add_argument("--check-every", type=int, default=10)
     ap.add_argument("--terrains", type=int, default=64)

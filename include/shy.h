@@ -156,6 +156,11 @@ int shy_world_timing(shy_world* w, shy_timing* out);
  * height updates, retirements), barrier wait plus spawn and exit};
  * *iterations = lock-step steps run. */
 int shy_world_lockstep_profile(shy_world* w, double* phase_ms, uint64_t* iterations);
+/* Launch shape of the batched kernel: at most `grid` CTAs (0, the default:
+ * every CTA that fits on the GPU at once, at least 32 drops each).  A CTA
+ * keeps its drops in shared memory while they fit and in global memory
+ * beyond that.  Results do not depend on the launch shape. */
+int shy_world_set_launch(shy_world* w, int grid);
 
 /* Source of erf(0.4 * discharge) (source/cellpool.h:242-244) for the exact
  * mode.  SHY_ERF_DEVICE (default) is the library's own erf, evaluated on the

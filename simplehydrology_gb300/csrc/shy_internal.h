@@ -166,12 +166,7 @@ struct shy_world {
   int erf_source = shy::ERF_DEVICE;
   int ceq_source = -1;        // erf source of the current ceqfac values (-1 stale)
   int track_mode = 0;         // 0: track_f holds the last call's tracks
-  int batch_grid = 0;         // CTAs of the lock-step kernel
-  int batch_block = 256;      // threads per CTA
-  int cycles_per_graph = 8;
-  cudaGraphExec_t graph = nullptr;
-  int graph_cycles = 0;
-  int graph_grid = 0;
+  int batch_grid = 0;         // CTAs of the lock-step kernel at most (0: all resident)
 
   shy::Timing timing;
   float* normals = nullptr;   // 3 x cells, lazily allocated

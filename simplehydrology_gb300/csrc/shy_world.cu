@@ -96,7 +96,6 @@ void free_world(shy_world* w) {
                   w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed, w->crand, w->plants};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  if (w->graph) cudaGraphExecDestroy(w->graph);
   for (auto& p : w->timing.pending) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);
@@ -536,6 +535,17 @@ int shy_world_set_field(shy_world* w, int field, const float* host, size_t count
 
 int shy_world_get_field(shy_world* w, int field, float* host, size_t count) {
   return shy_terrain_get_field(w, 0, field, host, count);
+}
+
+int shy_world_set_launch(shy_world* w, int grid) {
+  int rc = check_world(w);
+  if (rc) return rc;
+  if (grid < 0) {
+    set_error("shy_world_set_launch: grid must be >= 0");
+    return SHY_ERR_INVALID_ARG;
+  }
+  w->batch_grid = grid;
+  return SHY_OK;
 }
 
 int shy_world_sync(shy_world* w) {

@@ -154,3 +154,26 @@ def test_consecutive_calls_carry_fixed_point_state(shy, po):
     po.erode_batched(m, 8, 3, 1500, 1, hq=hq)
     compare_all(w.get_field, m, po, "after upload")
     w.close()
+
+
+@pytest.mark.parametrize("grid", [1, 7])
+def test_launch_shape_does_not_change_results(shy, po, grid):
+    """Few CTAs put the drop slots in global memory (4096 drops on one CTA
+    need 640 KiB); the results equal the default launch's and the oracle's."""
+    nx, ny, drops = 128, 96, 4096
+    H = po.value_noise(nx, ny, 13)
+    outs = []
+    for g in (0, grid):
+        w = shy.World(nx, ny, seed=6)
+        w.set_launch(g)
+        w.set_field("height", H)
+        w.erode(drops, 2)
+        outs.append([w.get_field(f) for f in po.FIELDS])
+        steps = w.stats().drop_steps
+        w.close()
+    m = po.Maps(nx, ny, height=H)
+    acc = po.erode_batched(m, 6, 0, drops, 2)
+    assert steps == acc.steps
+    for k, f in enumerate(po.FIELDS):
+        assert np.array_equal(bits(outs[0][k]), bits(outs[1][k])), f
+        assert np.array_equal(bits(outs[1][k]), bits(m.f[k])), f
