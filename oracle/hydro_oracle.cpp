@@ -20,6 +20,12 @@
 //     32.32 fixed point).  That schedule has no reference counterpart; its
 //     physics is the reference's, cited per line, and its oracle is this code.
 //
+//  3. The rest of the reference's frame: its plant agents (Vegetation::grow)
+//     on the C-library rand() stream that World::erode's spawns share, the
+//     front end's per-frame buffers, and the per-cell vegetation of the
+//     batched mode.  The first two are pinned against the reference build
+//     (tests/golden/ref_frames.json, ref_feed.json).
+//
 // Built with -ffp-contract=off so that no multiply-add is fused (the
 // reference's x86 build has no FMA either).
 #include <algorithm>
