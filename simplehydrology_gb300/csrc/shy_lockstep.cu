@@ -483,12 +483,25 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
 
     // ---- descend: one Drop::descend step per live drop ----
     if (threadIdx.x == 0) s_nq = 0;  // everyone read it before the last barrier
+    // Each iteration loads the next slot's state before working on its own,
+    // so that with several slots per thread (slots in global memory) their
+    // loads overlap the work instead of preceding it.
+    int ag_n = 0, ti_n = 0;
+    float2 p_n = make_float2(0.0f, 0.0f), s_n = p_n, v_n = p_n;
+    long long gn_n = 0;
+    if ((int)threadIdx.x < nd) {
+      const int j = threadIdx.x;
+      ag_n = S.age[j]; ti_n = S.terr[j]; p_n = S.pos[j]; s_n = S.spd[j]; v_n = S.vs[j]; gn_n = S.gain[j];
+    }
     for (int j = threadIdx.x; j < nd; j += blockDim.x) {
-      const int ag = S.age[j];
+      const int ag = ag_n, ti = ti_n;
+      float2 p = p_n, s = s_n, v = v_n;
+      long long gn = gn_n;
+      if (j + (int)blockDim.x < nd) {
+        const int jn = j + blockDim.x;
+        ag_n = S.age[jn]; ti_n = S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; v_n = S.vs[jn]; gn_n = S.gain[jn];
+      }
       if (ag < 0) continue;
-      const int ti = S.terr[j];
-      float2 p = S.pos[j], s = S.spd[j], v = S.vs[j];
-      long long gn = S.gain[j];
       const Terrain T = TT[ti];
       const CellQ* RT = a.cq + T.cell_base;
       const int ix = (int)p.x, iy = (int)p.y;
@@ -600,10 +613,20 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     // centre instead and is masked out.  The centre only changes through a
     // transfer, so without any excess to begin with the sequential loop moves
     // nothing and the cascade ends here.
+    long long c2_n = -1;
+    int ti_n2 = 0;
+    if ((int)threadIdx.x < nd) {
+      c2_n = S.ctr[threadIdx.x];
+      ti_n2 = S.terr[threadIdx.x];
+    }
     for (int j = threadIdx.x; j < nd; j += blockDim.x) {
-      const long long c2 = S.ctr[j];
+      const long long c2 = c2_n;
+      const int ti = ti_n2;
+      if (j + (int)blockDim.x < nd) {  // the next slot's claim, loaded ahead
+        c2_n = S.ctr[j + blockDim.x];
+        ti_n2 = S.terr[j + blockDim.x];
+      }
       if (c2 < 0) continue;
-      const int ti = S.terr[j];
       const Terrain T = TT[ti];
       const int lc = (int)(c2 - T.cell_base);  // < 2^31 cells per terrain
       const int ix = lc / T.ny, iy = lc - ix * T.ny;
@@ -674,19 +697,27 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       }
     }
     unsigned long long retired = 0;
+    int ag_f = -1, ti_f = 0;
+    long long c_f = -1, c2_f = -1, own_f = 0;
+    if ((int)threadIdx.x < nd) {
+      const int j = threadIdx.x;
+      ag_f = S.age[j]; ti_f = S.terr[j]; c_f = S.cell[j]; c2_f = S.ctr[j]; own_f = S.own[j];
+    }
     for (int j = threadIdx.x; j < nd; j += blockDim.x) {
-      const int ag = S.age[j];
+      const int ag = ag_f, ti = ti_f;
+      const long long c = c_f, c2 = c2_f, own = own_f;
+      if (j + (int)blockDim.x < nd) {  // the next slot, loaded ahead
+        const int jn = j + blockDim.x;
+        ag_f = S.age[jn]; ti_f = S.terr[jn]; c_f = S.cell[jn]; c2_f = S.ctr[jn]; own_f = S.own[jn];
+      }
       if (ag == -1) continue;
-      const long long c = S.cell[j];
-      const long long c2 = S.ctr[j];
       if (c2 >= 0) {  // the claim of this step ends
-        const Terrain T = TT[S.terr[j]];
+        const Terrain T = TT[ti];
         const int lc = (int)(c2 - T.cell_base);
         const int x = lc / T.ny, y = lc - x * T.ny;
         atomicAnd(&a.arr[arr_word(T, x, y)], ~arr_bit(x, y));
       }
       if (c >= 0) {
-        const long long own = S.own[j];
         if (own != 0) add_i64(&a.cq[c].hq, own);
         a.cq[c].e = 0;
         a.cq[c].cnt[par] = 0;
