@@ -209,12 +209,10 @@ class PlainWorkload:
         return bufs
 
     def upload(self, bufs):
-        for f in FIELDS:
-            self.w.set_field(f, bufs[f])
+        self.w.set_state(0, **bufs)
 
     def download(self, bufs):
-        for f in FIELDS:
-            self.w.get_field(f, out=bufs[f])
+        self.w.get_state(0, out=bufs)
 
 
 class LargeWorkload(PlainWorkload):
@@ -283,13 +281,11 @@ class BatchWorkload:
 
     def upload(self, bufs):
         for i, d in enumerate(bufs):
-            for f in FIELDS:
-                self.w.set_field(i, f, d[f])
+            self.w.set_state(i, **d)
 
     def download(self, bufs):
         for i, d in enumerate(bufs):
-            for f in FIELDS:
-                self.w.get_field(i, f, out=d[f])
+            self.w.get_state(i, out=d)
 
 
 FIELDS = ("height", "discharge", "momentum_x", "momentum_y")

@@ -141,6 +141,14 @@ int shy_world_size(shy_world* w, int* nx, int* ny);
 int shy_world_set_field(shy_world* w, int field, const float* host, size_t count);
 int shy_world_get_field(shy_world* w, int field, float* host, size_t count);
 int shy_world_sync(shy_world* w);
+/* Height, discharge and momentum of terrain t -- the state a front end
+ * exchanges every frame -- in one call each way, with one host
+ * synchronisation (count = nx * ny each; a NULL pointer leaves that field
+ * unchanged / unread).  Same effect as the matching set/get_field calls. */
+int shy_terrain_set_state(shy_world* w, int terrain, const float* height, const float* discharge,
+                          const float* momentum_x, const float* momentum_y, size_t count);
+int shy_terrain_get_state(shy_world* w, int terrain, float* height, float* discharge, float* momentum_x,
+                          float* momentum_y, size_t count);
 /* The world's cudaStream_t, for callers that order their own work with it. */
 int shy_world_stream(shy_world* w, void** stream);
 int shy_world_stats(shy_world* w, shy_stats* out);

@@ -106,6 +106,46 @@ class _Handle:
         check(lib().shy_world_stream(self._w, C.byref(s)))
         return s.value or 0
 
+    # ---- the state a front end exchanges every frame, in one call each way ----
+    _STATE = ("height", "discharge", "momentum_x", "momentum_y")
+
+    def _state_args(self, terrain, arrays, writable):
+        nx, ny = self._terrain_shape(terrain)
+        ptrs = []
+        for name in self._STATE:
+            a = arrays.get(name)
+            if a is None:
+                ptrs.append(None)
+                continue
+            if writable:
+                if a.dtype != np.float32 or a.shape != (nx, ny) or not a.flags.c_contiguous:
+                    raise ValueError(f"{name}: want a contiguous float32 array of shape {(nx, ny)}")
+            else:
+                a = np.ascontiguousarray(a, np.float32).reshape(nx, ny)
+                arrays[name] = a
+            ptrs.append(_fptr(a))
+        return ptrs, nx * ny
+
+    def set_state(self, terrain: int = 0, **fields):
+        """height / discharge / momentum_x / momentum_y of one terrain in one
+        call (shy_terrain_set_state); fields not given are left unchanged."""
+        unknown = set(fields) - set(self._STATE)
+        if unknown:
+            raise ValueError(f"unknown fields {sorted(unknown)}")
+        arrays = dict(fields)
+        ptrs, n = self._state_args(terrain, arrays, False)
+        check(lib().shy_terrain_set_state(self._w, terrain, *ptrs, n))
+
+    def get_state(self, terrain: int = 0, out=None):
+        """The four state fields of one terrain (shy_terrain_get_state), into
+        `out` (a dict of float32 arrays) when given."""
+        nx, ny = self._terrain_shape(terrain)
+        if out is None:
+            out = {name: np.empty((nx, ny), np.float32) for name in self._STATE}
+        ptrs, n = self._state_args(terrain, out, True)
+        check(lib().shy_terrain_get_state(self._w, terrain, *ptrs, n))
+        return out
+
     def save(self, path):
         """Write the world's state to a checkpoint file (shy_world_save)."""
         check(lib().shy_world_save(self._w, str(path).encode()))

@@ -104,6 +104,8 @@ SIGNATURES = {
     "shy_world_set_field": (C.c_int, [W, C.c_int, FP, C.c_size_t]),
     "shy_world_get_field": (C.c_int, [W, C.c_int, FP, C.c_size_t]),
     "shy_world_sync": (C.c_int, [W]),
+    "shy_terrain_set_state": (C.c_int, [W, C.c_int, FP, FP, FP, FP, C.c_size_t]),
+    "shy_terrain_get_state": (C.c_int, [W, C.c_int, FP, FP, FP, FP, C.c_size_t]),
     "shy_world_stream": (C.c_int, [W, P(C.c_void_p)]),
     "shy_world_stats": (C.c_int, [W, P(Stats)]),
     "shy_world_reset_stats": (C.c_int, [W]),

@@ -240,4 +240,52 @@ cudaError_t launch_scatter_comp(shy_world* w, int t, int comp, const float* in) 
   return cudaGetLastError();
 }
 
+namespace {
+
+// discharge and momentum into the per-cell records in one pass (null: keep),
+// with 1 + entrainment * erf(0.4 d) when the discharge changes
+// (source/water.h:127, source/cellpool.h:242-244)
+__global__ void pack_state_kernel(float4* __restrict__ rec, const float* __restrict__ d,
+                                  const float* __restrict__ mx, const float* __restrict__ my, long long n,
+                                  shy_params P) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float4 r = rec[i];
+    if (mx) r.x = mx[i];
+    if (my) r.y = my[i];
+    if (d) {
+      r.z = d[i];
+      r.w = 1.0f + P.entrainment * shy_erff(0.4f * r.z);
+    }
+    rec[i] = r;
+  }
+}
+
+__global__ void unpack_state_kernel(const float4* __restrict__ rec, float* __restrict__ d, float* __restrict__ mx,
+                                    float* __restrict__ my, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float4 r = rec[i];
+    if (mx) mx[i] = r.x;
+    if (my) my[i] = r.y;
+    if (d) d[i] = r.z;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_pack_state(shy_world* w, int t, const float* d, const float* mx, const float* my) {
+  const Terrain& T = w->terrains[t];
+  const long long n = (long long)T.nx * T.ny;
+  pack_state_kernel<<<blocks_for(n), kBlock, 0, w->stream>>>(w->rec + T.cell_base, d, mx, my, n, w->P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_state(shy_world* w, int t, float* d, float* mx, float* my) {
+  const Terrain& T = w->terrains[t];
+  const long long n = (long long)T.nx * T.ny;
+  unpack_state_kernel<<<blocks_for(n), kBlock, 0, w->stream>>>(w->rec + T.cell_base, d, mx, my, n);
+  return cudaGetLastError();
+}
+
 }  // namespace shy

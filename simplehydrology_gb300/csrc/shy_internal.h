@@ -144,6 +144,7 @@ struct shy_world {
   long long* dctr = nullptr;  // cascade centre this slot runs this step, -1 if none
   shy::SteepCell* dsteep = nullptr;  // steep-cascade queue (one entry per drop slot at most)
   unsigned long long* arr = nullptr;  // arrivals bitmap, all terrains
+  float* stage = nullptr;             // cells floats, third staging buffer of the state calls
   float* feed = nullptr;              // staging buffer of shy_feed for host output
   size_t feed_len = 0;
   // the reference's frame loop: C-library random stream and plant agents
@@ -225,6 +226,10 @@ cudaError_t launch_value_noise(shy_world* w, int terrain, unsigned long long see
                                double* raw, unsigned long long* minmax);
 cudaError_t launch_gather_comp(shy_world* w, int terrain, int comp, float* out);
 cudaError_t launch_scatter_comp(shy_world* w, int terrain, int comp, const float* in);
+// discharge / momentum (device arrays, null: keep) into terrain t's records,
+// erf records included; and back out
+cudaError_t launch_pack_state(shy_world* w, int t, const float* d, const float* mx, const float* my);
+cudaError_t launch_unpack_state(shy_world* w, int t, float* d, float* mx, float* my);
 // timing: open a launch interval of `kind` (returns the pair index or -1)
 cudaError_t timing_begin(shy_world* w, int kind, int* slot);
 cudaError_t timing_end(shy_world* w, int slot);

@@ -93,7 +93,7 @@ void free_world(shy_world* w) {
   void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
                   w->dterr, w->dcell, w->dctr, w->dterrains, w->stats, w->bar, w->ddrop,
                   w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down,
-                  w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed, w->crand, w->plants};
+                  w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed, w->crand, w->plants, w->stage};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& p : w->timing.pending) {
@@ -526,6 +526,64 @@ int shy_terrain_get_field(shy_world* w, int t, int field, float* host, size_t co
   }
   SHY_CHECK_CUDA(cudaMemcpyAsync(host, src, sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream), "download field");
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
+  return SHY_OK;
+}
+
+// The state a front end exchanges every frame, in one call each way: three
+// staging buffers (scratch, the relax buffer, stage) hold the record
+// components on the device.
+int shy_terrain_set_state(shy_world* w, int t, const float* height, const float* discharge,
+                          const float* momentum_x, const float* momentum_y, size_t count) {
+  int rc = check_terrain(w, t);
+  if (rc) return rc;
+  const long long n = (long long)w->terrains[t].nx * w->terrains[t].ny;
+  if (count != (size_t)n) {
+    set_error("set_state: count %zu, want %lld", count, n);
+    return SHY_ERR_INVALID_ARG;
+  }
+  if (momentum_y && !w->stage) SHY_CHECK_CUDA(dalloc(&w->stage, (size_t)w->cells), "allocate staging");
+  const size_t bytes = sizeof(float) * (size_t)n;
+  cudaStream_t s = w->stream;
+  if (height) {
+    SHY_CHECK_CUDA(cudaMemcpyAsync(w->h + w->terrains[t].cell_base, height, bytes, cudaMemcpyHostToDevice, s),
+                   "upload heights");
+    w->hq_stale = true;
+  }
+  if (discharge) SHY_CHECK_CUDA(cudaMemcpyAsync(w->scratch, discharge, bytes, cudaMemcpyHostToDevice, s), "upload");
+  if (momentum_x) SHY_CHECK_CUDA(cudaMemcpyAsync(w->relax, momentum_x, bytes, cudaMemcpyHostToDevice, s), "upload");
+  if (momentum_y) SHY_CHECK_CUDA(cudaMemcpyAsync(w->stage, momentum_y, bytes, cudaMemcpyHostToDevice, s), "upload");
+  if (discharge || momentum_x || momentum_y)
+    SHY_CHECK_CUDA(launch_pack_state(w, t, discharge ? w->scratch : nullptr, momentum_x ? w->relax : nullptr,
+                                     momentum_y ? w->stage : nullptr),
+                   "pack state");
+  if (discharge) w->ceq_source = ERF_DEVICE;
+  SHY_CHECK_CUDA(cudaStreamSynchronize(s), "synchronize");
+  return SHY_OK;
+}
+
+int shy_terrain_get_state(shy_world* w, int t, float* height, float* discharge, float* momentum_x,
+                          float* momentum_y, size_t count) {
+  int rc = check_terrain(w, t);
+  if (rc) return rc;
+  const long long n = (long long)w->terrains[t].nx * w->terrains[t].ny;
+  if (count != (size_t)n) {
+    set_error("get_state: count %zu, want %lld", count, n);
+    return SHY_ERR_INVALID_ARG;
+  }
+  if (momentum_y && !w->stage) SHY_CHECK_CUDA(dalloc(&w->stage, (size_t)w->cells), "allocate staging");
+  const size_t bytes = sizeof(float) * (size_t)n;
+  cudaStream_t s = w->stream;
+  if (discharge || momentum_x || momentum_y)
+    SHY_CHECK_CUDA(launch_unpack_state(w, t, discharge ? w->scratch : nullptr, momentum_x ? w->relax : nullptr,
+                                       momentum_y ? w->stage : nullptr),
+                   "unpack state");
+  if (height)
+    SHY_CHECK_CUDA(cudaMemcpyAsync(height, w->h + w->terrains[t].cell_base, bytes, cudaMemcpyDeviceToHost, s),
+                   "download heights");
+  if (discharge) SHY_CHECK_CUDA(cudaMemcpyAsync(discharge, w->scratch, bytes, cudaMemcpyDeviceToHost, s), "download");
+  if (momentum_x) SHY_CHECK_CUDA(cudaMemcpyAsync(momentum_x, w->relax, bytes, cudaMemcpyDeviceToHost, s), "download");
+  if (momentum_y) SHY_CHECK_CUDA(cudaMemcpyAsync(momentum_y, w->stage, bytes, cudaMemcpyDeviceToHost, s), "download");
+  SHY_CHECK_CUDA(cudaStreamSynchronize(s), "synchronize");
   return SHY_OK;
 }
 

@@ -177,3 +177,31 @@ def test_launch_shape_does_not_change_results(shy, po, grid):
     for k, f in enumerate(po.FIELDS):
         assert np.array_equal(bits(outs[0][k]), bits(outs[1][k])), f
         assert np.array_equal(bits(outs[1][k]), bits(m.f[k])), f
+
+
+def test_state_calls_equal_field_calls(shy, po):
+    """shy_terrain_set_state / get_state: the same bits as four set_field /
+    get_field calls, and the same erosion afterwards."""
+    nx, ny = 70, 90
+    rng = np.random.default_rng(3)
+    st = {"height": po.value_noise(nx, ny, 5), "discharge": rng.gamma(0.5, 2.0, (nx, ny)).astype(np.float32),
+          "momentum_x": rng.normal(0, 1, (nx, ny)).astype(np.float32),
+          "momentum_y": rng.normal(0, 1, (nx, ny)).astype(np.float32)}
+    a, b = shy.World(nx, ny, seed=4), shy.World(nx, ny, seed=4)
+    for f, v in st.items():
+        a.set_field(f, v)
+    b.set_state(0, **st)
+    got = b.get_state(0)
+    for f in st:
+        assert np.array_equal(bits(got[f]), bits(a.get_field(f))), f
+    a.erode(1500, 2)
+    b.erode(1500, 2)
+    got = b.get_state(0)
+    for f in st:
+        assert np.array_equal(bits(got[f]), bits(a.get_field(f))), f
+    # partial update leaves the other fields alone
+    b.set_state(0, momentum_x=np.zeros((nx, ny), np.float32))
+    assert np.array_equal(bits(b.get_field("discharge")), bits(got["discharge"]))
+    assert not b.get_field("momentum_x").any()
+    a.close()
+    b.close()
