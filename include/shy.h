@@ -167,8 +167,11 @@ int shy_world_lockstep_profile(shy_world* w, double* phase_ms, uint64_t* iterati
 /* Launch shape of the batched kernel: at most `grid` CTAs (0, the default:
  * every CTA that fits on the GPU at once, at least 32 drops each).  A CTA
  * keeps its drops in shared memory while they fit and in global memory
- * beyond that.  Results do not depend on the launch shape. */
-int shy_world_set_launch(shy_world* w, int grid);
+ * beyond that.  `order` puts the drops of a cycle into slots sorted by spawn
+ * cell, so that each CTA works on a compact stretch of the maps: -1 (the
+ * default) when the cell state is larger than L2, 0 never, 1 always.
+ * Results do not depend on either setting. */
+int shy_world_set_launch(shy_world* w, int grid, int order);
 
 /* Source of erf(0.4 * discharge) (source/cellpool.h:242-244) for the exact
  * mode.  SHY_ERF_DEVICE (default) is the library's own erf, evaluated on the

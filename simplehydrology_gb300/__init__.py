@@ -91,9 +91,10 @@ class _Handle:
         """Vegetation::grow(), per cell (source/vegetation.h:122-188)."""
         check(lib().shy_vegetation_step(self._w, steps))
 
-    def set_launch(self, grid: int = 0):
-        """At most `grid` CTAs for the batched kernel (0: all resident)."""
-        check(lib().shy_world_set_launch(self._w, grid))
+    def set_launch(self, grid: int = 0, order: int = -1):
+        """At most `grid` CTAs for the batched kernel (0: all resident); slots
+        in spawn-cell order (-1: when the state outgrows L2, 0 never, 1 always)."""
+        check(lib().shy_world_set_launch(self._w, grid, order))
 
     def set_cycle(self, cycle: int):
         check(lib().shy_world_set_cycle(self._w, cycle))

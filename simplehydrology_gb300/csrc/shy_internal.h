@@ -110,6 +110,7 @@ struct shy_world {
   long long cells = 0;                 // all terrains
   int max_drops = 0;                   // drop slots allocated
   int sm_count = 0;
+  long long l2_bytes = 0;
 
   // reference-visible per-cell fields
   float* h = nullptr;         // height (in batched mode: hq rounded to float)
@@ -144,6 +145,10 @@ struct shy_world {
   long long* dctr = nullptr;  // cascade centre this slot runs this step, -1 if none
   shy::SteepCell* dsteep = nullptr;  // steep-cascade queue (one entry per drop slot at most)
   unsigned long long* arr = nullptr;  // arrivals bitmap, all terrains
+  int* dorder = nullptr;      // drop run by each slot in a batched cycle (spawn-cell order)
+  int* dkey = nullptr;        // spawn-order scratch: run of each drop's spawn cell
+  int* drank = nullptr;       //   and its place within the run
+  int* dhist = nullptr;       //   runs' counts, then offsets (at most 65,536)
   float* stage = nullptr;             // cells floats, third staging buffer of the state calls
   float* feed = nullptr;              // staging buffer of shy_feed for host output
   size_t feed_len = 0;
@@ -168,6 +173,7 @@ struct shy_world {
   int ceq_source = -1;        // erf source of the current ceqfac values (-1 stale)
   int track_mode = 0;         // 0: track_f holds the last call's tracks
   int batch_grid = 0;         // CTAs of the lock-step kernel at most (0: all resident)
+  int batch_order = -1;       // slots in spawn-cell order: -1 when the cell state outgrows L2, 0 never, 1 always
 
   shy::Timing timing;
   float* normals = nullptr;   // 3 x cells, lazily allocated

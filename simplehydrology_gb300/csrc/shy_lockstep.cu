@@ -177,6 +177,7 @@ struct LockArgs {
   long long* ctr;
   SteepCell* steep;
   unsigned long long* arr;  // arrivals bitmap
+  const int* order;  // drop run by each slot (slots ordered by spawn cell), or null: slot = drop
   int smem_slots;   // 1: drop slots and queue live in dynamic shared memory
   shy_params P;
   DevStats* st;
@@ -445,7 +446,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   // spawn (source/world.h:64-74)
   unsigned long long born = 0;
   for (int j = threadIdx.x; j < nd; j += blockDim.x) {
-    const long long d = lo + j;
+    const long long d = a.order ? a.order[lo + j] : lo + j;
     const int t = find_terrain(TT, a.n_terrains, (int)d);
     const Terrain T = TT[t];
     int x, y;
@@ -856,6 +857,79 @@ int cells_grid(long long cells) {
 
 }  // namespace
 
+namespace {
+
+// Slot order of a cycle: drops sorted by their spawn cell, in runs of
+// 2^shift consecutive cells (x-major), so that each CTA's drops start in one
+// compact stretch of the maps.  Which slot runs which drop does not change
+// any result (every sum is an integer sum, and a cascade is the same
+// whichever drop claims it); the order within a run is whatever the atomics
+// give.
+__global__ void order_count_kernel(const Terrain* __restrict__ terrains, int n_terrains, int total,
+                                   const GridBar* __restrict__ bar, int shift, int* __restrict__ hist,
+                                   int* __restrict__ key, int* __restrict__ rank) {
+  const unsigned long long cycle = bar->cycle;
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < total; d += gridDim.x * blockDim.x) {
+    const Terrain T = terrains[find_terrain(terrains, n_terrains, d)];
+    int x, y;
+    shy_spawn_xy(T.seed, cycle, (unsigned)(d - T.drop_base), T.nx, T.ny, &x, &y);
+    const int b = (int)((T.cell_base + (long long)x * T.ny + y) >> shift);
+    key[d] = b;
+    rank[d] = atomicAdd(&hist[b], 1);
+  }
+}
+
+// exclusive prefix sum of hist[0 .. n) in place, one CTA of 1024 threads
+__global__ void order_scan_kernel(int* __restrict__ hist, int n) {
+  __shared__ int part[1024];
+  const int per = (n + 1023) / 1024, b0 = threadIdx.x * per;
+  int s = 0;
+  for (int i = 0; i < per && b0 + i < n; ++i) s += hist[b0 + i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {  // inclusive scan of the parts
+    const int v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+  for (int i = 0; i < per && b0 + i < n; ++i) {
+    const int h = hist[b0 + i];
+    hist[b0 + i] = run;
+    run += h;
+  }
+}
+
+__global__ void order_scatter_kernel(int total, const int* __restrict__ hist, const int* __restrict__ key,
+                                     const int* __restrict__ rank, int* __restrict__ order) {
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < total; d += gridDim.x * blockDim.x)
+    order[hist[key[d]] + rank[d]] = d;
+}
+
+}  // namespace
+
+// the bucket shift that keeps the spawn-order histogram at most 65,536 runs
+int order_shift(long long cells) {
+  int shift = 0;
+  while ((cells >> shift) > 65535) ++shift;
+  return shift;
+}
+
+cudaError_t launch_spawn_order(shy_world* w, int total) {
+  const int shift = order_shift(w->cells);
+  const int nb = (int)((w->cells - 1) >> shift) + 1;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(w->dhist, 0, sizeof(int) * (size_t)nb, w->stream)) != cudaSuccess) return e;
+  const int grid = (int)(((long long)total + 255) / 256 < 4096 ? ((long long)total + 255) / 256 : 4096);
+  order_count_kernel<<<grid < 1 ? 1 : grid, 256, 0, w->stream>>>(w->dterrains, (int)w->terrains.size(), total,
+                                                                  w->bar, shift, w->dhist, w->dkey, w->drank);
+  order_scan_kernel<<<1, 1024, 0, w->stream>>>(w->dhist, nb);
+  order_scatter_kernel<<<grid < 1 ? 1 : grid, 256, 0, w->stream>>>(total, w->dhist, w->dkey, w->drank,
+                                                                    w->dorder);
+  return cudaGetLastError();
+}
+
 int batched_max_grid(shy_world* w, int block) {
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lockstep_kernel, block, 0) != cudaSuccess)
@@ -934,6 +1008,13 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.ctr = w->dctr;
   a.steep = w->dsteep;
   a.arr = w->arr;
+  // Slots ordered by spawn cell when the cell state outgrows L2: each CTA's
+  // drops then touch a compact stretch of the maps (+49 % at 8192^2).  While
+  // the state fits in L2 locality buys nothing and compact CTAs at the map's
+  // edges finish early, so the slots keep the drop order.
+  const long long state_bytes = w->cells * (long long)(sizeof(CellQ) + sizeof(Tracks) + sizeof(float4) + 4);
+  const bool ordered = w->batch_order < 0 ? state_bytes > w->l2_bytes : w->batch_order != 0;
+  a.order = ordered ? w->dorder : nullptr;
   a.smem_slots = 0;
   a.P = w->P;
   a.st = w->stats;
@@ -941,8 +1022,13 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.max_steps = (int)w->P.max_age + 3;
 
   int slot = -1;
-  cudaError_t e = timing_begin(w, SHY_KERNEL_DROPS, &slot);
-  if (e != cudaSuccess) return e;
+  cudaError_t e;
+  if (a.order && a.total_drops > 0) {
+    if ((e = timing_begin(w, SHY_KERNEL_OTHER, &slot)) != cudaSuccess) return e;
+    if ((e = launch_spawn_order(w, a.total_drops)) != cudaSuccess) return e;
+    if ((e = timing_end(w, slot)) != cudaSuccess) return e;
+  }
+  if ((e = timing_begin(w, SHY_KERNEL_DROPS, &slot)) != cudaSuccess) return e;
   if ((e = launch_lockstep(a, w->sm_count, w->batch_grid, w->stream)) != cudaSuccess) return e;
   if ((e = timing_end(w, slot)) != cudaSuccess) return e;
 
@@ -992,6 +1078,7 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.ctr = b.ctr;
   a.steep = b.steep;
   a.arr = b.arr;
+  a.order = nullptr;
   a.smem_slots = 0;
   a.P = b.P;
   a.st = b.st;

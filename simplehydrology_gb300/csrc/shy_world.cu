@@ -93,7 +93,7 @@ void free_world(shy_world* w) {
   void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
                   w->dterr, w->dcell, w->dctr, w->dterrains, w->stats, w->bar, w->ddrop,
                   w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down,
-                  w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed, w->crand, w->plants, w->stage};
+                  w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed, w->crand, w->plants, w->stage, w->dorder, w->dkey, w->drank, w->dhist};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& p : w->timing.pending) {
@@ -108,7 +108,7 @@ void free_world(shy_world* w) {
 int alloc_drop_slots(shy_world* w, int n) {
   if (n <= w->max_drops) return SHY_OK;
   void* ptrs[] = {w->dpos, w->dspd, w->dvs, w->dage, w->dgain, w->dterr, w->dcell, w->dctr, w->down,
-                  w->dsteep};
+                  w->dsteep, w->dorder, w->dkey, w->drank};
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -116,6 +116,7 @@ int alloc_drop_slots(shy_world* w, int n) {
   w->dage = w->dterr = nullptr;
   w->dgain = w->down = nullptr;
   w->dsteep = nullptr;
+  w->dorder = w->dkey = w->drank = nullptr;
   w->dcell = w->dctr = nullptr;
   w->max_drops = 0;
   SHY_CHECK_CUDA(dalloc(&w->dpos, n), "allocate drop slots");
@@ -128,6 +129,10 @@ int alloc_drop_slots(shy_world* w, int n) {
   SHY_CHECK_CUDA(dalloc(&w->dctr, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->down, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dsteep, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->dorder, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->dkey, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->drank, n), "allocate drop slots");
+  if (!w->dhist) SHY_CHECK_CUDA(dalloc(&w->dhist, 65536), "allocate drop slots");
   w->max_drops = n;
   return SHY_OK;
 }
@@ -250,6 +255,10 @@ int create_world(int n, const int* nx, const int* ny, const int* drops, const ui
   if ((e = cudaGetDevice(&w->device)) != cudaSuccess) return fail(e, "get device");
   if ((e = cudaDeviceGetAttribute(&w->sm_count, cudaDevAttrMultiProcessorCount, w->device)) != cudaSuccess)
     return fail(e, "device attributes");
+  int l2 = 0;
+  if ((e = cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, w->device)) != cudaSuccess)
+    return fail(e, "device attributes");
+  w->l2_bytes = l2;
   if ((e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking)) != cudaSuccess)
     return fail(e, "create stream");
   const size_t N = (size_t)cells;
@@ -595,14 +604,15 @@ int shy_world_get_field(shy_world* w, int field, float* host, size_t count) {
   return shy_terrain_get_field(w, 0, field, host, count);
 }
 
-int shy_world_set_launch(shy_world* w, int grid) {
+int shy_world_set_launch(shy_world* w, int grid, int order) {
   int rc = check_world(w);
   if (rc) return rc;
-  if (grid < 0) {
-    set_error("shy_world_set_launch: grid must be >= 0");
+  if (grid < 0 || order < -1 || order > 1) {
+    set_error("shy_world_set_launch: grid must be >= 0 and order -1, 0 or 1");
     return SHY_ERR_INVALID_ARG;
   }
   w->batch_grid = grid;
+  w->batch_order = order;
   return SHY_OK;
 }
 

@@ -156,16 +156,17 @@ def test_consecutive_calls_carry_fixed_point_state(shy, po):
     w.close()
 
 
-@pytest.mark.parametrize("grid", [1, 7])
-def test_launch_shape_does_not_change_results(shy, po, grid):
+@pytest.mark.parametrize("grid,order", [(1, 0), (7, 0), (0, 1), (1, 1)])
+def test_launch_shape_does_not_change_results(shy, po, grid, order):
     """Few CTAs put the drop slots in global memory (4096 drops on one CTA
-    need 640 KiB); the results equal the default launch's and the oracle's."""
+    need 640 KiB), and slots may be in spawn-cell order; the results equal
+    the default launch's and the oracle's."""
     nx, ny, drops = 128, 96, 4096
     H = po.value_noise(nx, ny, 13)
     outs = []
-    for g in (0, grid):
+    for g, o in ((0, 0), (grid, order)):
         w = shy.World(nx, ny, seed=6)
-        w.set_launch(g)
+        w.set_launch(g, o)
         w.set_field("height", H)
         w.erode(drops, 2)
         outs.append([w.get_field(f) for f in po.FIELDS])
