@@ -144,7 +144,8 @@ struct shy_world {
   long long* dcell = nullptr; // cell of this step's exchange, -1 if none
   long long* dctr = nullptr;  // cascade centre this slot runs this step, -1 if none
   shy::SteepCell* dsteep = nullptr;  // steep-cascade queue (one entry per drop slot at most)
-  unsigned long long* arr = nullptr;  // arrivals bitmap, all terrains
+  unsigned long long* arr = nullptr;  // arrivals bitmaps (two step parities), all terrains
+  long long arr_words = 0;            // words of one parity's bitmap
   int* dorder = nullptr;      // drop run by each slot in a batched cycle (spawn-cell order)
   int* dkey = nullptr;        // spawn-order scratch: run of each drop's spawn cell
   int* drank = nullptr;       //   and its place within the run
@@ -202,7 +203,8 @@ struct CycleBuffers {
   long long* cell;
   long long* ctr;
   SteepCell* steep;
-  unsigned long long* arr;
+  unsigned long long* arr;  // two bitmaps of arr_words words
+  long long arr_words;
   DevStats* st;
   GridBar* bar;
   shy_params P;

@@ -176,7 +176,8 @@ struct LockArgs {
   long long* cell;
   long long* ctr;
   SteepCell* steep;
-  unsigned long long* arr;  // arrivals bitmap
+  unsigned long long* arr;  // arrivals bitmaps, one per step parity, arr_words words each
+  long long arr_words;
   const int* order;  // drop run by each slot (slots ordered by spawn cell), or null: slot = drop
   int smem_slots;   // 1: drop slots and queue live in dynamic shared memory
   shy_params P;
@@ -443,6 +444,13 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   const shy_evap ev = a.ev;
   const int vmax = (int)P.max_age + 2;  // last entry of the volume table
 
+  // both arrivals bitmaps start the cycle empty (this CTA's share of them)
+  {
+    const long long w0 = (long long)blockIdx.x * (2 * a.arr_words) / gridDim.x;
+    const long long w1 = (long long)(blockIdx.x + 1) * (2 * a.arr_words) / gridDim.x;
+    for (long long i = w0 + threadIdx.x; i < w1; i += blockDim.x) a.arr[i] = 0ull;
+  }
+
   // spawn (source/world.h:64-74)
   unsigned long long born = 0;
   for (int j = threadIdx.x; j < nd; j += blockDim.x) {
@@ -597,7 +605,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       }
       S.ctr[j] = arrived_before == 0 ? c2 : -1;  // World::cascade(pos), water.h:151
       if (arrived_before == 0)
-        atomicOr(&a.arr[arr_word(T, jx, jy)], arr_bit(jx, jy));
+        atomicOr(&a.arr[par * a.arr_words + arr_word(T, jx, jy)], arr_bit(jx, jy));
       S.age[j] = ag + 1;
       S.pos[j] = p;
       S.spd[j] = s;
@@ -643,7 +651,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       const int tx0 = (ix >= 2 ? ix - 2 : 0) >> 3, tx1 = (ix + 2 < T.nx ? ix + 2 : T.nx - 1) >> 3;
       const int ty0 = (iy >= 2 ? iy - 2 : 0) >> 3, ty1 = (iy + 2 < T.ny ? iy + 2 : T.ny - 1) >> 3;
       const long long tyn = (T.ny + 7) >> 3;
-      const unsigned long long* AW = a.arr + T.arr_base;
+      const unsigned long long* AW = a.arr + par * a.arr_words + T.arr_base;
       const unsigned long long aw00 = load_arr(AW + tx0 * tyn + ty0);
       const unsigned long long aw01 = load_arr(AW + tx0 * tyn + ty1);
       const unsigned long long aw10 = load_arr(AW + tx1 * tyn + ty0);
@@ -697,6 +705,14 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         settle_cascade(qc, TT[qc.ti], a.cq, P);
       }
     }
+    // the other parity's bitmap (last read in the previous step's scan)
+    // starts empty for the next step's descend: this CTA's share of it
+    {
+      unsigned long long* other = a.arr + (par ^ 1) * a.arr_words;
+      const long long w0 = (long long)blockIdx.x * a.arr_words / gridDim.x;
+      const long long w1 = (long long)(blockIdx.x + 1) * a.arr_words / gridDim.x;
+      for (long long i = w0 + threadIdx.x; i < w1; i += blockDim.x) other[i] = 0ull;
+    }
     unsigned long long retired = 0;
     int ag_f = -1, ti_f = 0;
     long long c_f = -1, c2_f = -1, own_f = 0;
@@ -712,12 +728,6 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         ag_f = S.age[jn]; ti_f = S.terr[jn]; c_f = S.cell[jn]; c2_f = S.ctr[jn]; own_f = S.own[jn];
       }
       if (ag == -1) continue;
-      if (c2 >= 0) {  // the claim of this step ends
-        const Terrain T = TT[ti];
-        const int lc = (int)(c2 - T.cell_base);
-        const int x = lc / T.ny, y = lc - x * T.ny;
-        atomicAnd(&a.arr[arr_word(T, x, y)], ~arr_bit(x, y));
-      }
       if (c >= 0) {
         if (own != 0) add_i64(&a.cq[c].hq, own);
         a.cq[c].e = 0;
@@ -1008,6 +1018,7 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.ctr = w->dctr;
   a.steep = w->dsteep;
   a.arr = w->arr;
+  a.arr_words = w->arr_words;
   // Slots ordered by spawn cell when the cell state outgrows L2: each CTA's
   // drops then touch a compact stretch of the maps (+49 % at 8192^2).  While
   // the state fits in L2 locality buys nothing and compact CTAs at the map's
@@ -1078,6 +1089,7 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.ctr = b.ctr;
   a.steep = b.steep;
   a.arr = b.arr;
+  a.arr_words = b.arr_words;
   a.order = nullptr;
   a.smem_slots = 0;
   a.P = b.P;

@@ -24,8 +24,9 @@ struct NoallocScratch {
   float track_f[3 * SHY_NOALLOC_MAX_CELLS];
   float voltab[SHY_NOALLOC_MAX_AGE + 3];
   SteepCell steep[SHY_NOALLOC_MAX_DROPS];
-  // arrivals bitmap: ceil(nx / 8) * ceil(ny / 8) <= cells / 64 + (nx + ny) / 8 + 1 words
-  unsigned long long arr[SHY_NOALLOC_MAX_CELLS / 64 + (SHY_NOALLOC_MAX_CELLS + 1) / 8 + 2];
+  // arrivals bitmaps, two step parities of ceil(nx / 8) * ceil(ny / 8)
+  // <= cells / 64 + (nx + ny) / 8 + 1 words each
+  unsigned long long arr[2 * (SHY_NOALLOC_MAX_CELLS / 64 + (SHY_NOALLOC_MAX_CELLS + 1) / 8 + 2)];
   float2 pos[SHY_NOALLOC_MAX_DROPS], spd[SHY_NOALLOC_MAX_DROPS], vs[SHY_NOALLOC_MAX_DROPS];
   long long gain[SHY_NOALLOC_MAX_DROPS], own[SHY_NOALLOC_MAX_DROPS];
   long long cell[SHY_NOALLOC_MAX_DROPS], ctr[SHY_NOALLOC_MAX_DROPS];
@@ -134,7 +135,7 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
               SHY_NOALLOC_MAX_CELLS);
     return SHY_ERR_INVALID_ARG;
   }
-  if (arr_words(nx, ny) > (long long)(sizeof(((NoallocScratch*)nullptr)->arr) / sizeof(unsigned long long))) {
+  if (2 * arr_words(nx, ny) > (long long)(sizeof(((NoallocScratch*)nullptr)->arr) / sizeof(unsigned long long))) {
     set_error("shy_erode_noalloc: %d x %d map exceeds the fixed arrivals bitmap", nx, ny);
     return SHY_ERR_INVALID_ARG;
   }
@@ -172,7 +173,7 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
   T.seed = seed;
   const int blocks = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
   noalloc_init_kernel<<<1, 32, 0, s>>>(sc, T, cycle0, params->evap_rate, (int)params->max_age + 3);
-  noalloc_pack_kernel<<<blocks, 256, 0, s>>>(sc, n, arr_words(nx, ny), height, discharge, momentum_x,
+  noalloc_pack_kernel<<<blocks, 256, 0, s>>>(sc, n, 2 * arr_words(nx, ny), height, discharge, momentum_x,
                                              momentum_y, root_density, *params);
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "shy_erode_noalloc: set-up kernels");
 
@@ -198,6 +199,7 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
   b.ctr = sc->ctr;
   b.steep = sc->steep;
   b.arr = sc->arr;
+  b.arr_words = arr_words(nx, ny);
   b.st = &sc->st;
   b.bar = &sc->bar;
   b.P = *params;

@@ -272,7 +272,8 @@ int create_world(int n, const int* nx, const int* ny, const int* drops, const ui
   if ((e = dalloc(&w->cq, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->scratch, N)) != cudaSuccess) return fail(e, "allocate maps");
   if ((e = dalloc(&w->relax, N)) != cudaSuccess) return fail(e, "allocate maps");
-  if ((e = dalloc(&w->arr, (size_t)words)) != cudaSuccess) return fail(e, "allocate maps");
+  if ((e = dalloc(&w->arr, 2 * (size_t)words)) != cudaSuccess) return fail(e, "allocate maps");
+  w->arr_words = words;
   if ((e = dalloc(&w->dterrains, (size_t)n)) != cudaSuccess) return fail(e, "allocate terrain table");
   if ((e = dalloc(&w->stats, 1)) != cudaSuccess) return fail(e, "allocate counters");
   if ((e = dalloc(&w->bar, 1)) != cudaSuccess) return fail(e, "allocate counters");
@@ -286,7 +287,7 @@ int create_world(int n, const int* nx, const int* ny, const int* drops, const ui
   cudaMemsetAsync(w->rec, 0, sizeof(float4) * N, s);
   cudaMemsetAsync(w->trk, 0, sizeof(Tracks) * N, s);
   cudaMemsetAsync(w->cq, 0, sizeof(CellQ) * N, s);
-  cudaMemsetAsync(w->arr, 0, sizeof(unsigned long long) * (size_t)words, s);
+  cudaMemsetAsync(w->arr, 0, sizeof(unsigned long long) * 2 * (size_t)words, s);
   cudaMemsetAsync(w->stats, 0, sizeof(DevStats), s);
   cudaMemsetAsync(w->bar, 0, sizeof(GridBar), s);
   if ((e = cudaGetLastError()) != cudaSuccess) return fail(e, "initialise maps");
