@@ -27,7 +27,10 @@
 //      sequential transfer loop on one thread and adds its transfers straight
 //      to the fixed-point heights (no height is read in this phase).  Every
 //      drop adds its own height change to its cell's fixed-point height and
-//      clears the cell's pending sum and count; finished drops retire.
+//      clears the cell's pending sum and count; finished drops retire.  The
+//      arrivals bitmap of the other step parity is cleared for the next step.
+// With the cell state larger than L2, each cycle's drops go to slots sorted by
+// spawn cell, so that a CTA works on a compact stretch of the maps.
 // Heights live in 32.32 fixed point for the whole cycle (the float map is
 // rewritten at its end), so every update is an integer addition.
 // Integer sums make every result independent of thread timing: the same
