@@ -206,3 +206,38 @@ def test_state_calls_equal_field_calls(shy, po):
     assert not b.get_field("momentum_x").any()
     a.close()
     b.close()
+
+
+def test_batch_beyond_shared_terrain_table(shy, po):
+    """More terrains than the kernel's shared-memory terrain table (128): the
+    table is read from global memory; every terrain still equals the oracle."""
+    n = 130
+    rng = np.random.default_rng(11)
+    sizes = [(int(rng.integers(4, 20)), int(rng.integers(4, 20))) for _ in range(n)]
+    drops = [int(rng.integers(0, 40)) for _ in range(n)]
+    seeds = [500 + i for i in range(n)]
+    b = shy.Batch(sizes, drops, seeds)
+    for t in range(n):
+        b.generate(t, seeds[t], 4)
+    b.erode(2)
+    for t in (0, 1, 64, 127, 128, 129):
+        nx, ny = sizes[t]
+        m = po.Maps(nx, ny, height=po.value_noise(nx, ny, seeds[t], 4))
+        po.erode_batched(m, seeds[t], 0, drops[t], 2)
+        compare_all(lambda f: b.get_field(t, f), m, po, f"terrain {t}")
+    b.close()
+
+
+def test_autotune_applies_a_shape_and_keeps_results(shy, po):
+    from simplehydrology_gb300 import autotune
+    nx, ny, drops = 96, 80, 2000
+    H = po.value_noise(nx, ny, 21)
+    w = shy.World(nx, ny, seed=3)
+    w.set_field("height", H)
+    best, times = autotune.autotune(w, drops, cycles=1, shapes=[(0, -1), (7, 0), (0, 1)])
+    assert best in times and len(times) == 3
+    w.erode(drops, 2)  # with the chosen shape
+    m = po.Maps(nx, ny, height=H)
+    po.erode_batched(m, 3, 0, drops, 2)
+    compare_all(w.get_field, m, po, "after autotune")
+    w.close()
