@@ -66,10 +66,7 @@ class Map {
     momx_.resize(n);
     momy_.resize(n);
     root_.resize(n);
-    check(shy_world_get_field(w, SHY_FIELD_HEIGHT, height_.data(), n));
-    check(shy_world_get_field(w, SHY_FIELD_DISCHARGE, discharge_.data(), n));
-    check(shy_world_get_field(w, SHY_FIELD_MOMENTUM_X, momx_.data(), n));
-    check(shy_world_get_field(w, SHY_FIELD_MOMENTUM_Y, momy_.data(), n));
+    check(shy_terrain_get_state(w, 0, height_.data(), discharge_.data(), momx_.data(), momy_.data(), n));
     check(shy_world_get_field(w, SHY_FIELD_ROOT_DENSITY, root_.data(), n));
   }
   // quad::map::oob, source/cellpool.h:413-419 (positions truncate like glm::ivec2)
