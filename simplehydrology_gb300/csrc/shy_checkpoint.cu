@@ -242,8 +242,8 @@ extern "C" int shy_world_load(const char* path, shy_world** out) {
   bool ok = r.get(&P, sizeof(P));
   uint64_t cells = 0;
   for (uint32_t t = 0; ok && t < h.n_terrains; ++t) {
-    TerrainRec tr;
-    ok = r.get(&tr, sizeof(tr));
+    TerrainRec tr = {};
+    if (!(ok = r.get(&tr, sizeof(tr)))) break;
     nx[t] = tr.nx;
     ny[t] = tr.ny;
     drops[t] = tr.drops;

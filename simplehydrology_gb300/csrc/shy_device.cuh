@@ -14,17 +14,6 @@
 
 namespace shy {
 
-// ---- 32.32 fixed point ------------------------------------------------------
-__device__ __forceinline__ long long q32(float v) { return __float2ll_rn(v * 4294967296.0f); }
-__device__ __forceinline__ long long q64(double v) { return __double2ll_rn(v * 4294967296.0); }
-__device__ __forceinline__ float unq(long long q) {
-  return __double2float_rn(__ll2double_rn(q) * (1.0 / 4294967296.0));
-}
-// h plus a fixed-point sum, rounded once
-__device__ __forceinline__ float addq(float h, long long q) {
-  return __double2float_rn((double)h + __ll2double_rn(q) * (1.0 / 4294967296.0));
-}
-
 // ---- glm semantics on float2/float3 (component-wise, dot summed left to right)
 __device__ __forceinline__ float dot2(float ax, float ay, float bx, float by) { return ax * bx + ay * by; }
 __device__ __forceinline__ float len2(float x, float y) { return sqrtf(dot2(x, y, x, y)); }

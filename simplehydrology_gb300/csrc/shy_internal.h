@@ -241,7 +241,6 @@ cudaError_t launch_unpack_state(shy_world* w, int t, float* d, float* mx, float*
 // timing: open a launch interval of `kind` (returns the pair index or -1)
 cudaError_t timing_begin(shy_world* w, int kind, int* slot);
 cudaError_t timing_end(shy_world* w, int slot);
-int batched_max_grid(shy_world* w, int block);
 
 void set_error(const char* fmt, ...);
 int cuda_fail(cudaError_t e, const char* what);

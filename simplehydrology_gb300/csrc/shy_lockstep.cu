@@ -93,6 +93,7 @@ __device__ __forceinline__ CellView load_cell(const CellQ* p) {
   asm volatile("ld.global.v4.u64 {%0, %1, %2, %3}, [%4];"
                : "=l"(w0), "=l"(w1), "=l"(w2), "=l"(w3)
                : "l"(p));
+  (void)w1;  // the pending erosion sum: not needed here
   CellView v;
   v.hq = (long long)w0;
   v.effd = __uint_as_float((unsigned)(w2 & 0xffffffffull));
@@ -717,18 +718,18 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       for (long long i = w0 + threadIdx.x; i < w1; i += blockDim.x) other[i] = 0ull;
     }
     unsigned long long retired = 0;
-    int ag_f = -1, ti_f = 0;
-    long long c_f = -1, c2_f = -1, own_f = 0;
+    int ag_f = -1;
+    long long c_f = -1, own_f = 0;
     if ((int)threadIdx.x < nd) {
       const int j = threadIdx.x;
-      ag_f = S.age[j]; ti_f = S.terr[j]; c_f = S.cell[j]; c2_f = S.ctr[j]; own_f = S.own[j];
+      ag_f = S.age[j]; c_f = S.cell[j]; own_f = S.own[j];
     }
     for (int j = threadIdx.x; j < nd; j += blockDim.x) {
-      const int ag = ag_f, ti = ti_f;
-      const long long c = c_f, c2 = c2_f, own = own_f;
+      const int ag = ag_f;
+      const long long c = c_f, own = own_f;
       if (j + (int)blockDim.x < nd) {  // the next slot, loaded ahead
         const int jn = j + blockDim.x;
-        ag_f = S.age[jn]; ti_f = S.terr[jn]; c_f = S.cell[jn]; c2_f = S.ctr[jn]; own_f = S.own[jn];
+        ag_f = S.age[jn]; c_f = S.cell[jn]; own_f = S.own[jn];
       }
       if (ag == -1) continue;
       if (c >= 0) {
@@ -941,13 +942,6 @@ cudaError_t launch_spawn_order(shy_world* w, int total) {
   order_scatter_kernel<<<grid < 1 ? 1 : grid, 256, 0, w->stream>>>(total, w->dhist, w->dkey, w->drank,
                                                                     w->dorder);
   return cudaGetLastError();
-}
-
-int batched_max_grid(shy_world* w, int block) {
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lockstep_kernel, block, 0) != cudaSuccess)
-    return 0;
-  return per_sm * w->sm_count;
 }
 
 namespace {
