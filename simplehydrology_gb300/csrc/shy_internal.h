@@ -60,17 +60,27 @@ struct DevStats {
   double gain_exact, loss_exact;  // exact (sequential) mode
 };
 
-// A cascade of the current step that will move height: its centre, the
-// nine heights it starts from, and the arrivals-bitmap words around it from
-// which its overlap counts are taken (aw[2 * i + j]: tile column tx0 + i,
-// tile row ty0 + j).
+// A cascade of the current step that will move height.  Phase scan queues
+// its centre, the nine heights it starts from, and the arrivals-bitmap words
+// around it from which its overlap counts are taken (aw[2 * i + j]: tile
+// column tx0 + i, tile row ty0 + j).  Its transfers are then worked out in
+// place: the 32.32 change of each neighbour (by neighbour index) and of the
+// centre replace those inputs until settle adds them.
 struct alignas(16) SteepCell {
   long long c2;
   int ti;
   float h0;
-  float v[8];
-  unsigned long long aw[4];
-  int tx0, ty0, ix, iy;
+  union {
+    struct {
+      float v[8];
+      unsigned long long aw[4];
+      int tx0, ty0, ix, iy;
+    } in;
+    struct {
+      long long dq[8];  // neighbour changes
+      long long dc;     // centre change
+    } out;
+  } u;
 };
 
 // Grid barrier state of the persistent lock-step kernel.

@@ -19,16 +19,18 @@
 //      Cascades that move nothing end here.  The steep ones are queued in the
 //      CTA with the heights they read and the words of an arrivals bitmap
 //      (8 x 8 cells per word, loaded with the heights) that hold the claimed
-//      centres of the 5 x 5 block around theirs.
-//   settle  each queued cascade takes its overlap counts from those words:
-//      where the 3 x 3 blocks of k cascades overlap, a pair's transfer is
-//      divided by k (the larger count of its two cells), so overlapping
-//      cascades together move what one would.  It then runs the reference's
-//      sequential transfer loop on one thread and adds its transfers straight
-//      to the fixed-point heights (no height is read in this phase).  Every
-//      drop adds its own height change to its cell's fixed-point height and
-//      clears the cell's pending sum and count; finished drops retire.  The
-//      arrivals bitmap of the other step parity is cleared for the next step.
+//      centres of the 5 x 5 block around theirs.  While thread 0 waits at
+//      the grid barrier, the CTA's other warps work out each queued
+//      cascade's transfers from what scan read: its overlap counts from those
+//      words (where the 3 x 3 blocks of k cascades overlap, a pair's transfer
+//      is divided by k, the larger count of its two cells, so overlapping
+//      cascades together move what one would), then the reference's
+//      sequential transfer loop on one thread.
+//   settle  the queued transfers go straight to the fixed-point heights (no
+//      height is read in this phase).  Every drop adds its own height change
+//      to its cell's fixed-point height and clears the cell's pending sum and
+//      count; finished drops retire.  The arrivals bitmap of the other step
+//      parity is cleared for the next step.
 // With the cell state larger than L2, each cycle's drops go to slots sorted by
 // spawn cell, so that a CTA works on a compact stretch of the maps.
 // Heights live in 32.32 fixed point for the whole cycle (the float map is
@@ -85,6 +87,7 @@ __device__ __forceinline__ void add_i64(long long* p, long long v) {
 // rate and the two step-parity drop counts.
 struct CellView {
   long long hq;
+  long long e;  // the pending erosion sum (not needed by descend)
   float effd;
   int cnt0, cnt1;  // drop counts by step parity
 };
@@ -93,9 +96,9 @@ __device__ __forceinline__ CellView load_cell(const CellQ* p) {
   asm volatile("ld.global.v4.u64 {%0, %1, %2, %3}, [%4];"
                : "=l"(w0), "=l"(w1), "=l"(w2), "=l"(w3)
                : "l"(p));
-  (void)w1;  // the pending erosion sum: not needed here
   CellView v;
   v.hq = (long long)w0;
+  v.e = (long long)w1;
   v.effd = __uint_as_float((unsigned)(w2 & 0xffffffffull));
   v.cnt0 = (int)(unsigned)(w3 & 0xffffffffull);
   v.cnt1 = (int)(unsigned)(w3 >> 32);
@@ -124,10 +127,14 @@ __device__ __forceinline__ unsigned long long arr_bit(int x, int y) {
 // added its retirements before arriving) and leaves it in `*live` for the
 // whole CTA.  Every wait is bounded: past kBarrierLimitNs the waiter sets
 // bar->abort and every later barrier returns false at once, so the kernel
-// always ends.
-__device__ bool grid_barrier(GridBar* bar, unsigned& passed, unsigned long long* live) {
+// always ends.  Warps 1 and up run `work` while thread 0 waits: work that
+// neither reads what other CTAs write before the barrier nor writes what they
+// read.
+template <class Work>
+__device__ bool grid_barrier(GridBar* bar, unsigned& passed, unsigned long long* live, Work&& work) {
   __shared__ int s_ok;
   __syncthreads();
+  if (threadIdx.x >= 32) work();
   if (threadIdx.x == 0) {
     const unsigned long long target = (unsigned long long)(passed + 1) * gridDim.x;
     red_release_add_u64(&bar->arrive, 1ull);
@@ -155,6 +162,10 @@ __device__ bool grid_barrier(GridBar* bar, unsigned& passed, unsigned long long*
   __syncthreads();
   ++passed;
   return s_ok != 0;
+}
+
+__device__ __forceinline__ bool grid_barrier(GridBar* bar, unsigned& passed, unsigned long long* live) {
+  return grid_barrier(bar, passed, live, [] {});
 }
 
 struct LockArgs {
@@ -346,19 +357,18 @@ __device__ __forceinline__ void overlap_counts(unsigned long long w00, unsigned 
 // centre: the neighbours in the reference's stable height order, the live
 // centre height, each transfer divided by the overlap count of its pair.
 // Everything that does not depend on the live centre height is computed
-// before the sequential loop.  Transfers go straight to the fixed-point
-// heights.
-__device__ __forceinline__ void settle_cascade(const SteepCell& qc, const Terrain& T, CellQ* cq,
-                                               const shy_params& P) {
-  const long long c2 = qc.c2;
+// before the sequential loop.  The 32.32 changes replace the entry's inputs
+// (all read first); `steep_apply` adds them to the heights.
+__device__ __forceinline__ void steep_transfers(SteepCell& q, const Terrain& T, const shy_params& P) {
   unsigned kv;
   int kc;
-  overlap_counts(qc.aw[0], qc.aw[1], qc.aw[2], qc.aw[3], qc.tx0, qc.ty0, qc.ix, qc.iy, T, kv, kc);
+  overlap_counts(q.u.in.aw[0], q.u.in.aw[1], q.u.in.aw[2], q.u.in.aw[3], q.u.in.tx0, q.u.in.ty0, q.u.in.ix,
+                 q.u.in.iy, T, kv, kc);
   float v[8];
   int sk[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    v[k] = qc.v[k];
+    v[k] = q.u.in.v[k];
     sk[k] = k;
   }
   sort8(v, sk);
@@ -375,7 +385,7 @@ __device__ __forceinline__ void settle_cascade(const SteepCell& qc, const Terrai
     const int kn = (int)((kv >> (4 * k)) & 15u);
     kk[j] = kc > kn ? kc : kn;
   }
-  const float h0 = qc.h0;
+  const float h0 = q.h0;
   float hcv = h0;
   float tr[8];
   bool moved = false;
@@ -399,10 +409,23 @@ __device__ __forceinline__ void settle_cascade(const SteepCell& qc, const Terrai
     moved = true;
   }
 #pragma unroll
+  for (int k = 0; k < 8; ++k) q.u.out.dq[k] = 0;
+#pragma unroll
   for (int j = 0; j < 8; ++j)
-    if (tr[j] != 0.0f)
-      add_i64(&cq[c2 + (long long)nb_dx(sk[j]) * T.ny + nb_dy(sk[j])].hq, shy_q32(tr[j]));
-  if (moved) add_i64(&cq[c2].hq, shy_q32(hcv - h0));
+    if (tr[j] != 0.0f) q.u.out.dq[sk[j]] = shy_q32(tr[j]);
+  q.u.out.dc = moved ? shy_q32(hcv - h0) : 0;
+}
+
+// The changes `steep_transfers` left in a queued entry, added to the
+// fixed-point heights.
+__device__ __forceinline__ void steep_apply(const SteepCell& q, const Terrain& T, CellQ* cq) {
+  const long long c2 = q.c2;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const long long d = q.u.out.dq[k];
+    if (d != 0) add_i64(&cq[c2 + (long long)nb_dx(k) * T.ny + nb_dy(k)].hq, d);
+  }
+  if (q.u.out.dc != 0) add_i64(&cq[c2].hq, q.u.out.dc);
 }
 
 // 128 registers: two 256-thread CTAs per SM
@@ -676,38 +699,43 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       }
       if (any) {
         // one claim per drop slot, so the queue (cap entries) cannot overflow;
-        // the overlap counts are worked out in settle, off this phase's tail
+        // the transfers are worked out during the barrier, off this phase's tail
         SteepCell& q = S.steep[atomicAdd(&s_nq, 1)];
         q.c2 = c2;
         q.ti = ti;
         q.h0 = h0;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) q.v[k] = sh[k];
-        q.aw[0] = aw00;
-        q.aw[1] = aw01;
-        q.aw[2] = aw10;
-        q.aw[3] = aw11;
-        q.tx0 = tx0;
-        q.ty0 = ty0;
-        q.ix = ix;
-        q.iy = iy;
+        for (int k = 0; k < 8; ++k) q.u.in.v[k] = sh[k];
+        q.u.in.aw[0] = aw00;
+        q.u.in.aw[1] = aw01;
+        q.u.in.aw[2] = aw10;
+        q.u.in.aw[3] = aw11;
+        q.u.in.tx0 = tx0;
+        q.u.in.ty0 = ty0;
+        q.u.in.ix = ix;
+        q.u.in.iy = iy;
       }
     }
     lap(2);
-    if (!grid_barrier(a.bar, passed, nullptr)) { ok = false; break; }
+    // The queued cascades' transfers use only what scan read, so warps 1 and
+    // up work them out while thread 0 waits; the entries go to the highest
+    // threads first (those past the CTA's last drop slot) and each thread
+    // adds its own entries' changes in settle.
+    auto transfers = [&]() {
+      const int nq = s_nq;
+      for (int i = (int)blockDim.x - 1 - (int)threadIdx.x; i < nq; i += (int)blockDim.x - 32)
+        steep_transfers(S.steep[i], TT[S.steep[i].ti], P);
+    };
+    if (!grid_barrier(a.bar, passed, nullptr, transfers)) { ok = false; break; }
     lap(3);
 
     // ---- settle: steep cascades, each drop's own change, retirements ----
     // Every addition here is an integer atomic on a fixed-point height that
     // nobody reads in this phase, so the order does not matter.
-    {
-      // queued cascades go to the highest threads first: those past the
-      // CTA's last drop slot have no drop of their own to settle
+    if (threadIdx.x >= 32) {  // the entries each thread worked out during the barrier
       const int nq = s_nq;
-      for (int i = (int)blockDim.x - 1 - (int)threadIdx.x; i < nq; i += blockDim.x) {
-        const SteepCell qc = S.steep[i];
-        settle_cascade(qc, TT[qc.ti], a.cq, P);
-      }
+      for (int i = (int)blockDim.x - 1 - (int)threadIdx.x; i < nq; i += (int)blockDim.x - 32)
+        steep_apply(S.steep[i], TT[S.steep[i].ti], a.cq);
     }
     // the other parity's bitmap (last read in the previous step's scan)
     // starts empty for the next step's descend: this CTA's share of it
