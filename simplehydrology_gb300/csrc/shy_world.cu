@@ -93,7 +93,8 @@ void free_world(shy_world* w) {
   void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
                   w->dterr, w->dcell, w->dctr, w->dterrains, w->stats, w->bar, w->ddrop,
                   w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down,
-                  w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed, w->crand, w->plants, w->stage, w->dorder, w->dkey, w->drank, w->dhist};
+                  w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed, w->crand, w->plants, w->stage, w->dorder, w->dkey, w->drank, w->dhist,
+                  w->dsteep};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& p : w->timing.pending) {
