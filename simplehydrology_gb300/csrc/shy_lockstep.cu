@@ -31,8 +31,10 @@
 //      to its cell's fixed-point height and clears the cell's pending sum and
 //      count; finished drops retire.  The arrivals bitmap of the other step
 //      parity is cleared for the next step.
-// With the cell state larger than L2, each cycle's drops go to slots sorted by
-// spawn cell, so that a CTA works on a compact stretch of the maps.
+// With the cell state larger than L2, each cycle's drops are sorted by spawn
+// cell and dealt to the CTAs in runs of consecutive drops, round-robin: each
+// run is a compact stretch of the maps, and every CTA samples stretches from
+// the whole map, so live drops stay balanced across CTAs as drops retire.
 // Heights live in 32.32 fixed point for the whole cycle (the float map is
 // rewritten at its end), so every update is an integer addition.
 // Integer sums make every result independent of thread timing: the same
@@ -168,6 +170,39 @@ __device__ __forceinline__ bool grid_barrier(GridBar* bar, unsigned& passed, uns
   return grid_barrier(bar, passed, live, [] {});
 }
 
+// Drops sorted by spawn cell go to the CTAs in runs of this many, dealt
+// round-robin: at least about eight runs per CTA, at most 256 drops per run.
+__host__ __device__ __forceinline__ long long order_run(long long total, long long grid) {
+  const long long r = total / (8 * grid);
+  return r < 1 ? 1 : (r > 256 ? 256 : r);
+}
+
+// The drop slots of CTA b of `grid`: first slot `lo`, `nd` of them, storage
+// for `cap` (the most any CTA of the launch has).  Unordered, the slots are
+// consecutive drops.  Ordered, run k of the CTA's is run k * grid + b of the
+// sorted drops, the runs being `run` drops long (the last one may be short).
+struct SlotRange {
+  long long lo;
+  int nd, cap;
+};
+__host__ __device__ __forceinline__ SlotRange slot_range(long long total, long long grid, long long b, bool ordered) {
+  SlotRange r;
+  if (!ordered) {
+    r.lo = b * total / grid;
+    r.nd = (int)((b + 1) * total / grid - r.lo);
+    r.cap = (int)((total + grid - 1) / grid);
+    return r;
+  }
+  const long long R = order_run(total, grid);
+  const long long runs = (total + R - 1) / R, q = runs / grid, m = runs % grid;
+  const long long short_by = total % R ? R - total % R : 0;  // the last run's shortfall
+  const long long last_owner = (runs - 1) % grid;
+  r.nd = (int)((q + (b < m ? 1 : 0)) * R - (last_owner == b ? short_by : 0));
+  r.lo = R * (b * q + (b < m ? b : m)) - (last_owner < b ? short_by : 0);
+  r.cap = (int)((q + (m ? 1 : 0)) * R);
+  return r;
+}
+
 struct LockArgs {
   const Terrain* terrains;
   int n_terrains;
@@ -193,7 +228,7 @@ struct LockArgs {
   SteepCell* steep;
   unsigned long long* arr;  // arrivals bitmaps, one per step parity, arr_words words each
   long long arr_words;
-  const int* order;  // drop run by each slot (slots ordered by spawn cell), or null: slot = drop
+  const int* order;  // drops sorted by spawn cell (dealt to the CTAs in runs), or null: slot = drop
   int smem_slots;   // 1: drop slots and queue live in dynamic shared memory
   shy_params P;
   DevStats* st;
@@ -441,12 +476,12 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   __syncthreads();
   const Terrain* TT = smem_t ? sT : a.terrains;
 
-  // this CTA's drop slots: [lo, hi), at most `cap` of them
-  const long long lo = (long long)blockIdx.x * a.total_drops / gridDim.x;
-  const long long hi = (long long)(blockIdx.x + 1) * a.total_drops / gridDim.x;
-  const int nd = (int)(hi - lo);
-  const int cap = (int)(((long long)a.total_drops + gridDim.x - 1) / gridDim.x);
+  // this CTA's drop slots: [lo, lo + nd), storage for `cap`
+  const SlotRange sr = slot_range(a.total_drops, gridDim.x, blockIdx.x, a.order != nullptr);
+  const long long lo = sr.lo;
+  const int nd = sr.nd, cap = sr.cap;
   const Slots S = slots_of(a, s_dyn, lo, cap);
+  const long long run = order_run(a.total_drops, gridDim.x);
 
   const shy_params& P = a.P;
   const unsigned long long cycle = a.bar->cycle;
@@ -481,7 +516,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   // spawn (source/world.h:64-74)
   unsigned long long born = 0;
   for (int j = threadIdx.x; j < nd; j += blockDim.x) {
-    const long long d = a.order ? a.order[lo + j] : lo + j;
+    const long long d = a.order ? a.order[((long long)(j / run) * gridDim.x + blockIdx.x) * run + j % run] : lo + j;
     const int t = find_terrain(TT, a.n_terrains, (int)d);
     const Terrain T = TT[t];
     int x, y;
@@ -995,7 +1030,7 @@ cudaError_t launch_lockstep(LockArgs& a, int sm_count, int grid_hint, cudaStream
 
   const long long g = (long long)per0 * sm_count < want ? (long long)per0 * sm_count : want;
   const int grid = (int)g;
-  const long long b = (((long long)a.total_drops + g - 1) / g) * kSlotBytes;
+  const long long b = (long long)slot_range(a.total_drops, g, 0, a.order != nullptr).cap * kSlotBytes;
   size_t bytes = 0;
   a.smem_slots = 0;
   if (b <= max_dyn) {
@@ -1044,10 +1079,11 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.steep = w->dsteep;
   a.arr = w->arr;
   a.arr_words = w->arr_words;
-  // Slots ordered by spawn cell when the cell state outgrows L2: each CTA's
-  // drops then touch a compact stretch of the maps (+49 % at 8192^2).  While
-  // the state fits in L2 locality buys nothing and compact CTAs at the map's
-  // edges finish early, so the slots keep the drop order.
+  // Drops sorted by spawn cell and dealt to the CTAs in runs when the cell
+  // state outgrows L2: each run touches a compact stretch of the maps, and
+  // every CTA holds runs from the whole map, so its live drops stay in
+  // balance with the other CTAs'.  While the state fits in L2 the slots keep
+  // the drop order.
   const long long state_bytes = w->cells * (long long)(sizeof(CellQ) + sizeof(Tracks) + sizeof(float4) + 4);
   const bool ordered = w->batch_order < 0 ? state_bytes > w->l2_bytes : w->batch_order != 0;
   a.order = ordered ? w->dorder : nullptr;
