@@ -261,6 +261,16 @@ int shy_terrain_erode_exact(shy_world* w, int terrain, const int32_t* spawn_xy, 
  * the workloads' recipe; the normalisation is the reference's (:382-409). */
 int shy_terrain_generate(shy_world* w, int terrain, uint64_t seed, int octaves);
 
+/* Terrain input: the reference's own map initialisation, quad::map::init
+ * (source/cellpool.h:323-411).  Eight layers of FastNoiseLite OpenSimplex2
+ * FBm noise at frequencies 2^o and weights 0.6^(o+1), sampled at
+ * (x / nx, y / ny, seed % 10000) with the library's default settings, then
+ * min-max normalised with the minimum and maximum starting at 0.  Generated
+ * on the device with the reference's float operations in its order: the
+ * heights are the reference's bit for bit (pinned against the reference's
+ * own init at 512 x 512).  `seed` is the reference's int SEED. */
+int shy_terrain_init(shy_world* w, int terrain, int32_t seed);
+
 /* ---- batched erosion without allocation ------------------------------------
  * No counterpart in the reference (which has no GPU path); the library adds
  * it for callers that cannot allocate device memory themselves or through

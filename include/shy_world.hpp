@@ -4,6 +4,7 @@
 // Vegetation::grow(); reads of map cells) keeps its shape:
 //
 //   shy_ref::World::init(512, 512, seed);          // World::map.init, source/cellpool.h:323
+//                                                  //   (the reference's terrain for seed)
 //   shy_ref::World::map.set_heights(h);            // inject a terrain
 //   shy_ref::World::erode(512);                    // World::erode, source/world.h:54-88
 //   shy_ref::World::cascade({x, y});               // World::cascade, source/world.h:90-168
@@ -97,6 +98,8 @@ class World {
     check(shy_world_create(nx, ny, p, seed, &map.w));
     map.nx = nx;
     map.ny = ny;
+    // the reference's terrain: quad::map::init(..., int SEED), cellpool.h:323-411
+    check(shy_terrain_init(map.w, 0, (int32_t)seed));
   }
   static void shutdown() {
     if (map.w) shy_world_destroy(map.w);

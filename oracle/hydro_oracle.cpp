@@ -26,6 +26,11 @@
 //     batched mode.  The first two are pinned against the reference build
 //     (tests/golden/ref_frames.json, ref_feed.json).
 //
+//  4. The reference's terrain: quad::map::init's OpenSimplex2 FBm layers
+//     (source/cellpool.h:323-411), through the vendored FastNoiseLite
+//     library's noise as that call configures it.  Pinned against the
+//     reference build (tests/golden/ref_terrain.json).
+//
 // Built with -ffp-contract=off so that no multiply-add is fused (the
 // reference's x86 build has no FMA either).
 #include <algorithm>
@@ -753,6 +758,102 @@ void vegetation_step(Grid<float>& g, float* plant, const shy_params& P, uint64_t
     if (dq[i] != 0) g.root[i] = g.root[i] + unq(dq[i]);
 }
 
+// ---- 4. the reference's terrain (source/cellpool.h:323-411) ----------------
+//
+// quad::map::init keeps one static FastNoiseLite object
+// (source/include/FastNoiseLite.h) set to OpenSimplex2 noise with FBm
+// fractals and otherwise at the library's defaults: noise seed 1337, three
+// octaves, lacunarity 2, gain 0.5, weighted strength 0, fractal bounding
+// 1 / 1.75, and the OpenSimplex2 3D rotation of the coordinates.  Integer
+// arithmetic is done on uint32_t, which wraps as the library's int does.
+struct FnlNoise {
+  float frequency = 0.01f;
+  static constexpr uint32_t kPx = 501125321u, kPy = 1136930381u, kPz = 1720413743u;
+
+  // the library's 3D gradient set: its twelve cube-edge vectors five times
+  // over, then edges 8, 1, 9 and 3
+  static void gradient(int index, float g[3]) {
+    static const signed char edge[12][3] = {{0, 1, 1},  {0, -1, 1},  {0, 1, -1},  {0, -1, -1},
+                                            {1, 0, 1},  {-1, 0, 1},  {1, 0, -1},  {-1, 0, -1},
+                                            {1, 1, 0},  {-1, 1, 0},  {1, -1, 0},  {-1, -1, 0}};
+    static const int tail[4] = {8, 1, 9, 3};
+    const int e = index < 60 ? index % 12 : tail[index - 60];
+    for (int c = 0; c < 3; ++c) g[c] = (float)edge[e][c];
+  }
+  static float grad_coord(uint32_t seed, uint32_t xp, uint32_t yp, uint32_t zp, float xd, float yd, float zd) {
+    uint32_t hash = (seed ^ xp ^ yp ^ zp) * 0x27d4eb2du;
+    hash ^= hash >> 15;
+    float g[3];
+    gradient((int)((hash & (63u << 2)) >> 2), g);
+    return xd * g[0] + yd * g[1] + zd * g[2];
+  }
+  static int round_half_away(float f) { return f >= 0 ? (int)(f + 0.5f) : (int)(f - 0.5f); }
+
+  // one octave of 3D OpenSimplex2 (coordinates already rotated)
+  static float opensimplex2(uint32_t seed, float x, float y, float z) {
+    const int ri = round_half_away(x), rj = round_half_away(y), rk = round_half_away(z);
+    float d[3] = {x - (float)ri, y - (float)rj, z - (float)rk};
+    int sign[3];
+    float ad[3];
+    for (int c = 0; c < 3; ++c) {
+      sign[c] = (int)(-1.0f - d[c]) | 1;
+      ad[c] = (float)sign[c] * -d[c];
+    }
+    const uint32_t prime[3] = {kPx, kPy, kPz};
+    uint32_t lat[3] = {(uint32_t)ri * kPx, (uint32_t)rj * kPy, (uint32_t)rk * kPz};
+    float value = 0.0f;
+    float a = (0.6f - d[0] * d[0]) - (d[1] * d[1] + d[2] * d[2]);
+    for (int pass = 0;; ++pass) {
+      if (a > 0) value += (a * a) * (a * a) * grad_coord(seed, lat[0], lat[1], lat[2], d[0], d[1], d[2]);
+      // the next vertex along the coordinate of largest distance (ties: x
+      // before y before z)
+      const int c = (ad[0] >= ad[1] && ad[0] >= ad[2]) ? 0 : ((ad[1] > ad[0] && ad[1] >= ad[2]) ? 1 : 2);
+      float b = a + 1;
+      float d1[3] = {d[0], d[1], d[2]};
+      uint32_t lat1[3] = {lat[0], lat[1], lat[2]};
+      d1[c] += (float)sign[c];
+      b -= (float)(sign[c] * 2) * d1[c];
+      lat1[c] -= (uint32_t)sign[c] * prime[c];
+      if (b > 0) value += (b * b) * (b * b) * grad_coord(seed, lat1[0], lat1[1], lat1[2], d1[0], d1[1], d1[2]);
+      if (pass == 1) break;
+      for (int k = 0; k < 3; ++k) {
+        ad[k] = 0.5f - ad[k];
+        d[k] = (float)sign[k] * ad[k];
+      }
+      a += (0.75f - ad[0]) - (ad[1] + ad[2]);
+      for (int k = 0; k < 3; ++k) {
+        if (sign[k] < 0) lat[k] += prime[k];
+        sign[k] = -sign[k];
+      }
+      seed = ~seed;
+    }
+    return value * 32.69428253173828125f;
+  }
+
+  // GetNoise(x, y, z): frequency, the OpenSimplex2 rotation, FBm octaves
+  float get(float x, float y, float z) const {
+    x *= frequency;
+    y *= frequency;
+    z *= frequency;
+    const float r = (x + y + z) * (float)(2.0 / 3.0);
+    x = r - x;
+    y = r - y;
+    z = r - z;
+    uint32_t seed = 1337u;
+    float sum = 0.0f, amp = 1 / 1.75f;
+    for (int o = 0; o < 3; ++o) {
+      const float n = opensimplex2(seed++, x, y, z);
+      sum += n * amp;
+      amp *= 1.0f + 0.0f * ((n + 1) * 0.5f - 1.0f);  // Lerp with weighted strength 0
+      x *= 2.0f;
+      y *= 2.0f;
+      z *= 2.0f;
+      amp *= 0.5f;
+    }
+    return sum;
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -975,6 +1076,34 @@ void orc_value_noise(int nx, int ny, uint64_t seed, int octaves, float* out) {
     }
   const double span = hi - lo;
   for (size_t i = 0; i < N; ++i) out[i] = span > 0.0 ? (float)((v[i] - lo) / span) : 0.0f;
+}
+
+// quad::map::init's terrain (source/cellpool.h:349-409) for an nx x ny map:
+// eight layers at frequencies 2^o, weights from 0.6 times 0.6 per layer, at
+// (x / nx, y / ny, SEED % 10000), then min-max normalised with both bounds
+// starting at 0.
+void orc_terrain_init(int nx, int ny, int32_t seed, float* out) {
+  FnlNoise noise;
+  const size_t N = (size_t)nx * ny;
+  for (size_t i = 0; i < N; ++i) out[i] = 0.0f;
+  float frequency = 1.0f, scale = 0.6f;
+  const float zc = (float)(seed % 10000);
+  for (int o = 0; o < 8; ++o) {
+    noise.frequency = frequency;
+    for (int x = 0; x < nx; ++x)
+      for (int y = 0; y < ny; ++y) {
+        const float px = (float)x / (float)nx, py = (float)y / (float)ny;
+        out[(size_t)x * ny + y] += scale * noise.get(px, py, zc);
+      }
+    frequency *= 2;
+    scale *= 0.6;
+  }
+  float lo = 0.0f, hi = 0.0f;
+  for (size_t i = 0; i < N; ++i) {
+    lo = (lo < out[i]) ? lo : out[i];
+    hi = (hi > out[i]) ? hi : out[i];
+  }
+  for (size_t i = 0; i < N; ++i) out[i] = (out[i] - lo) / (hi - lo);
 }
 
 // The integer routines the GPU's batched kernels use, for the tests.

@@ -16,6 +16,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 import subprocess
+import sys
 
 import numpy as np
 
@@ -107,6 +108,7 @@ def lib():
         L.orc_erode_batched_f32.argtypes = [P(GridF32), P(Params), C.c_uint64, C.c_uint64, C.c_int,
                                             C.c_int, P(Acc), P(C.c_int64), C.c_int]
         L.orc_value_noise.argtypes = [C.c_int, C.c_int, C.c_uint64, C.c_int, P(C.c_float)]
+        L.orc_terrain_init.argtypes = [C.c_int, C.c_int, C.c_int32, P(C.c_float)]
         L.orc_vegetation_step_f32.argtypes = [P(GridF32), P(C.c_float), P(Params), C.c_uint64, C.c_uint64]
         L.orc_erff_libm.argtypes = [C.c_float]
         L.orc_erff_libm.restype = C.c_float
@@ -141,6 +143,23 @@ def ref():
         R.ref_init(1)
         _ref = R
     return _ref
+
+
+def ref_terrain(seed):
+    """quad::map::init's heights for `seed` (the reference's int SEED) from the
+    reference build, as a (512, 512) array.  The reference builds its map once
+    per process, so each seed runs in a child process."""
+    code = ("import ctypes as C, sys, numpy as np\n"
+            "R = C.CDLL(sys.argv[1]); n = R.ref_tilesize()\n"
+            "R.ref_init.argtypes = [C.c_uint]; R.ref_init(int(sys.argv[2]) & 0xffffffff)\n"
+            "o = np.empty(n * n, np.float32)\n"
+            "R.ref_get_field(0, o.ctypes.data_as(C.POINTER(C.c_float)))\n"
+            "sys.stdout.buffer.write(o.tobytes())\n")
+    out = subprocess.run([sys.executable, "-c", code, REF_PATH, str(seed)], capture_output=True,
+                         check=True).stdout
+    a = np.frombuffer(out, np.float32)
+    n = int(round(len(a) ** 0.5))
+    return a.reshape(n, n).copy()
 
 
 def fptr(a):
@@ -203,6 +222,13 @@ class Maps:
 def value_noise(nx, ny, seed, octaves=8):
     out = np.empty((nx, ny), np.float32)
     lib().orc_value_noise(nx, ny, seed, octaves, fptr(out))
+    return out
+
+
+def terrain_init(nx, ny, seed):
+    """quad::map::init's terrain for an nx x ny map (source/cellpool.h:323-411)."""
+    out = np.empty((nx, ny), np.float32)
+    lib().orc_terrain_init(nx, ny, seed, fptr(out))
     return out
 
 

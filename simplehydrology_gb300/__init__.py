@@ -207,6 +207,11 @@ class World(_Handle):
         """Seeded fractal value-noise heights, normalised to [0, 1], on the GPU."""
         check(lib().shy_terrain_generate(self._w, 0, seed, octaves))
 
+    def init_terrain(self, seed: int):
+        """The reference's own terrain for `seed`: quad::map::init's OpenSimplex2
+        FBm layers, min-max normalised (source/cellpool.h:323-411), on the GPU."""
+        check(lib().shy_terrain_init(self._w, 0, seed))
+
     def set_erf_source(self, source: int):
         check(lib().shy_world_set_erf_source(self._w, source))
 
@@ -344,6 +349,9 @@ class Batch(_Handle):
 
     def generate(self, t, seed: int, octaves: int = 8):
         check(lib().shy_terrain_generate(self._w, t, seed, octaves))
+
+    def init_terrain(self, t, seed: int):
+        check(lib().shy_terrain_init(self._w, t, seed))
 
     def erode(self, cycles: int = 1):
         check(lib().shy_batch_erode(self._w, cycles))

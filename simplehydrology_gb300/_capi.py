@@ -130,6 +130,7 @@ SIGNATURES = {
     "shy_terrain_get_field": (C.c_int, [W, C.c_int, C.c_int, FP, C.c_size_t]),
     "shy_terrain_erode_exact": (C.c_int, [W, C.c_int, P(C.c_int32), C.c_int]),
     "shy_terrain_generate": (C.c_int, [W, C.c_int, C.c_uint64, C.c_int]),
+    "shy_terrain_init": (C.c_int, [W, C.c_int, C.c_int32]),
     "shy_vegetation_step": (C.c_int, [W, C.c_int]),
     "shy_world_set_vegetation_step": (C.c_int, [W, C.c_uint64]),
     "shy_erode_noalloc": (C.c_int, [C.c_int, C.c_int, P(Params), C.c_uint64, C.c_uint64, C.c_int, C.c_int,

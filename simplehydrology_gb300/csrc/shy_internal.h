@@ -240,6 +240,9 @@ cudaError_t launch_normals(shy_world* w, int terrain, float* out3);
 cudaError_t launch_batched_cycle(shy_world* w);
 cudaError_t launch_heights_to_fixed(shy_world* w);
 cudaError_t launch_vegetation_step(shy_world* w);
+// the reference's init terrain (source/cellpool.h:349-409) into terrain t's
+// heights; `minmax` is two device words of scratch
+cudaError_t launch_reference_terrain(shy_world* w, int terrain, int32_t seed, unsigned* minmax);
 cudaError_t launch_value_noise(shy_world* w, int terrain, unsigned long long seed, int octaves,
                                double* raw, unsigned long long* minmax);
 cudaError_t launch_gather_comp(shy_world* w, int terrain, int comp, float* out);

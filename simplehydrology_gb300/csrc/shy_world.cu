@@ -908,6 +908,19 @@ int shy_terrain_generate(shy_world* w, int t, uint64_t seed, int octaves) {
   return SHY_OK;
 }
 
+int shy_terrain_init(shy_world* w, int t, int32_t seed) {
+  int rc = check_terrain(w, t);
+  if (rc) return rc;
+  unsigned* mm = nullptr;
+  SHY_CHECK_CUDA(cudaMallocAsync((void**)&mm, 2 * sizeof(unsigned), w->stream), "allocate terrain scratch");
+  w->hq_stale = true;
+  cudaError_t e = launch_reference_terrain(w, t, seed, mm);
+  cudaFreeAsync(mm, w->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "initialise terrain");
+  SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
+  return SHY_OK;
+}
+
 int shy_vegetation_step(shy_world* w, int steps) {
   int rc = check_world(w);
   if (rc) return rc;

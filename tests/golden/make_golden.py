@@ -22,6 +22,9 @@ Drop::descend, World::cascade, quad::map::normal -- on the reference's
   ref_feed.json    the per-frame buffers on the map after those frames: the
                    mesh written by the reference's updatenode and the two
                    textures over its map accessors (SHA-256 each)
+  ref_terrain.json the reference's own terrain, World::map.init for five
+                   seeds (one child process each): SHA-256 of the 512 x 512
+                   heights and every 4099th value
 
 The input terrain is the workloads' value noise (seed 1) written over the
 reference's own map after World::map.init.  Values that go through erf (the
@@ -29,6 +32,7 @@ discharge-coupled parts after the first erosion call) are the host C
 library's erff; these fixtures were made with glibc 2.39 on x86-64.
 
 Run from the repository root:  python tests/golden/make_golden.py
+(`python tests/golden/make_golden.py terrain` rewrites ref_terrain.json only).
 """
 import hashlib
 import json
@@ -159,5 +163,29 @@ def main():
     print("wrote fixtures:", sorted(os.listdir(HERE)))
 
 
+TERRAIN_SEEDS = [1, 42, 12345, -7, 2147483647]
+
+
+def terrain():
+    po.build()
+    assert po.ref_available(), "oracle/_ref/libshyref.so was not built (needs the reference checkout)"
+    out = {}
+    for s in TERRAIN_SEEDS:
+        h = po.ref_terrain(s)
+        assert h.shape == (N, N)
+        out[str(s)] = {"height_sha": sha(h), "sample_every": 4099,
+                       "sample": [float(v) for v in h.reshape(-1)[::4099]]}
+    meta = {"generator": "tests/golden/make_golden.py terrain", "map": N,
+            "what": "World::map.init(vertexpool, cellpool, SEED) heights, x-major",
+            "machine": platform.machine()}
+    with open(os.path.join(HERE, "ref_terrain.json"), "w") as f:
+        json.dump({"meta": meta, "seeds": out}, f, indent=1)
+    print("wrote ref_terrain.json")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["terrain"]:
+        terrain()
+    else:
+        main()
+        terrain()
