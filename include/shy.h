@@ -383,6 +383,15 @@ typedef struct shy_l2_probe {
 } shy_l2_probe;
 int shy_measure_l2(int device, shy_l2_probe* out);
 
+/* Self-check of the batched kernel's fixed-point conversions on the current
+ * device: the hardware converters it uses against the library's integer
+ * restatements of (float)((double)q * 2^-32) and llrintf(v * 2^32).
+ * mismatches[0] counts floats (all with |v| < 2^31), mismatches[1] int64
+ * values (all |q| < 2^26, powers of two and their neighbours, 2^31 spread
+ * over the range) that differ; both are 0 on a conforming device.  Takes a
+ * few tens of milliseconds. */
+int shy_check_conversions(uint64_t mismatches[2]);
+
 #ifdef __cplusplus
 }
 #endif

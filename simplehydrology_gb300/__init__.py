@@ -22,7 +22,7 @@ from ._capi import (ERF_DEVICE, ERF_HOST_LIBM, FEED_KINDS, FIELD_NAMES, DropStat
                     Stats, Timing, check, default_params, lib)
 
 __all__ = ["World", "Batch", "Drop", "Params", "Stats", "Timing", "ShyError", "default_params",
-           "lib", "load", "measure_l2", "ERF_DEVICE", "ERF_HOST_LIBM", "FIELD_NAMES"]
+           "lib", "load", "measure_l2", "check_conversions", "ERF_DEVICE", "ERF_HOST_LIBM", "FIELD_NAMES"]
 
 
 def measure_l2(device: int = 0) -> dict:
@@ -30,6 +30,15 @@ def measure_l2(device: int = 0) -> dict:
     out = L2Probe()
     check(lib().shy_measure_l2(int(device), C.byref(out)))
     return out.as_dict()
+
+
+def check_conversions():
+    """(float mismatches, int64 mismatches) of the batched kernel's hardware
+    fixed-point conversions against the integer restatements; (0, 0) on a
+    conforming device."""
+    out = (C.c_uint64 * 2)()
+    check(lib().shy_check_conversions(out))
+    return int(out[0]), int(out[1])
 
 
 def _fptr(a):

@@ -137,6 +137,7 @@ SIGNATURES = {
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     P(Stats)]),
     "shy_measure_l2": (C.c_int, [C.c_int, P(L2Probe)]),
+    "shy_check_conversions": (C.c_int, [P(C.c_uint64)]),
     "shy_feed": (C.c_int, [W, C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.c_int]),
     "shy_world_save": (C.c_int, [W, C.c_char_p]),
     "shy_world_srand": (C.c_int, [W, C.c_uint32]),

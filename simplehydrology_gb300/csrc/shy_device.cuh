@@ -25,6 +25,22 @@ __device__ __forceinline__ float3 cross_scaled(float3 a, float3 b, float ms) {
   return make_float3(sa.y * sb.z - sb.y * sa.z, sa.z * sb.x - sb.z * sa.x, sa.x * sb.y - sb.x * sa.y);
 }
 
+// Fixed-point conversions on the hardware converters, with the bits of the
+// integer restatements shy_unq / shy_q32 (shy_math.h).  The converters have
+// a low throughput but a short latency, and the lock-step phases are latency
+// chains, so the batched kernel uses these; shy_check_conversions compares
+// them with the restatements over every float and 2^30 int64 values.
+//  * shy_unq_dev: the int64 -> float conversion rounds q once and the scaling
+//    by 2^-32 is exact, so for |q| <= 2^53 this is (float)((double)q * 2^-32);
+//    larger |q| (heights of 2^21 and more) take the integer restatement.
+//  * shy_q32_dev: the scaling by 2^32 is exact and the float -> int64
+//    conversion rounds half to even: llrintf(v * 2^32) for |v| < 2^31.
+__device__ __forceinline__ float shy_unq_dev(long long q) {
+  if (__builtin_expect((unsigned long long)q + (1ull << 53) > (1ull << 54), 0)) return shy_unq(q);
+  return __ll2float_rn(q) * 2.3283064365386963e-10f;
+}
+__device__ __forceinline__ long long shy_q32_dev(float v) { return __float2ll_rn(v * 4294967296.0f); }
+
 __device__ __forceinline__ bool oob(int x, int y, int nx, int ny) {
   return x < 0 || y < 0 || x >= nx || y >= ny;
 }

@@ -447,8 +447,8 @@ __device__ __forceinline__ void steep_transfers(SteepCell& q, const Terrain& T, 
   for (int k = 0; k < 8; ++k) q.u.out.dq[k] = 0;
 #pragma unroll
   for (int j = 0; j < 8; ++j)
-    if (tr[j] != 0.0f) q.u.out.dq[sk[j]] = shy_q32(tr[j]);
-  q.u.out.dc = moved ? shy_q32(hcv - h0) : 0;
+    if (tr[j] != 0.0f) q.u.out.dq[sk[j]] = shy_q32_dev(tr[j]);
+  q.u.out.dc = moved ? shy_q32_dev(hcv - h0) : 0;
 }
 
 // The changes `steep_transfers` left in a queued entry, added to the
@@ -597,11 +597,11 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       qxm = xm ? qxm : 0;
       qyp = yp ? qyp : 0;
       qym = ym ? qym : 0;
-      const float hp = shy_unq(q0);
-      const float3 n = normal5(hp, shy_unq(qxp), shy_unq(qxm), shy_unq(qyp), shy_unq(qym), xp && yp, xm && ym,
+      const float hp = shy_unq_dev(q0);
+      const float3 n = normal5(hp, shy_unq_dev(qxp), shy_unq_dev(qxm), shy_unq_dev(qyp), shy_unq_dev(qym), xp && yp, xm && ym,
                                xp && ym, xm && yp, P.map_scale);
       if ((float)ag > P.max_age || v.x < P.min_vol) {  // water.h:74-83
-        const long long dep = shy_q32(v.y);
+        const long long dep = shy_q32_dev(v.y);
         add_i64(&a.cq[c].e, dep);
         S.own[j] = dep;
         gain_q += gn;
@@ -633,9 +633,9 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       const bool out = oob(jx, jy, T.nx, T.ny);
       const long long c2 = T.cell_base + (long long)jx * T.ny + jy;
       // the tracks need nothing from the next cell: out before its loads
-      add_i64(&a.trk[c].td, shy_q32(v.x));  // water.h:115-117
-      add_i64(&a.trk[c].tmx, shy_q32(v.x * s.x));
-      add_i64(&a.trk[c].tmy, shy_q32(v.x * s.y));
+      add_i64(&a.trk[c].td, shy_q32_dev(v.x));  // water.h:115-117
+      add_i64(&a.trk[c].tmx, shy_q32_dev(v.x * s.x));
+      add_i64(&a.trk[c].tmy, shy_q32_dev(v.x * s.y));
       // the next cell's height and the drop's registration there travel
       // together; the first drop to arrive runs the cell's cascade
       int arrived_before = 1;
@@ -644,22 +644,22 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         qn = a.cq[c2].hq;
         arrived_before = atomicAdd(&a.cq[c2].cnt[par ^ 1], 1);
       }
-      const float h2 = out ? __double2float_rn((double)hp - 0.002) : shy_unq(qn);  // water.h:120-124
+      const float h2 = out ? __double2float_rn((double)hp - 0.002) : shy_unq_dev(qn);  // water.h:120-124
       float ceq = r.w * (hp - h2);  // water.h:127-128
       if (ceq < 0.0f) ceq = 0.0f;
       const float edn = ed / (float)nhere;
       const float ex = edn * (ceq - v.y);  // water.h:129-132
       v.y += ex;
-      const long long de = -shy_q32(ex);
+      const long long de = -shy_q32_dev(ex);
       add_i64(&a.cq[c].e, de);
       S.own[j] = de;
       const float s0 = v.y;  // water.h:135-136, without the FP64 unit
       v.y = shy_evap_div(v.y, &ev);
       v.x = vnext;
-      gn += shy_q32(v.y - s0);  // exact difference (Sterbenz)
+      gn += shy_q32_dev(v.y - s0);  // exact difference (Sterbenz)
       if (out) {  // water.h:139-142
         ++n_oob;
-        loss_q += shy_q32(v.y);
+        loss_q += shy_q32_dev(v.y);
         gain_q += gn;
         S.age[j] = -2;
         S.ctr[j] = -1;
@@ -722,8 +722,8 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
 #pragma unroll
       for (int k = 0; k < 8; ++k)
         sh[k] = oob(ix + nb_dx(k), iy + nb_dy(k), T.nx, T.ny) ? __int_as_float(0x7f800000)  // never used
-                                                              : shy_unq(nv[k].x + nv[k].y);
-      const float h0 = shy_unq(v0.x + v0.y);
+                                                              : shy_unq_dev(nv[k].x + nv[k].y);
+      const float h0 = shy_unq_dev(v0.x + v0.y);
       bool any = false;
 #pragma unroll
       for (int k = 0; k < 8; ++k) {

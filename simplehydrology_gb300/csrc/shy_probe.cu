@@ -147,11 +147,80 @@ int measure(int device, shy_l2_probe* out) {
   return SHY_OK;
 }
 
+// Every float with |v| < 2^31 (and no NaN or infinity): the hardware
+// float -> 32.32 conversion against the integer restatement.
+__global__ void check_q32_kernel(unsigned long long* bad) {
+  unsigned long long n = 0;
+  for (unsigned long long u = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < (1ull << 32);
+       u += (unsigned long long)gridDim.x * blockDim.x) {
+    const float v = __uint_as_float((unsigned)u);
+    if (!(fabsf(v) < 2147483648.0f)) continue;
+    n += shy_q32_dev(v) != shy_q32(v);
+  }
+  if (n) atomicAdd(bad, n);
+}
+
+// 32.32 -> float: every q with |q| < 2^26, every power of two with its
+// neighbours, and 2^30 values spread over the whole int64 range.
+__global__ void check_unq_kernel(unsigned long long* bad) {
+  unsigned long long n = 0;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  const unsigned long long tid = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  auto test = [&](long long q) { n += __float_as_uint(shy_unq_dev(q)) != __float_as_uint(shy_unq(q)); };
+  for (unsigned long long i = tid; i < (1ull << 27); i += stride) test((long long)i - (1ll << 26));
+  for (unsigned long long i = tid; i < 63 * 64; i += stride) {
+    const long long p = 1ll << (i / 64);
+    const long long d = (long long)(i % 64) - 32;
+    test(p + d);
+    test(-(p + d));
+  }
+  for (unsigned long long i = tid; i < (1ull << 30); i += stride) {
+    unsigned long long z = (i + 1) * 0x9E3779B97F4A7C15ull;  // SplitMix64 finaliser
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    test((long long)(z >> (i & 63)));  // magnitudes of every size, both signs
+    test((long long)(0ull - (z >> (i & 63))));
+  }
+  if (n) atomicAdd(bad, n);
+}
+
 }  // namespace
 
 }  // namespace shy
 
 using namespace shy;
+
+extern "C" int shy_check_conversions(uint64_t* mismatches) {
+  if (!mismatches) {
+    set_error("shy_check_conversions: null output");
+    return SHY_ERR_INVALID_ARG;
+  }
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    set_error("shy_check_conversions: no CUDA device");
+    return SHY_ERR_NO_DEVICE;
+  }
+  unsigned long long* bad = nullptr;
+  SHY_CHECK_CUDA(cudaMalloc((void**)&bad, 2 * sizeof(unsigned long long)), "allocate check counters");
+  cudaError_t e = cudaMemset(bad, 0, 2 * sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    check_q32_kernel<<<4096, 256>>>(bad);
+    check_unq_kernel<<<4096, 256>>>(bad + 1);
+    e = cudaGetLastError();
+  }
+  unsigned long long h[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  if (e != cudaSuccess) {
+    set_error("shy_check_conversions: %s", cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? SHY_ERR_OUT_OF_MEMORY : SHY_ERR_CUDA;
+  }
+  mismatches[0] = h[0];
+  mismatches[1] = h[1];
+  return SHY_OK;
+}
 
 extern "C" int shy_measure_l2(int device, shy_l2_probe* out) {
   if (!out) {
