@@ -292,7 +292,7 @@ int shy_terrain_init(shy_world* w, int terrain, int32_t seed);
  * call's counters.
  *
  * It allocates nothing: no cudaMalloc or cudaFree and no allocating library
- * routine.  Its working memory is one fixed device array of about 8 MiB
+ * routine.  Its working memory is one fixed device array of about 9 MiB
  * inside the library, sized for at most SHY_NOALLOC_MAX_CELLS cells,
  * SHY_NOALLOC_MAX_DROPS drops per cycle and max_age SHY_NOALLOC_MAX_AGE
  * (larger requests fail with SHY_ERR_INVALID_ARG), and cascade_passes must be

@@ -150,11 +150,15 @@ SHY_HD double shy_value_noise(uint64_t seed, int x, int y, int side, int octaves
   return total;
 }
 
-// ---- integer-only conversions for the batched kernels ---------------------
-// The GPU's FP64 and 64-bit conversion units are far slower than its integer
-// and FP32 units, so the batched hot loop does these three roundings with
-// integer arithmetic.  Each gives exactly the bits of the expression named;
-// oracle/emulation_check.c verifies them over every normal float.
+// ---- integer restatements of three roundings -----------------------------
+// The reference evaluates these in FP64, which the GPU runs far slower than
+// FP32 and integer arithmetic.  Each function gives exactly the bits of the
+// expression named, with integer arithmetic only; oracle/emulation_check.c
+// verifies them over every normal float.  They are the definition the host,
+// the oracle and the streaming kernels use.  The lock-step kernel converts
+// between 32.32 and float on the hardware int64 <-> float converters instead
+// (shy_unq_dev, shy_q32_dev in shy_device.cuh), which give the same bits with
+// a shorter latency.
 
 #if defined(__CUDA_ARCH__)
 #define SHY_CLZ64(x) __clzll((long long)(x))
