@@ -383,14 +383,18 @@ typedef struct shy_l2_probe {
 } shy_l2_probe;
 int shy_measure_l2(int device, shy_l2_probe* out);
 
-/* Self-check of the batched kernel's fixed-point conversions on the current
- * device: the hardware converters it uses against the library's integer
- * restatements of (float)((double)q * 2^-32) and llrintf(v * 2^32).
- * mismatches[0] counts floats (all with |v| < 2^31), mismatches[1] int64
- * values (all |q| < 2^26, powers of two and their neighbours, 2^31 spread
- * over the range) that differ; both are 0 on a conforming device.  Takes a
- * few tens of milliseconds. */
-int shy_check_conversions(uint64_t mismatches[2]);
+/* Self-check of the kernels' fast arithmetic on the current device, against
+ * the library's reference restatements:
+ *  [0] the batched kernel's float -> 32.32 conversion on the hardware
+ *      converter against llrintf(v * 2^32), over every float |v| < 2^31;
+ *  [1] its 32.32 -> float conversion against (float)((double)q * 2^-32),
+ *      over all |q| < 2^26, powers of two and their neighbours, and 2^31
+ *      values spread over the int64 range;
+ *  [2] the device kernels' float-float erf against the FP64 evaluation it
+ *      reproduces, over every float.
+ * Each count of differing inputs is 0 on a conforming device.  Takes well
+ * under a second. */
+int shy_check_conversions(uint64_t mismatches[3]);
 
 #ifdef __cplusplus
 }

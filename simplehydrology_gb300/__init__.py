@@ -33,12 +33,12 @@ def measure_l2(device: int = 0) -> dict:
 
 
 def check_conversions():
-    """(float mismatches, int64 mismatches) of the batched kernel's hardware
-    fixed-point conversions against the integer restatements; (0, 0) on a
-    conforming device."""
-    out = (C.c_uint64 * 2)()
+    """Mismatch counts of the kernels' fast arithmetic against the library's
+    restatements: (float -> 32.32, 32.32 -> float, float-float erf);
+    (0, 0, 0) on a conforming device (shy_check_conversions)."""
+    out = (C.c_uint64 * 3)()
     check(lib().shy_check_conversions(out))
-    return int(out[0]), int(out[1])
+    return int(out[0]), int(out[1]), int(out[2])
 
 
 def _fptr(a):

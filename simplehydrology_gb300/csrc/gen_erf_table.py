@@ -16,8 +16,13 @@ arithmetic:
   physicists' Hermite polynomials.
 * |x| >= 4: erf rounds to +-1 in float (erfc(3.85) < 2^-25).
 
+Each double coefficient is also written as a pair of floats (the float
+nearest it, then the float nearest the remainder), for the float-float
+evaluation of the same polynomials (shy_erff_ff in shy_math.h).
+
 Run:  python gen_erf_table.py > shy_erf_table.h
 """
+import struct
 from decimal import Decimal, getcontext
 
 getcontext().prec = 60
@@ -95,6 +100,18 @@ def fmt(d):
     return repr(float(d))
 
 
+def f32(x):
+    # round a double to the nearest float (ties to even)
+    return struct.unpack("f", struct.pack("f", x))[0]
+
+
+def fmt_pair(d):
+    c = float(d)
+    hi = f32(c)
+    lo = f32(c - hi)  # c - hi is exact in double
+    return "{" + repr(hi) + "f, " + repr(lo) + "f}"
+
+
 def main():
     out = []
     out.append("// Generated by gen_erf_table.py -- do not edit by hand.")
@@ -115,10 +132,21 @@ def main():
     out.append("// segment s covers [0.5 + 0.25 s, 0.75 + 0.25 s); erf = sum_k SEG[s][k] * u^k,")
     out.append("// u = x - (0.625 + 0.25 s)")
     out.append("SHY_ERF_TABLE_QUAL double shy_erf_seg[SHY_ERF_SEG_COUNT][SHY_ERF_SEG_DEGREE + 1] = {")
+    segs = []
     for s in range(SEG_COUNT):
         centre = SEG_START + SEG_WIDTH * s + SEG_WIDTH / 2
         co = taylor_coeffs(centre, SEG_DEGREE)
+        segs.append(co)
         out.append("  {" + ", ".join(fmt(c) for c in co) + "},")
+    out.append("};")
+    out.append("// the same coefficients as float pairs {hi, lo}, hi + lo = the double to")
+    out.append("// about 48 bits")
+    out.append("SHY_ERF_TABLE_QUAL float shy_erf_small_f[SHY_ERF_SMALL_TERMS][2] = {")
+    out.append("  " + ", ".join(fmt_pair(c) for c in small))
+    out.append("};")
+    out.append("SHY_ERF_TABLE_QUAL float shy_erf_seg_f[SHY_ERF_SEG_COUNT][SHY_ERF_SEG_DEGREE + 1][2] = {")
+    for co in segs:
+        out.append("  {" + ", ".join(fmt_pair(c) for c in co) + "},")
     out.append("};")
     print("\n".join(out))
 

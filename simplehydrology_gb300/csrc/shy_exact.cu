@@ -26,7 +26,7 @@ __global__ void rebuild_records_kernel(float4* __restrict__ rec, float* __restri
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells;
        i += (long long)gridDim.x * blockDim.x) {
     float4 r = rec[i];
-    r.w = 1.0f + P.entrainment * shy_erff(0.4f * r.z);
+    r.w = 1.0f + P.entrainment * shy_erff_ff(0.4f * r.z);
     rec[i] = r;
     const float e = P.deposition_rate * (1.0f - root[i]);
     effd[i] = e < 0.0f ? 0.0f : e;
@@ -45,7 +45,7 @@ __global__ void exact_blend_kernel(float4* __restrict__ rec, const float* __rest
     r.z = a * r.z + b * td[i];
     r.x = a * r.x + b * tmx[i];
     r.y = a * r.y + b * tmy[i];
-    r.w = 1.0f + P.entrainment * shy_erff(0.4f * r.z);
+    r.w = 1.0f + P.entrainment * shy_erff_ff(0.4f * r.z);
     rec[i] = r;
   }
 }
@@ -255,7 +255,7 @@ __global__ void pack_state_kernel(float4* __restrict__ rec, const float* __restr
     if (my) r.y = my[i];
     if (d) {
       r.z = d[i];
-      r.w = 1.0f + P.entrainment * shy_erff(0.4f * r.z);
+      r.w = 1.0f + P.entrainment * shy_erff_ff(0.4f * r.z);
     }
     rec[i] = r;
   }

@@ -31,13 +31,13 @@ __global__ void feed_kernel(int kind, const float* __restrict__ h, const float4*
       o.x = 92.0f / 255.0f;
       o.y = 133.0f / 255.0f;
       o.z = 142.0f / 255.0f;
-      o.w = shy_erff(0.4f * r.z);
+      o.w = shy_erff_ff(0.4f * r.z);
       reinterpret_cast<float4*>(out)[i] = o;
     } else if (kind == SHY_FEED_MOMENTUM_RGBA) {
       const float4 r = rec[i];
       float4 o;
-      o.x = 0.5f * (1.0f + shy_erff(r.x));
-      o.y = 0.5f * (1.0f + shy_erff(r.y));
+      o.x = 0.5f * (1.0f + shy_erff_ff(r.x));
+      o.y = 0.5f * (1.0f + shy_erff_ff(r.y));
       o.z = 0.5f;
       o.w = 1.0f;
       reinterpret_cast<float4*>(out)[i] = o;

@@ -853,7 +853,7 @@ __global__ void cycle_end_kernel(Tracks* __restrict__ trk, float4* __restrict__ 
     r.z = a * r.z + b * fd;
     r.x = a * r.x + b * fx;
     r.y = a * r.y + b * fy;
-    r.w = 1.0f + P.entrainment * shy_erff(0.4f * r.z);
+    r.w = 1.0f + P.entrainment * shy_erff_ff(0.4f * r.z);
     rec[i] = r;
     Tracks z;
     z.td = 0;

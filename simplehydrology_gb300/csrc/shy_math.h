@@ -6,6 +6,7 @@
 // -ffp-contract=off), so the host and the GPU produce the same bits.
 #pragma once
 
+#include <math.h>
 #include <stdint.h>
 
 #if defined(__CUDACC__)
@@ -174,6 +175,72 @@ static inline float shy_as_float_h(uint32_t u) { float f; memcpy(&f, &u, 4); ret
 #define SHY_AS_UINT(f) shy_as_uint_h(f)
 #define SHY_AS_FLOAT(u) shy_as_float_h(u)
 #endif
+
+// x + y = s + e exactly (Knuth's TwoSum).
+SHY_HD void shy_two_sum(float a, float b, float* s, float* e) {
+  const float t = a + b;
+  const float bb = t - a;
+  *e = (a - (t - bb)) + (b - bb);
+  *s = t;
+}
+
+// shy_erff in float arithmetic.  The polynomial shy_erf_d evaluates is
+// evaluated again in float-float arithmetic (TwoSum and the FMA-based exact
+// product; coefficients as float pairs), to about 2^-42 relative.  Rounded to
+// float, that gives shy_erff's result except within 2^-37 of a rounding
+// midpoint, where shy_erf_d itself decides; tiny arguments take shy_erf_d
+// too.  Equal to shy_erff for every float (shy_check_conversions compares
+// all 2^32 on the device); the GPU's FP64 unit is far slower than this.
+SHY_HD float shy_erff_ff(float x) {
+#if defined(__CUDA_ARCH__)
+  using namespace shy_dev_tables;
+#elif defined(__CUDACC__)
+  using namespace shy_host_tables;
+#endif
+  if (!(x == x) || x == 0.0f) return x;
+  const float ax = x < 0.0f ? -x : x;
+  if (ax >= 4.0f) return x < 0.0f ? -1.0f : 1.0f;
+  if (ax < 8.673617379884035e-19f) return shy_erff(x);  // 2^-60
+  float uh, ul;
+  const float(*c)[2];
+  int n;
+  if (ax < 0.5f) {  // x * P(x^2)
+    uh = ax * ax;
+    ul = fmaf(ax, ax, -uh);
+    c = shy_erf_small_f;
+    n = SHY_ERF_SMALL_TERMS - 1;
+  } else {  // P(x - centre) on the segment (the subtraction is exact)
+    const int sg = (int)((ax - 0.5f) * 4.0f);
+    uh = ax - (0.625f + 0.25f * (float)sg);
+    ul = 0.0f;
+    c = shy_erf_seg_f[sg];
+    n = SHY_ERF_SEG_DEGREE;
+  }
+  float ph = c[n][0], pl = c[n][1];
+  for (int k = n - 1; k >= 0; --k) {  // p = p * u + c[k]
+    const float th = ph * uh;
+    const float te = fmaf(ph, uh, -th) + (pl * uh + ph * ul);
+    float sh, se;
+    shy_two_sum(th, c[k][0], &sh, &se);
+    se = se + (te + c[k][1]);
+    ph = sh + se;
+    pl = se - (ph - sh);
+  }
+  if (ax < 0.5f) {
+    const float rh = ph * ax;
+    const float re = fmaf(ph, ax, -rh) + pl * ax;
+    ph = rh + re;
+    pl = re - (ph - rh);
+  }
+  // r = the float nearest ph + pl; e = the rest, exactly
+  float r, e;
+  shy_two_sum(ph, pl, &r, &e);
+  const uint32_t ru = SHY_AS_UINT(r);
+  float half = 0.5f * SHY_AS_FLOAT((ru & 0x7F800000u) - (23u << 23));  // half an ulp of r (r >= 2^-61)
+  if (e < 0.0f && (ru & 0x7FFFFFu) == 0u) half *= 0.5f;  // below a power of two the ulp halves
+  if ((e < 0.0f ? -e : e) > half * (1.0f - 1.220703125e-4f)) return shy_erff(x);  // within 2^-13 half-ulp
+  return x < 0.0f ? -r : r;
+}
 
 // Round x (> 0) to nearest-even after dropping its `cut` low bits (cut >= 1);
 // `sticky` says whether nonzero bits were already dropped below x.

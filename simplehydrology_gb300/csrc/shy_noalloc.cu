@@ -96,7 +96,7 @@ __global__ void noalloc_pack_kernel(NoallocScratch* s, int n, long long words, f
     c.cnt[1] = 0;
     s->cq[i] = c;
     h[i] = shy_unq(q);
-    s->rec[i] = make_float4(mx[i], my[i], d[i], 1.0f + P.entrainment * shy_erff(0.4f * d[i]));
+    s->rec[i] = make_float4(mx[i], my[i], d[i], 1.0f + P.entrainment * shy_erff_ff(0.4f * d[i]));
     s->effd[i] = c.effd;
     Tracks t;
     t.td = t.tmx = t.tmy = t.pad = 0;

@@ -43,7 +43,7 @@ struct PlantMaps {
 
 // quad::map::discharge, source/cellpool.h:439-443
 __device__ float map_discharge(const PlantMaps& M, int x, int y) {
-  return oob(x, y, M.nx, M.ny) ? 0.0f : shy_erff(0.4f * M.rec[(long long)x * M.ny + y].z);
+  return oob(x, y, M.nx, M.ny) ? 0.0f : shy_erff_ff(0.4f * M.rec[(long long)x * M.ny + y].z);
 }
 
 // Plant::root(f), source/vegetation.h:87-118, and the deposition rate of

@@ -185,6 +185,19 @@ __global__ void check_unq_kernel(unsigned long long* bad) {
   if (n) atomicAdd(bad, n);
 }
 
+// Every float: the float-float erf against the FP64 evaluation whose
+// rounding it reproduces (NaN inputs must give NaN).
+__global__ void check_erf_kernel(unsigned long long* bad) {
+  unsigned long long n = 0;
+  for (unsigned long long u = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < (1ull << 32);
+       u += (unsigned long long)gridDim.x * blockDim.x) {
+    const float v = __uint_as_float((unsigned)u);
+    const float a = shy_erff_ff(v), b = shy_erff(v);
+    n += (a == a || b == b) && __float_as_uint(a) != __float_as_uint(b);
+  }
+  if (n) atomicAdd(bad, n);
+}
+
 }  // namespace
 
 }  // namespace shy
@@ -203,14 +216,15 @@ extern "C" int shy_check_conversions(uint64_t* mismatches) {
     return SHY_ERR_NO_DEVICE;
   }
   unsigned long long* bad = nullptr;
-  SHY_CHECK_CUDA(cudaMalloc((void**)&bad, 2 * sizeof(unsigned long long)), "allocate check counters");
-  cudaError_t e = cudaMemset(bad, 0, 2 * sizeof(unsigned long long));
+  SHY_CHECK_CUDA(cudaMalloc((void**)&bad, 3 * sizeof(unsigned long long)), "allocate check counters");
+  cudaError_t e = cudaMemset(bad, 0, 3 * sizeof(unsigned long long));
   if (e == cudaSuccess) {
     check_q32_kernel<<<4096, 256>>>(bad);
     check_unq_kernel<<<4096, 256>>>(bad + 1);
+    check_erf_kernel<<<4096, 256>>>(bad + 2);
     e = cudaGetLastError();
   }
-  unsigned long long h[2] = {0, 0};
+  unsigned long long h[3] = {0, 0, 0};
   if (e == cudaSuccess) e = cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost);
   cudaFree(bad);
   if (e != cudaSuccess) {
@@ -219,6 +233,7 @@ extern "C" int shy_check_conversions(uint64_t* mismatches) {
   }
   mismatches[0] = h[0];
   mismatches[1] = h[1];
+  mismatches[2] = h[2];
   return SHY_OK;
 }
 

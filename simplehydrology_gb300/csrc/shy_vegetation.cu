@@ -49,7 +49,7 @@ __global__ void veg_step_kernel(const Terrain* __restrict__ terrains, int n_terr
     const int x = (int)(lc / T.ny), y = (int)(lc - (long long)x * T.ny);
     const float* hT = h + T.cell_base;
     auto u = [&](long long cell, unsigned what) { return shy_uniform24(T.seed, step, (unsigned long long)cell, what); };
-    auto erfd = [&](long long gi) { return shy_erff(0.4f * rec[gi].z); };
+    auto erfd = [&](long long gi) { return shy_erff_ff(0.4f * rec[gi].z); };
     auto root_add = [&](int cx, int cy, float f) {
       for (int dx = -1; dx <= 1; ++dx)
         for (int dy = -1; dy <= 1; ++dy)
