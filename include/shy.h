@@ -384,17 +384,20 @@ typedef struct shy_l2_probe {
 int shy_measure_l2(int device, shy_l2_probe* out);
 
 /* Self-check of the kernels' fast arithmetic on the current device, against
- * the library's reference restatements:
+ * the library's reference restatements (integer or FP64):
  *  [0] the batched kernel's float -> 32.32 conversion on the hardware
  *      converter against llrintf(v * 2^32), over every float |v| < 2^31;
  *  [1] its 32.32 -> float conversion against (float)((double)q * 2^-32),
  *      over all |q| < 2^26, powers of two and their neighbours, and 2^31
  *      values spread over the int64 range;
  *  [2] the device kernels' float-float erf against the FP64 evaluation it
- *      reproduces, over every float.
- * Each count of differing inputs is 0 on a conforming device.  Takes well
- * under a second. */
-int shy_check_conversions(uint64_t mismatches[3]);
+ *      reproduces, over every float;
+ *  [3] the batched kernel's float evaporation division s / (1 - evap)
+ *      against its integer restatement, over every positive float, for the
+ *      default evaporation rate.
+ * Each count of differing inputs is 0 on a conforming device.  Takes about a
+ * second. */
+int shy_check_conversions(uint64_t mismatches[4]);
 
 #ifdef __cplusplus
 }

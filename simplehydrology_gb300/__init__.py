@@ -34,11 +34,12 @@ def measure_l2(device: int = 0) -> dict:
 
 def check_conversions():
     """Mismatch counts of the kernels' fast arithmetic against the library's
-    restatements: (float -> 32.32, 32.32 -> float, float-float erf);
-    (0, 0, 0) on a conforming device (shy_check_conversions)."""
-    out = (C.c_uint64 * 3)()
+    restatements: (float -> 32.32, 32.32 -> float, float-float erf, float
+    evaporation division); (0, 0, 0, 0) on a conforming device
+    (shy_check_conversions)."""
+    out = (C.c_uint64 * 4)()
     check(lib().shy_check_conversions(out))
-    return int(out[0]), int(out[1]), int(out[2])
+    return tuple(int(v) for v in out)
 
 
 def _fptr(a):

@@ -654,7 +654,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       add_i64(&a.cq[c].e, de);
       S.own[j] = de;
       const float s0 = v.y;  // water.h:135-136, without the FP64 unit
-      v.y = shy_evap_div(v.y, &ev);
+      v.y = shy_evap_div_ff(v.y, &ev);
       v.x = vnext;
       gn += shy_q32_dev(v.y - s0);  // exact difference (Sterbenz)
       if (out) {  // water.h:139-142

@@ -306,11 +306,15 @@ typedef struct shy_evap {
   int k;
   int fast;       // 0: use the double expression
   double c;       // 1 - (double)evap
+  float ih, il;   // 1 / c as a float pair: ih + il to about 2^-48
 } shy_evap;
 
 SHY_HD shy_evap shy_evap_make(float evap) {
   shy_evap E;
   E.c = 1.0 - (double)evap;
+  const double inv = 1.0 / E.c;
+  E.ih = (float)inv;
+  E.il = (float)(inv - (double)E.ih);
   E.fast = 0;
   E.nc = E.inv = E.d = 0;
   E.k = 0;
@@ -353,6 +357,25 @@ SHY_HD float shy_evap_div(float s, const shy_evap* E) {
   const int be = ef + lead - 53;
   const uint64_t mant = x >> (lead - 23);
   return SHY_AS_FLOAT(((uint32_t)be << 23) | ((uint32_t)mant & 0x7FFFFFu));
+}
+
+// shy_evap_div in float arithmetic: s times 1 / c held as a float pair,
+// accurate to about 2^-46 relative.  Within 2^-37 of a float rounding
+// midpoint, and for s outside [2^-100, 2^100], the integer restatement
+// decides.  Equal to shy_evap_div: the bound above leaves no other input
+// undecided, and shy_check_conversions compares every positive float on the
+// device for the default evaporation rate.
+SHY_HD float shy_evap_div_ff(float s, const shy_evap* E) {
+  if (!(s >= 7.888609052210118e-31f && s <= 1.2676506002282294e30f)) return s == 0.0f ? s : shy_evap_div(s, E);
+  const float qh = s * E->ih;
+  const float ql = fmaf(s, E->ih, -qh) + s * E->il;
+  float r, e;
+  shy_two_sum(qh, ql, &r, &e);
+  const uint32_t ru = SHY_AS_UINT(r);
+  float half = 0.5f * SHY_AS_FLOAT((ru & 0x7F800000u) - (23u << 23));  // half an ulp of r
+  if (e < 0.0f && (ru & 0x7FFFFFu) == 0u) half *= 0.5f;  // below a power of two the ulp halves
+  if ((e < 0.0f ? -e : e) > half * (1.0f - 1.220703125e-4f)) return shy_evap_div(s, E);
+  return r;
 }
 
 // The C library's rand() as the reference's process draws it (spawn

@@ -198,6 +198,18 @@ __global__ void check_erf_kernel(unsigned long long* bad) {
   if (n) atomicAdd(bad, n);
 }
 
+// Every positive float: the float evaporation division against the integer
+// restatement, for the evaporation constant `E`.
+__global__ void check_evap_kernel(shy_evap E, unsigned long long* bad) {
+  unsigned long long n = 0;
+  for (unsigned long long u = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < 0x7F800000ull;
+       u += (unsigned long long)gridDim.x * blockDim.x) {
+    const float v = __uint_as_float((unsigned)u);
+    n += __float_as_uint(shy_evap_div_ff(v, &E)) != __float_as_uint(shy_evap_div(v, &E));
+  }
+  if (n) atomicAdd(bad, n);
+}
+
 }  // namespace
 
 }  // namespace shy
@@ -216,15 +228,18 @@ extern "C" int shy_check_conversions(uint64_t* mismatches) {
     return SHY_ERR_NO_DEVICE;
   }
   unsigned long long* bad = nullptr;
-  SHY_CHECK_CUDA(cudaMalloc((void**)&bad, 3 * sizeof(unsigned long long)), "allocate check counters");
-  cudaError_t e = cudaMemset(bad, 0, 3 * sizeof(unsigned long long));
+  SHY_CHECK_CUDA(cudaMalloc((void**)&bad, 4 * sizeof(unsigned long long)), "allocate check counters");
+  cudaError_t e = cudaMemset(bad, 0, 4 * sizeof(unsigned long long));
   if (e == cudaSuccess) {
+    shy_params P;
+    shy_params_default(&P);
     check_q32_kernel<<<4096, 256>>>(bad);
     check_unq_kernel<<<4096, 256>>>(bad + 1);
     check_erf_kernel<<<4096, 256>>>(bad + 2);
+    check_evap_kernel<<<4096, 256>>>(shy_evap_make(P.evap_rate), bad + 3);
     e = cudaGetLastError();
   }
-  unsigned long long h[3] = {0, 0, 0};
+  unsigned long long h[4] = {0, 0, 0, 0};
   if (e == cudaSuccess) e = cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost);
   cudaFree(bad);
   if (e != cudaSuccess) {
@@ -234,6 +249,7 @@ extern "C" int shy_check_conversions(uint64_t* mismatches) {
   mismatches[0] = h[0];
   mismatches[1] = h[1];
   mismatches[2] = h[2];
+  mismatches[3] = h[3];
   return SHY_OK;
 }
 
