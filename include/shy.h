@@ -394,9 +394,9 @@ int shy_measure_l2(int device, shy_l2_probe* out);
  *      reproduces, over every float;
  *  [3] the batched kernel's float evaporation division s / (1 - evap)
  *      against its integer restatement, over every positive float, for the
- *      default evaporation rate.
- * Each count of differing inputs is 0 on a conforming device.  Takes about a
- * second. */
+ *      default evaporation rate and the rates 0.0005, 0.01 and 0.1.
+ * Each count of differing inputs is 0 on a conforming device.  Takes about
+ * two seconds. */
 int shy_check_conversions(uint64_t mismatches[4]);
 
 #ifdef __cplusplus

@@ -364,7 +364,7 @@ SHY_HD float shy_evap_div(float s, const shy_evap* E) {
 // midpoint, and for s outside [2^-100, 2^100], the integer restatement
 // decides.  Equal to shy_evap_div: the bound above leaves no other input
 // undecided, and shy_check_conversions compares every positive float on the
-// device for the default evaporation rate.
+// device for the default evaporation rate and three others.
 SHY_HD float shy_evap_div_ff(float s, const shy_evap* E) {
   if (!(s >= 7.888609052210118e-31f && s <= 1.2676506002282294e30f)) return s == 0.0f ? s : shy_evap_div(s, E);
   const float qh = s * E->ih;

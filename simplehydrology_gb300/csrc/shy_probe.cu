@@ -236,7 +236,9 @@ extern "C" int shy_check_conversions(uint64_t* mismatches) {
     check_q32_kernel<<<4096, 256>>>(bad);
     check_unq_kernel<<<4096, 256>>>(bad + 1);
     check_erf_kernel<<<4096, 256>>>(bad + 2);
-    check_evap_kernel<<<4096, 256>>>(shy_evap_make(P.evap_rate), bad + 3);
+    // the default evaporation rate and three others
+    const float rates[4] = {P.evap_rate, 0.0005f, 0.01f, 0.1f};
+    for (float r : rates) check_evap_kernel<<<4096, 256>>>(shy_evap_make(r), bad + 3);
     e = cudaGetLastError();
   }
   unsigned long long h[4] = {0, 0, 0, 0};

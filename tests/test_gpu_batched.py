@@ -58,6 +58,24 @@ def test_relax_passes_bitwise(shy, po):
     compare_all(w.get_field, m, po, "relax")
 
 
+def test_other_evaporation_rates_bitwise(shy, po):
+    # the batched kernel's float evaporation division off the default rate
+    nx, ny = 90, 64
+    H = po.value_noise(nx, ny, 6)
+    for evap in (0.01, 0.0005):
+        p = shy.default_params()
+        p.evap_rate = evap
+        w = shy.World(nx, ny, params=p, seed=8)
+        w.set_field("height", H)
+        w.erode(900, 2)
+        pp = po.default_params()
+        pp.evap_rate = evap
+        m = po.Maps(nx, ny, height=H)
+        po.erode_batched(m, 8, 0, 900, 2, pp)
+        compare_all(w.get_field, m, po, f"evap {evap}")
+        w.close()
+
+
 def test_batch_of_terrains_matches_each_alone(shy, po):
     sizes = [(64, 96), (128, 128), (100, 37), (130, 70)]
     drops = [1536, 4096, 925, 2275]

@@ -6,7 +6,7 @@ those past 2^53 that take the restatement itself.  The device kernels' erf
 (float-float, shy_erff_ff) must give the FP64 evaluation's bits (shy_erff)
 for every one of the 2^32 floats, and the batched kernel's float evaporation
 division (shy_evap_div_ff) the integer restatement's (shy_evap_div) for every
-positive float at the default evaporation rate."""
+positive float at the default evaporation rate and three others."""
 import pytest
 
 
