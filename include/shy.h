@@ -394,10 +394,12 @@ int shy_measure_l2(int device, shy_l2_probe* out);
  *      reproduces, over every float;
  *  [3] the batched kernel's float evaporation division s / (1 - evap)
  *      against its integer restatement, over every positive float, for the
- *      default evaporation rate and the rates 0.0005, 0.01 and 0.1.
+ *      default evaporation rate and the rates 0.0005, 0.01 and 0.1;
+ *  [4] its float edge height (float)((double)h - 0.002) against the double
+ *      expression, over every float.
  * Each count of differing inputs is 0 on a conforming device.  Takes about
  * two seconds. */
-int shy_check_conversions(uint64_t mismatches[4]);
+int shy_check_conversions(uint64_t mismatches[5]);
 
 #ifdef __cplusplus
 }

@@ -35,9 +35,9 @@ def measure_l2(device: int = 0) -> dict:
 def check_conversions():
     """Mismatch counts of the kernels' fast arithmetic against the library's
     restatements: (float -> 32.32, 32.32 -> float, float-float erf, float
-    evaporation division); (0, 0, 0, 0) on a conforming device
+    evaporation division, float edge height); all 0 on a conforming device
     (shy_check_conversions)."""
-    out = (C.c_uint64 * 4)()
+    out = (C.c_uint64 * 5)()
     check(lib().shy_check_conversions(out))
     return tuple(int(v) for v in out)
 

@@ -644,7 +644,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         qn = a.cq[c2].hq;
         arrived_before = atomicAdd(&a.cq[c2].cnt[par ^ 1], 1);
       }
-      const float h2 = out ? __double2float_rn((double)hp - 0.002) : shy_unq_dev(qn);  // water.h:120-124
+      const float h2 = out ? shy_minus_0002(hp) : shy_unq_dev(qn);  // water.h:120-124
       float ceq = r.w * (hp - h2);  // water.h:127-128
       if (ceq < 0.0f) ceq = 0.0f;
       const float edn = ed / (float)nhere;

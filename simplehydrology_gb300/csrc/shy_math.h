@@ -378,6 +378,29 @@ SHY_HD float shy_evap_div_ff(float s, const shy_evap* E) {
   return r;
 }
 
+// (float)((double)h - 0.002), the height past the map's edge
+// (source/water.h:120-124), in float arithmetic: h minus 0.002 held as a
+// float pair (0x1.0624dep-9 + -0x1.a1cacp-34, within 2^-59 of the double
+// 0.002), by TwoSum, to about 2^-56 absolute.  Within 2^-37 of a float
+// rounding midpoint, for results below 2^-12 in magnitude and for |h| above
+// 2^100, the double expression decides.  Equal to the double expression for
+// every float (shy_check_conversions compares all 2^32 on the device).
+SHY_HD float shy_minus_0002(float h) {
+  if (!(h >= -1.2676506002282294e30f && h <= 1.2676506002282294e30f)) return (float)((double)h - 0.002);
+  float s, e;
+  shy_two_sum(h, -0x1.0624dep-9f, &s, &e);
+  e = e - -0x1.a1cacp-34f;
+  float r, f;
+  shy_two_sum(s, e, &r, &f);
+  const float ar = r < 0.0f ? -r : r;
+  if (!(ar >= 0x1p-12f)) return (float)((double)h - 0.002);
+  const uint32_t ru = SHY_AS_UINT(ar);
+  float half = 0.5f * SHY_AS_FLOAT((ru & 0x7F800000u) - (23u << 23));  // half an ulp of r
+  if ((ru & 0x7FFFFFu) == 0u && ((f < 0.0f) == (r > 0.0f))) half *= 0.5f;  // toward zero past a power of two
+  if ((f < 0.0f ? -f : f) > half * (1.0f - 1.220703125e-4f)) return (float)((double)h - 0.002);
+  return r;
+}
+
 // The C library's rand() as the reference's process draws it (spawn
 // positions, source/world.h:69; plant events, source/vegetation.h:67-182):
 // the GNU C library's default generator, an additive lagged-Fibonacci

@@ -198,6 +198,18 @@ __global__ void check_erf_kernel(unsigned long long* bad) {
   if (n) atomicAdd(bad, n);
 }
 
+// Every float: the float edge height h - 0.002 against the double expression.
+__global__ void check_edge_kernel(unsigned long long* bad) {
+  unsigned long long n = 0;
+  for (unsigned long long u = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < (1ull << 32);
+       u += (unsigned long long)gridDim.x * blockDim.x) {
+    const float v = __uint_as_float((unsigned)u);
+    const float a = shy_minus_0002(v), b = (float)((double)v - 0.002);
+    n += (a == a || b == b) && __float_as_uint(a) != __float_as_uint(b);
+  }
+  if (n) atomicAdd(bad, n);
+}
+
 // Every positive float: the float evaporation division against the integer
 // restatement, for the evaporation constant `E`.
 __global__ void check_evap_kernel(shy_evap E, unsigned long long* bad) {
@@ -228,8 +240,8 @@ extern "C" int shy_check_conversions(uint64_t* mismatches) {
     return SHY_ERR_NO_DEVICE;
   }
   unsigned long long* bad = nullptr;
-  SHY_CHECK_CUDA(cudaMalloc((void**)&bad, 4 * sizeof(unsigned long long)), "allocate check counters");
-  cudaError_t e = cudaMemset(bad, 0, 4 * sizeof(unsigned long long));
+  SHY_CHECK_CUDA(cudaMalloc((void**)&bad, 5 * sizeof(unsigned long long)), "allocate check counters");
+  cudaError_t e = cudaMemset(bad, 0, 5 * sizeof(unsigned long long));
   if (e == cudaSuccess) {
     shy_params P;
     shy_params_default(&P);
@@ -239,9 +251,10 @@ extern "C" int shy_check_conversions(uint64_t* mismatches) {
     // the default evaporation rate and three others
     const float rates[4] = {P.evap_rate, 0.0005f, 0.01f, 0.1f};
     for (float r : rates) check_evap_kernel<<<4096, 256>>>(shy_evap_make(r), bad + 3);
+    check_edge_kernel<<<4096, 256>>>(bad + 4);
     e = cudaGetLastError();
   }
-  unsigned long long h[4] = {0, 0, 0, 0};
+  unsigned long long h[5] = {0, 0, 0, 0, 0};
   if (e == cudaSuccess) e = cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost);
   cudaFree(bad);
   if (e != cudaSuccess) {
@@ -252,6 +265,7 @@ extern "C" int shy_check_conversions(uint64_t* mismatches) {
   mismatches[1] = h[1];
   mismatches[2] = h[2];
   mismatches[3] = h[3];
+  mismatches[4] = h[4];
   return SHY_OK;
 }
 

@@ -6,13 +6,14 @@ those past 2^53 that take the restatement itself.  The device kernels' erf
 (float-float, shy_erff_ff) must give the FP64 evaluation's bits (shy_erff)
 for every one of the 2^32 floats, and the batched kernel's float evaporation
 division (shy_evap_div_ff) the integer restatement's (shy_evap_div) for every
-positive float at the default evaporation rate and three others."""
+positive float at the default evaporation rate and three others; its edge
+height (shy_minus_0002) the double expression's for every float."""
 import pytest
 
 
 @pytest.mark.gpu
 def test_hardware_conversions_match_integer_restatements(shy):
-    assert shy.check_conversions() == (0, 0, 0, 0)
+    assert shy.check_conversions() == (0, 0, 0, 0, 0)
 
 
 def test_check_conversions_rejects_null(shy):
