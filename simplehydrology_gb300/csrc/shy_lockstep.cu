@@ -40,6 +40,11 @@
 // Integer sums make every result independent of thread timing: the same
 // inputs give the same bits on every run, and oracle/hydro_oracle.cpp
 // (Lockstep) restates the schedule on the CPU.
+// Each phase is a latency chain, so the kernel keeps its arithmetic short:
+// fixed point <-> float on the hardware converters (shy_unq_dev,
+// shy_q32_dev) and the reference's FP64 roundings in float-float
+// (shy_evap_div_ff, shy_minus_0002), each with the bits of the library's
+// restatement (checked on the device by shy_check_conversions).
 //
 // The end-of-cycle kernel converts the tracks to float, applies the lrate
 // blend (source/world.h:81-86) and rebuilds the per-cell records.
