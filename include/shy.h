@@ -392,10 +392,11 @@ int shy_measure_l2(int device, shy_l2_probe* out);
  *      values spread over the int64 range;
  *  [2] the device kernels' float-float erf against the FP64 evaluation it
  *      reproduces, over every float;
- *  [3] the batched kernel's float evaporation division s / (1 - evap)
- *      against its integer restatement, over every positive float, for the
- *      default evaporation rate and the rates 0.0005, 0.01 and 0.1;
- *  [4] its float edge height (float)((double)h - 0.002) against the double
+ *  [3] the float evaporation roundings (float)((double)s / (1 - evap)) and
+ *      (float)((double)v * (1 - evap)) against the integer restatement and
+ *      the double expression, over every positive float, for the default
+ *      evaporation rate and the rates 0.0005, 0.01 and 0.1;
+ *  [4] the float edge height (float)((double)h - 0.002) against the double
  *      expression, over every float.
  * Each count of differing inputs is 0 on a conforming device.  Takes about
  * two seconds. */

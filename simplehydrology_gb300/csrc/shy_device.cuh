@@ -86,14 +86,6 @@ __device__ __forceinline__ int nb_dy(int k) {
   return (k == 0 || k == 3 || k == 5) ? -1 : ((k == 1 || k == 6) ? 0 : 1);
 }
 
-// Sediment and volume evaporation, source/water.h:135-136, in double as the
-// reference evaluates them.
-__device__ __forceinline__ float evap_div(float s, float evap) {
-  return __double2float_rn((double)s / (1.0 - (double)evap));
-}
-__device__ __forceinline__ float evap_mul(float v, float evap) {
-  return __double2float_rn((double)v * (1.0 - (double)evap));
-}
 
 // ---- exact (sequential, live) model ------------------------------------------
 
@@ -142,7 +134,7 @@ __device__ __forceinline__ void cascade_live(float* h, int nx, int ny, float px,
     const float diff = *hc - sh[i];
     if (diff == 0.0f) continue;
     float excess;
-    if ((double)sh[i] > 0.1)
+    if (sh[i] >= 0.1f)  // (double)h > 0.1: no float lies between 0.1 and 0.1f
       excess = fabsf(diff) - sd[i] * P.max_diff;
     else
       excess = fabsf(diff);
@@ -165,7 +157,7 @@ __device__ __forceinline__ bool descend_live(float* h, const float4* rec, const 
                                              float* td, float* tmx, float* tmy, int nx, int ny,
                                              DropS& d, const shy_params& P, double& gain,
                                              double& loss, unsigned long long& steps,
-                                             unsigned long long& oobs) {
+                                             unsigned long long& oobs, const shy_evap& E) {
   const int ix = (int)d.px, iy = (int)d.py;
   if (oob(ix, iy, nx, ny)) return false;
   const long long c = (long long)ix * ny + iy;
@@ -206,7 +198,7 @@ __device__ __forceinline__ bool descend_live(float* h, const float4* rec, const 
   const bool out = oob(jx, jy, nx, ny);
   float h2;
   if (out)
-    h2 = __double2float_rn((double)h[c] - 0.002);
+    h2 = shy_minus_0002(h[c]);  // (float)((double)h - 0.002)
   else
     h2 = h[(long long)jx * ny + jy];
   float ceq = r.w * (h[c] - h2);
@@ -215,8 +207,9 @@ __device__ __forceinline__ bool descend_live(float* h, const float4* rec, const 
   d.sed += ed * cdiff;
   h[c] -= ed * cdiff;
   const float s0 = d.sed;
-  d.sed = evap_div(d.sed, P.evap_rate);
-  d.vol = evap_mul(d.vol, P.evap_rate);
+  // water.h:135-136, the reference's double roundings in float arithmetic
+  d.sed = shy_evap_div_ff(d.sed, &E);
+  d.vol = shy_evap_mul_ff(d.vol, &E);
   gain += (double)d.sed - (double)s0;
   if (out) {
     d.vol = 0.0f;

@@ -54,17 +54,19 @@ __global__ void exact_erode_kernel(Terrain T, float* h, const float4* rec, const
                                    float* td, float* tmx, float* tmy, const int2* spawns, int n,
                                    shy_params P, DevStats* st) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const shy_evap E = shy_evap_make(P.evap_rate);  // water.h:135-136 constants
   double gain = 0.0, loss = 0.0;
   unsigned long long steps = 0, oobs = 0, drops = 0, skipped = 0;
   for (int i = 0; i < n; ++i) {
     const int2 s = spawns[i];
-    if (oob(s.x, s.y, T.nx, T.ny) || (double)h[(long long)s.x * T.ny + s.y] < 0.1) {
+    // (double)h < 0.1: no float lies between 0.1 and 0.1f
+    if (oob(s.x, s.y, T.nx, T.ny) || h[(long long)s.x * T.ny + s.y] < 0.1f) {
       ++skipped;  // source/world.h:71
       continue;
     }
     ++drops;
     DropS d = {0, (float)s.x, (float)s.y, 0.0f, 0.0f, 1.0f, 0.0f};
-    while (descend_live(h, rec, effd, td, tmx, tmy, T.nx, T.ny, d, P, gain, loss, steps, oobs)) {
+    while (descend_live(h, rec, effd, td, tmx, tmy, T.nx, T.ny, d, P, gain, loss, steps, oobs, E)) {
     }
   }
   st->drops += drops;
@@ -79,11 +81,12 @@ __global__ void drop_descend_kernel(Terrain T, float* h, const float4* rec, cons
                                     float* td, float* tmx, float* tmy, shy_drop* drop, int* more,
                                     shy_params P, DevStats* st) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const shy_evap E = shy_evap_make(P.evap_rate);  // water.h:135-136 constants
   DropS d = {drop->age, drop->pos[0], drop->pos[1], drop->speed[0], drop->speed[1], drop->volume,
              drop->sediment};
   double gain = 0.0, loss = 0.0;
   unsigned long long steps = 0, oobs = 0;
-  const bool m = descend_live(h, rec, effd, td, tmx, tmy, T.nx, T.ny, d, P, gain, loss, steps, oobs);
+  const bool m = descend_live(h, rec, effd, td, tmx, tmy, T.nx, T.ny, d, P, gain, loss, steps, oobs, E);
   drop->age = d.age;
   drop->pos[0] = d.px;
   drop->pos[1] = d.py;
@@ -102,12 +105,13 @@ __global__ void drop_run_kernel(Terrain T, float* h, const float4* rec, const fl
                                 float* td, float* tmx, float* tmy, float x, float y, float* trace,
                                 int max_records, int* n_out, shy_params P, DevStats* st) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const shy_evap E = shy_evap_make(P.evap_rate);  // water.h:135-136 constants
   DropS d = {0, x, y, 0.0f, 0.0f, 1.0f, 0.0f};
   double gain = 0.0, loss = 0.0;
   unsigned long long steps = 0, oobs = 0;
   int n = 0;
   for (;;) {
-    const bool m = descend_live(h, rec, effd, td, tmx, tmy, T.nx, T.ny, d, P, gain, loss, steps, oobs);
+    const bool m = descend_live(h, rec, effd, td, tmx, tmy, T.nx, T.ny, d, P, gain, loss, steps, oobs, E);
     if (n < max_records) {
       float* r = trace + 8 * (long long)n;
       r[0] = m ? 1.0f : 0.0f;

@@ -307,6 +307,7 @@ typedef struct shy_evap {
   int fast;       // 0: use the double expression
   double c;       // 1 - (double)evap
   float ih, il;   // 1 / c as a float pair: ih + il to about 2^-48
+  float ch, cl;   // c as a float pair
 } shy_evap;
 
 SHY_HD shy_evap shy_evap_make(float evap) {
@@ -315,6 +316,8 @@ SHY_HD shy_evap shy_evap_make(float evap) {
   const double inv = 1.0 / E.c;
   E.ih = (float)inv;
   E.il = (float)(inv - (double)E.ih);
+  E.ch = (float)E.c;
+  E.cl = (float)(E.c - (double)E.ch);
   E.fast = 0;
   E.nc = E.inv = E.d = 0;
   E.k = 0;
@@ -375,6 +378,25 @@ SHY_HD float shy_evap_div_ff(float s, const shy_evap* E) {
   float half = 0.5f * SHY_AS_FLOAT((ru & 0x7F800000u) - (23u << 23));  // half an ulp of r
   if (e < 0.0f && (ru & 0x7FFFFFu) == 0u) half *= 0.5f;  // below a power of two the ulp halves
   if ((e < 0.0f ? -e : e) > half * (1.0f - 1.220703125e-4f)) return shy_evap_div(s, E);
+  return r;
+}
+
+// (float)((double)v * (1 - (double)evap)) of the reference's volume
+// evaporation (source/water.h:136), in float arithmetic: v times c held as a
+// float pair, like shy_evap_div_ff, with the double expression near rounding
+// midpoints and for v outside [2^-100, 2^100].  Equal to the double
+// expression (shy_check_conversions compares every positive float at four
+// evaporation rates).
+SHY_HD float shy_evap_mul_ff(float v, const shy_evap* E) {
+  if (!(v >= 7.888609052210118e-31f && v <= 1.2676506002282294e30f)) return (float)((double)v * E->c);
+  const float ph = v * E->ch;
+  const float pl = fmaf(v, E->ch, -ph) + v * E->cl;
+  float r, e;
+  shy_two_sum(ph, pl, &r, &e);
+  const uint32_t ru = SHY_AS_UINT(r);
+  float half = 0.5f * SHY_AS_FLOAT((ru & 0x7F800000u) - (23u << 23));  // half an ulp of r
+  if (e < 0.0f && (ru & 0x7FFFFFu) == 0u) half *= 0.5f;  // below a power of two the ulp halves
+  if ((e < 0.0f ? -e : e) > half * (1.0f - 1.220703125e-4f)) return (float)((double)v * E->c);
   return r;
 }
 

@@ -211,13 +211,15 @@ __global__ void check_edge_kernel(unsigned long long* bad) {
 }
 
 // Every positive float: the float evaporation division against the integer
-// restatement, for the evaporation constant `E`.
+// restatement, and the float volume evaporation against the double
+// expression, for the evaporation constant `E`.
 __global__ void check_evap_kernel(shy_evap E, unsigned long long* bad) {
   unsigned long long n = 0;
   for (unsigned long long u = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < 0x7F800000ull;
        u += (unsigned long long)gridDim.x * blockDim.x) {
     const float v = __uint_as_float((unsigned)u);
     n += __float_as_uint(shy_evap_div_ff(v, &E)) != __float_as_uint(shy_evap_div(v, &E));
+    n += __float_as_uint(shy_evap_mul_ff(v, &E)) != __float_as_uint((float)((double)v * E.c));
   }
   if (n) atomicAdd(bad, n);
 }

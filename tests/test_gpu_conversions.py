@@ -6,8 +6,9 @@ those past 2^53 that take the restatement itself.  The device kernels' erf
 (float-float, shy_erff_ff) must give the FP64 evaluation's bits (shy_erff)
 for every one of the 2^32 floats, and the batched kernel's float evaporation
 division (shy_evap_div_ff) the integer restatement's (shy_evap_div) for every
-positive float at the default evaporation rate and three others; its edge
-height (shy_minus_0002) the double expression's for every float."""
+positive float at the default evaporation rate and three others, as must the
+exact mode's volume evaporation (shy_evap_mul_ff); the edge height
+(shy_minus_0002) must give the double expression's for every float."""
 import pytest
 
 
