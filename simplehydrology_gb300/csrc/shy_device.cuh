@@ -129,9 +129,14 @@ __device__ __forceinline__ void cascade_live(float* h, int nx, int ny, float px,
     sh[j] = vh;
     sd[j] = vd;
   }
+  // The centre is never one of its neighbours, so its live height stays in a
+  // register through the loop (written back once) instead of a global-memory
+  // read after every transfer.
   float* hc = h + (long long)ix * ny + iy;
+  float hcv = *hc;
+  bool moved = false;
   for (int i = 0; i < num; ++i) {
-    const float diff = *hc - sh[i];
+    const float diff = hcv - sh[i];
     if (diff == 0.0f) continue;
     float excess;
     if (sh[i] >= 0.1f)  // (double)h > 0.1: no float lies between 0.1 and 0.1f
@@ -142,13 +147,15 @@ __device__ __forceinline__ void cascade_live(float* h, int nx, int ny, float px,
     const float transfer = P.settling * excess / 2.0f;
     float* hn = h + (long long)sxs[i] * ny + sys_[i];
     if (diff > 0.0f) {
-      *hc -= transfer;
+      hcv -= transfer;
       *hn += transfer;
     } else {
-      *hc += transfer;
+      hcv += transfer;
       *hn -= transfer;
     }
+    moved = true;
   }
+  if (moved) *hc = hcv;
 }
 
 // Drop::descend (source/water.h:58-156) on live maps.  `rec` holds the
