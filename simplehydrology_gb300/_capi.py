@@ -1,4 +1,4 @@
-"""ctypes declarations of the C ABI in include/shy.h.
+"""ctypes declarations of the C ABI in include/shy.h and include/shy_surrogate.h.
 
 The library is loaded from this package directory (built in place by
 simplehydrology_gb300/build.py).  There is no fallback: if libshy.so is
@@ -87,6 +87,21 @@ class ShyError(RuntimeError):
         self.code = code
 
 
+class SgConvDesc(C.Structure):
+    _fields_ = [("batch", C.c_int32), ("height", C.c_int32), ("width", C.c_int32),
+                ("cin", C.c_int32), ("cout", C.c_int32), ("ksize", C.c_int32)]
+
+
+class SgAdamw(C.Structure):
+    _fields_ = [("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
+                ("weight_decay", C.c_float), ("bc1", C.c_float), ("bc2", C.c_float)]
+
+
+class SgNorm(C.Structure):
+    _fields_ = [("height_mean", C.c_float), ("height_scale", C.c_float), ("slope_scale", C.c_float),
+                ("out_mean", C.c_float * 3), ("out_scale", C.c_float * 3)]
+
+
 W = C.c_void_p
 P = C.POINTER
 FP = P(C.c_float)
@@ -146,6 +161,25 @@ SIGNATURES = {
     "shy_vegetation_grow": (C.c_int, [W]),
     "shy_plants": (C.c_int, [W, FP, C.c_int, P(C.c_int)]),
     "shy_world_load": (C.c_int, [C.c_char_p, P(W)]),
+    # include/shy_surrogate.h: device pointers and a stream handle
+    "shy_sg_conv_forward": (C.c_int, [P(SgConvDesc), W, C.c_int32, W, W, W, C.c_int32, C.c_int32, W,
+                                      C.c_int32, C.c_int32, C.c_int32, W]),
+    "shy_sg_conv_wgrad": (C.c_int, [P(SgConvDesc), W, C.c_int32, W, C.c_int32, W, W]),
+    "shy_sg_bias_grad": (C.c_int, [C.c_int64, C.c_int32, W, C.c_int32, W, W]),
+    "shy_sg_gelu_backward": (C.c_int, [C.c_int64, C.c_int32, W, C.c_int32, C.c_int32, W, C.c_int32, C.c_int32,
+                                       W, W]),
+    "shy_sg_pool_forward": (C.c_int, [C.c_int32] * 4 + [W, C.c_int32, C.c_int32, W, C.c_int32, C.c_int32, W]),
+    "shy_sg_pool_backward": (C.c_int, [C.c_int32] * 4 + [W, C.c_int32, C.c_int32, W, C.c_int32, C.c_int32, W]),
+    "shy_sg_upsample_forward": (C.c_int, [C.c_int32] * 4 + [W, C.c_int32, C.c_int32, W, C.c_int32, C.c_int32,
+                                                            W]),
+    "shy_sg_upsample_backward": (C.c_int, [C.c_int32] * 4 + [W, C.c_int32, C.c_int32, W, C.c_int32, C.c_int32,
+                                                             W]),
+    "shy_sg_weight_prep": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, W, W, W, W]),
+    "shy_sg_adamw": (C.c_int, [C.c_int64, W, W, W, W, P(SgAdamw), W]),
+    "shy_sg_features": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, W, P(SgNorm), W, W]),
+    "shy_sg_loss": (C.c_int, [C.c_int64, W, C.c_int32, W, FP, W, W, W]),
+    "shy_sg_decode": (C.c_int, [C.c_int64, W, C.c_int32, P(SgNorm), W, W, W, W]),
+    "shy_sg_status": (C.c_int, []),
 }
 
 _lib = None

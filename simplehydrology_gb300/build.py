@@ -47,7 +47,7 @@ def sources():
 
 def headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    hs.append(os.path.join(INCLUDE, "shy.h"))
+    hs += [os.path.join(INCLUDE, "shy.h"), os.path.join(INCLUDE, "shy_surrogate.h")]
     return sorted(hs)
 
 

@@ -1,0 +1,972 @@
+// shy_surrogate.cu -- device side of the learned warm-start surrogate: the
+// convolutions of a small U-Net as BF16 implicit GEMMs on the tensor cores
+// (tcgen05.mma, FP32 accumulators in tensor memory), their weight and input
+// gradients, and the elementwise pieces of training and inference.
+//
+// Convolution forward (conv_fwd_kernel).  One CTA of 128 threads computes a
+// tile of M = 128 output pixels (consecutive in (b, y, x) order) by N output
+// channels (16..128).  K = taps x cin is walked one tap and one channel chunk
+// (kc = 16, 32 or 64) at a time.  For each chunk the CTA stages A (the input
+// pixels shifted by the tap, zero outside the image) and B (weights
+// [cout][tap][cin]) in shared memory, in the no-swizzle K-major core-matrix
+// layout: a core matrix is 8 rows x 16 bytes stored as 128 contiguous bytes;
+// core matrices adjacent along K are 128 B apart (the descriptor's leading
+// byte offset) and 8-row groups kc * 16 B apart (its stride byte offset).
+// Stages are double-buffered: thread 0 issues kc / 16 MMAs of K = 16 on a
+// stage and commits them to the stage's mbarrier, and the stage is filled
+// again, two chunks later, once that barrier has completed.  So the loads of
+// one chunk overlap the MMAs of the previous one.  The epilogue reads the
+// accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31, the tile's
+// pixels 32w..32w+31), adds the bias and writes f32 and/or bf16 GELU output.
+//
+// Input gradient: the same kernel on the output gradient, with the weights
+// rotated by 180 degrees and transposed (shy_sg_weight_prep).
+//
+// Weight gradient (conv_wgrad_kernel): a GEMM with M = 128 rows of
+// (tap, cin), N = a cout tile and K = pixels in chunks of 64.  Both operands
+// are K-major in shared memory but pixel-major in HBM, so the threads stage
+// them transposed (a 16-byte load of 8 channels, 8 two-byte stores).  The
+// pixel range is split over CTAs; each adds its partial sums to the f32
+// weight gradient with atomics.
+//
+// Every wait on an mbarrier is bounded (2 s); a CTA that gives up records
+// SHY_ERR_TIMEOUT, skips its epilogue and still frees its tensor memory.
+#include <cuda_bf16.h>
+
+#include "../../include/shy_surrogate.h"
+#include "shy_internal.h"
+
+namespace shy {
+
+namespace {
+
+constexpr int kTileM = 128;     // MMA M: pixels (forward) or weight rows (wgrad)
+constexpr int kThreads = 128;   // one warpgroup: warp w reads TMEM lanes 32w..32w+31
+constexpr int kWgradK = 64;     // pixels per weight-gradient chunk
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;
+constexpr int kSmemPerSm = 233472;  // shared memory per SM (228 KiB)
+constexpr int kSmemReservedPerCta = 1024;
+
+__device__ int g_sg_status;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits until the phase of `bar` with parity `parity` has completed; gives up
+// after kWaitLimitNs.
+__device__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = now_ns();
+  while (!mbar_try(bar, parity))
+    if (now_ns() - t0 > kWaitLimitNs) return false;
+  return true;
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// Makes this thread's shared-memory stores visible to the tensor cores.
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Warp-wide: allocate `cols` TMEM columns (a power of two >= 32); the base
+// address lands in *slot.
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t cols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(slot)),
+               "r"(cols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_free(uint32_t base, uint32_t cols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(base), "r"(cols)
+               : "memory");
+}
+
+// Shared-memory matrix descriptor, no swizzle, K-major.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) |
+         ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: F32 accumulator (bits 4-5 = 1), BF16
+// A and B (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at
+// bit 24, M = 128.
+__host__ __device__ constexpr uint32_t idesc_bf16_m128(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(kTileM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Arrives once on `bar` when every MMA this thread issued so far is done.
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+// Warp-wide: 8 consecutive f32 columns of this warp's 32 TMEM lanes (one
+// lane per thread); the wait is in the same statement so that no use of
+// the registers can be scheduled before the load has landed.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float v[8]) {
+  uint32_t r0, r1, r2, r3, r4, r5, r6, r7;
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3), "=r"(r4), "=r"(r5), "=r"(r6), "=r"(r7)
+      : "r"(taddr)
+      : "memory");
+  v[0] = __uint_as_float(r0);
+  v[1] = __uint_as_float(r1);
+  v[2] = __uint_as_float(r2);
+  v[3] = __uint_as_float(r3);
+  v[4] = __uint_as_float(r4);
+  v[5] = __uint_as_float(r5);
+  v[6] = __uint_as_float(r6);
+  v[7] = __uint_as_float(r7);
+}
+
+__device__ __forceinline__ float gelu(float z) {
+  return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f));
+}
+__device__ __forceinline__ float gelu_grad(float z) {
+  const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * z * z);
+  return cdf + z * pdf;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
+
+struct ConvFwd {
+  const __nv_bfloat16* x;
+  const __nv_bfloat16* w;
+  const float* bias;
+  float* z;
+  __nv_bfloat16* a;
+  int batch, h, w_, cin, cout, ks;
+  int xs, zs, zo, as, ao, act;
+  int ntile, kc, tmem_cols;
+};
+
+__global__ void __launch_bounds__(kThreads) conv_fwd_kernel(const ConvFwd p) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ uint64_t bars[3];
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const long long hw = (long long)p.h * p.w_;
+  const long long npix = (long long)p.batch * hw;
+  const long long q = (long long)blockIdx.x * kTileM + tid;  // this thread's output pixel
+  const bool valid = q < npix;
+  int qb = 0, qy = 0, qx = 0;
+  if (valid) {
+    qb = (int)(q / hw);
+    const long long r = q - (long long)qb * hw;
+    qy = (int)(r / p.w_);
+    qx = (int)(r - (long long)qy * p.w_);
+  }
+  const int n0 = blockIdx.y * p.ntile;
+  const uint32_t sbo = (uint32_t)p.kc * 16;
+  const uint32_t a_bytes = (uint32_t)kTileM * p.kc * 2, b_bytes = (uint32_t)p.ntile * p.kc * 2;
+  const uint32_t stage_bytes = a_bytes + b_bytes;
+
+  if (warp == 0) tmem_alloc(&tmem_slot, p.tmem_cols);
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_init(&bars[2], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  const int taps = p.ks * p.ks, half = p.ks >> 1;
+  const int nchunk = p.cin / p.kc;
+  const int iters = taps * nchunk;
+  const int vecs = p.kc >> 3;
+  const long long wrow = (long long)taps * p.cin;
+  const uint32_t idesc = idesc_bf16_m128(p.ntile);
+  bool failed = false;
+  for (int it = 0; it < iters; ++it) {
+    const int s = it & 1;
+    uint8_t* sa = smem + s * stage_bytes;
+    uint8_t* sb = sa + a_bytes;
+    int fail = 0;
+    if (it >= 2 && !mbar_wait(&bars[s], (uint32_t)((it >> 1) - 1) & 1u)) fail = 1;
+    const int tap = it / nchunk, c0 = (it - tap * nchunk) * p.kc;
+    const int dy = tap / p.ks - half, dx = tap % p.ks - half;
+    {
+      const int yy = qy + dy, xx = qx + dx;
+      const bool in = valid && yy >= 0 && yy < p.h && xx >= 0 && xx < p.w_;
+      const uint4* src =
+          reinterpret_cast<const uint4*>(p.x + (((long long)qb * p.h + yy) * p.w_ + xx) * p.xs + c0);
+      uint8_t* dst = sa + (tid >> 3) * sbo + (tid & 7) * 16;
+      for (int j = 0; j < vecs; ++j) {
+        const uint4 v = in ? __ldg(src + j) : make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(dst + j * 128) = v;
+      }
+    }
+    if (tid < p.ntile) {
+      const uint4* src =
+          reinterpret_cast<const uint4*>(p.w + (long long)(n0 + tid) * wrow + (long long)tap * p.cin + c0);
+      uint8_t* dst = sb + (tid >> 3) * sbo + (tid & 7) * 16;
+      for (int j = 0; j < vecs; ++j) *reinterpret_cast<uint4*>(dst + j * 128) = __ldg(src + j);
+    }
+    fence_async_smem();
+    if (__syncthreads_or(fail)) {
+      failed = true;
+      break;
+    }
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+      for (int kk = 0; kk < (p.kc >> 4); ++kk)
+        mma_bf16(tmem, smem_desc(a0 + kk * 256, 128, sbo), smem_desc(b0 + kk * 256, 128, sbo), idesc,
+                 (it | kk) != 0);
+      mma_commit(&bars[s]);
+    }
+  }
+  if (tid == 0) mma_commit(&bars[2]);
+  const bool done = mbar_wait(&bars[2], 0);
+  const bool ok = __syncthreads_and(done && !failed) != 0;
+  if (ok) {
+    tc_fence_after();
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int nc = 0; nc < p.ntile; nc += 8) {
+      float v[8];
+      tmem_ld8(lane_base + (uint32_t)nc, v);
+      if (!valid) continue;
+      const int n = n0 + nc;
+      if (p.bias)
+        for (int j = 0; j < 8; ++j) v[j] += __ldg(p.bias + n + j);
+      if (p.z) {
+        float4* zp = reinterpret_cast<float4*>(p.z + q * p.zs + p.zo + n);
+        zp[0] = make_float4(v[0], v[1], v[2], v[3]);
+        zp[1] = make_float4(v[4], v[5], v[6], v[7]);
+      }
+      if (p.a) {
+        if (p.act == SHY_SG_ACT_GELU)
+          for (int j = 0; j < 8; ++j) v[j] = gelu(v[j]);
+        uint4 o;
+        o.x = pack_bf16(v[0], v[1]);
+        o.y = pack_bf16(v[2], v[3]);
+        o.z = pack_bf16(v[4], v[5]);
+        o.w = pack_bf16(v[6], v[7]);
+        *reinterpret_cast<uint4*>(p.a + q * p.as + p.ao + n) = o;
+      }
+    }
+  } else if (tid == 0) {
+    atomicCAS(&g_sg_status, 0, SHY_ERR_TIMEOUT);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_free(tmem, p.tmem_cols);
+  }
+}
+
+struct ConvWgrad {
+  const __nv_bfloat16* x;
+  const __nv_bfloat16* dz;
+  float* dw;
+  int batch, h, w_, cin, cout, ks;
+  int xs, dzs;
+  int ntile, tmem_cols;
+  long long chunks_per_split;
+};
+
+// Stores the 8 bf16 of `v` down 8 consecutive rows of a K-major core-matrix
+// group: row e at byte e * 16 from `dst`.
+__device__ __forceinline__ void scatter8(uint8_t* dst, const uint4 v) {
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    *reinterpret_cast<uint16_t*>(dst + (2 * e) * 16) = (uint16_t)(w[e] & 0xFFFFu);
+    *reinterpret_cast<uint16_t*>(dst + (2 * e + 1) * 16) = (uint16_t)(w[e] >> 16);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) conv_wgrad_kernel(const ConvWgrad p) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ uint64_t bars[3];
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const long long hw = (long long)p.h * p.w_;
+  const long long npix = (long long)p.batch * hw;
+  const int taps = p.ks * p.ks, half = p.ks >> 1;
+  const int rows = taps * p.cin;  // weight rows (tap, cin)
+  const int m0 = blockIdx.x * kTileM;
+  const int n0 = blockIdx.y * p.ntile;
+  const long long nchunks = (npix + kWgradK - 1) / kWgradK;
+  const long long c_begin = (long long)blockIdx.z * p.chunks_per_split;
+  const long long c_end = min(c_begin + p.chunks_per_split, nchunks);
+  const int iters = (int)max(0ll, c_end - c_begin);
+  const uint32_t sbo = (uint32_t)kWgradK * 16;
+  const uint32_t a_bytes = (uint32_t)kTileM * kWgradK * 2, b_bytes = (uint32_t)p.ntile * kWgradK * 2;
+  const uint32_t stage_bytes = a_bytes + b_bytes;
+
+  if (warp == 0) tmem_alloc(&tmem_slot, p.tmem_cols);
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_init(&bars[2], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = idesc_bf16_m128(p.ntile);
+  const int b_items = p.ntile * (kWgradK / 8);  // (8-channel group, pixel) pairs of B
+  bool failed = false;
+  for (int it = 0; it < iters; ++it) {
+    const int s = it & 1;
+    uint8_t* sa = smem + s * stage_bytes;
+    uint8_t* sb = sa + a_bytes;
+    int fail = 0;
+    if (it >= 2 && !mbar_wait(&bars[s], (uint32_t)((it >> 1) - 1) & 1u)) fail = 1;
+    const long long q0 = (c_begin + it) * kWgradK;
+    // A: 16 groups of 8 weight rows x 64 pixels
+    for (int i = tid; i < (kTileM / 8) * kWgradK; i += kThreads) {
+      const int pix = i & (kWgradK - 1), grp = i / kWgradK;
+      const int r0 = m0 + grp * 8;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      const long long q = q0 + pix;
+      if (r0 < rows && q < npix) {
+        const int tap = r0 / p.cin, ci = r0 - tap * p.cin;
+        const int qb = (int)(q / hw);
+        const long long r = q - (long long)qb * hw;
+        const int qy = (int)(r / p.w_), qx = (int)(r - (long long)(r / p.w_) * p.w_);
+        const int yy = qy + tap / p.ks - half, xx = qx + tap % p.ks - half;
+        if (yy >= 0 && yy < p.h && xx >= 0 && xx < p.w_)
+          v = __ldg(reinterpret_cast<const uint4*>(
+              p.x + (((long long)qb * p.h + yy) * p.w_ + xx) * p.xs + ci));
+      }
+      scatter8(sa + grp * sbo + (pix >> 3) * 128 + (pix & 7) * 2, v);
+    }
+    // B: ntile / 8 groups of 8 output channels x 64 pixels
+    for (int i = tid; i < b_items; i += kThreads) {
+      const int pix = i & (kWgradK - 1), grp = i / kWgradK;
+      const long long q = q0 + pix;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (q < npix) v = __ldg(reinterpret_cast<const uint4*>(p.dz + q * p.dzs + n0 + grp * 8));
+      scatter8(sb + grp * sbo + (pix >> 3) * 128 + (pix & 7) * 2, v);
+    }
+    fence_async_smem();
+    if (__syncthreads_or(fail)) {
+      failed = true;
+      break;
+    }
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+      for (int kk = 0; kk < kWgradK / 16; ++kk)
+        mma_bf16(tmem, smem_desc(a0 + kk * 256, 128, sbo), smem_desc(b0 + kk * 256, 128, sbo), idesc,
+                 (it | kk) != 0);
+      mma_commit(&bars[s]);
+    }
+  }
+  if (tid == 0) mma_commit(&bars[2]);
+  const bool done = mbar_wait(&bars[2], 0);
+  const bool ok = __syncthreads_and(done && !failed) != 0;
+  if (ok && iters > 0) {
+    tc_fence_after();
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const int r = m0 + tid;
+    for (int nc = 0; nc < p.ntile; nc += 8) {
+      float v[8];
+      tmem_ld8(lane_base + (uint32_t)nc, v);
+      if (r >= rows) continue;
+      for (int j = 0; j < 8; ++j) atomicAdd(p.dw + (long long)(n0 + nc + j) * rows + r, v[j]);
+    }
+  } else if (!ok && tid == 0) {
+    atomicCAS(&g_sg_status, 0, SHY_ERR_TIMEOUT);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_free(tmem, p.tmem_cols);
+  }
+}
+
+__global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ dz, int dzs, long long npix,
+                                 int channels, long long per_block, float* __restrict__ db) {
+  const long long q0 = (long long)blockIdx.x * per_block;
+  const long long q1 = min(q0 + per_block, npix);
+  for (int c = threadIdx.x; c < channels; c += blockDim.x) {
+    float s = 0.0f;
+    for (long long q = q0; q < q1; ++q) s += __bfloat162float(dz[q * dzs + c]);
+    atomicAdd(db + c, s);
+  }
+}
+
+__global__ void gelu_backward_kernel(long long n, int channels, const float* __restrict__ da, int das,
+                                     int dao, const float* __restrict__ z, int zs, int zo,
+                                     __nv_bfloat16* __restrict__ dz) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long q = i / channels;
+    const int c = (int)(i - q * channels);
+    dz[i] = __float2bfloat16_rn(da[q * das + dao + c] * gelu_grad(z[q * zs + zo + c]));
+  }
+}
+
+// one thread per (pooled pixel, 8-channel vector)
+__global__ void pool_fwd_kernel(int batch, int h, int w, int channels, const __nv_bfloat16* __restrict__ x,
+                                int xs, int xo, __nv_bfloat16* __restrict__ y, int ys, int yo) {
+  const int ho = h >> 1, wo = w >> 1, nv = channels >> 3;
+  const long long n = (long long)batch * ho * wo * nv;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int v = (int)(i % nv);
+    const long long qo = i / nv;
+    const int ox = (int)(qo % wo);
+    const long long t = qo / wo;
+    const int oy = (int)(t % ho), b = (int)(t / ho);
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int dy = 0; dy < 2; ++dy)
+      for (int dx = 0; dx < 2; ++dx) {
+        const long long qi = ((long long)b * h + 2 * oy + dy) * w + 2 * ox + dx;
+        const uint4 u = __ldg(reinterpret_cast<const uint4*>(x + qi * xs + xo + 8 * v));
+        const uint32_t ws[4] = {u.x, u.y, u.z, u.w};
+        for (int e = 0; e < 4; ++e) {
+          acc[2 * e] += bf16_lo(ws[e]);
+          acc[2 * e + 1] += bf16_hi(ws[e]);
+        }
+      }
+    uint4 o;
+    o.x = pack_bf16(0.25f * acc[0], 0.25f * acc[1]);
+    o.y = pack_bf16(0.25f * acc[2], 0.25f * acc[3]);
+    o.z = pack_bf16(0.25f * acc[4], 0.25f * acc[5]);
+    o.w = pack_bf16(0.25f * acc[6], 0.25f * acc[7]);
+    *reinterpret_cast<uint4*>(y + qo * ys + yo + 8 * v) = o;
+  }
+}
+
+// one thread per (input pixel, channel)
+__global__ void pool_bwd_kernel(int batch, int h, int w, int channels, const float* __restrict__ dy, int dys,
+                                int dyo, float* __restrict__ dx, int dxs, int dxo) {
+  const long long n = (long long)batch * h * w * channels;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % channels);
+    const long long qi = i / channels;
+    const int x = (int)(qi % w);
+    const long long t = qi / w;
+    const int y = (int)(t % h), b = (int)(t / h);
+    const long long qo = ((long long)b * (h >> 1) + (y >> 1)) * (w >> 1) + (x >> 1);
+    dx[qi * dxs + dxo + c] += 0.25f * dy[qo * dys + dyo + c];
+  }
+}
+
+// one thread per (fine pixel, 8-channel vector); h, w: the coarse grid
+__global__ void up_fwd_kernel(int batch, int h, int w, int channels, const __nv_bfloat16* __restrict__ x,
+                              int xs, int xo, __nv_bfloat16* __restrict__ y, int ys, int yo) {
+  const int hf = 2 * h, wf = 2 * w, nv = channels >> 3;
+  const long long n = (long long)batch * hf * wf * nv;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int v = (int)(i % nv);
+    const long long qf = i / nv;
+    const int fx = (int)(qf % wf);
+    const long long t = qf / wf;
+    const int fy = (int)(t % hf), b = (int)(t / hf);
+    const long long qc = ((long long)b * h + (fy >> 1)) * w + (fx >> 1);
+    *reinterpret_cast<uint4*>(y + qf * ys + yo + 8 * v) =
+        __ldg(reinterpret_cast<const uint4*>(x + qc * xs + xo + 8 * v));
+  }
+}
+
+// one thread per (coarse pixel, channel)
+__global__ void up_bwd_kernel(int batch, int h, int w, int channels, const float* __restrict__ dy, int dys,
+                              int dyo, float* __restrict__ dx, int dxs, int dxo) {
+  const long long n = (long long)batch * h * w * channels;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % channels);
+    const long long qc = i / channels;
+    const int x = (int)(qc % w);
+    const long long t = qc / w;
+    const int y = (int)(t % h), b = (int)(t / h);
+    float s = 0.0f;
+    for (int ddy = 0; ddy < 2; ++ddy)
+      for (int ddx = 0; ddx < 2; ++ddx) {
+        const long long qf = ((long long)b * 2 * h + 2 * y + ddy) * (2 * w) + 2 * x + ddx;
+        s += dy[qf * dys + dyo + c];
+      }
+    dx[qc * dxs + dxo + c] += s;
+  }
+}
+
+__global__ void weight_prep_kernel(int cout, int taps, int cin, const float* __restrict__ w,
+                                   __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wf) {
+  const long long n = (long long)cout * taps * cin;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int ci = (int)(i % cin);
+    const long long t = i / cin;
+    const int tap = (int)(t % taps), co = (int)(t / taps);
+    const __nv_bfloat16 v = __float2bfloat16_rn(w[i]);
+    wb[i] = v;
+    if (wf) wf[((long long)ci * taps + (taps - 1 - tap)) * cout + co] = v;
+  }
+}
+
+__global__ void adamw_kernel(long long n, float* __restrict__ p, const float* __restrict__ g,
+                             float* __restrict__ m, float* __restrict__ v, const shy_sg_adamw_args a) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = a.beta1 * m[i] + (1.0f - a.beta1) * gi;
+    const float vi = a.beta2 * v[i] + (1.0f - a.beta2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float step = (mi / a.bc1) / (sqrtf(vi / a.bc2) + a.eps);
+    p[i] -= a.lr * (step + a.weight_decay * p[i]);
+  }
+}
+
+__global__ void features_kernel(int batch, int h, int w, const float* __restrict__ hm, const shy_sg_norm nm,
+                                __nv_bfloat16* __restrict__ x) {
+  const long long n = (long long)batch * h * w;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(q % w);
+    const long long t = q / w;
+    const int r = (int)(t % h), b = (int)(t / h);
+    const float* img = hm + (long long)b * h * w;
+    const int r0 = max(r - 1, 0), r1 = min(r + 1, h - 1);
+    const int c0 = max(c - 1, 0), c1 = min(c + 1, w - 1);
+    const float gr = (img[(long long)r1 * w + c] - img[(long long)r0 * w + c]) / (float)max(r1 - r0, 1);
+    const float gc = (img[(long long)r * w + c1] - img[(long long)r * w + c0]) / (float)max(c1 - c0, 1);
+    const float hv = (img[(long long)r * w + c] - nm.height_mean) * nm.height_scale;
+    uint4* dst = reinterpret_cast<uint4*>(x + q * 16);
+    dst[0] = make_uint4(pack_bf16(hv, gr * nm.slope_scale), pack_bf16(gc * nm.slope_scale, 0.0f), 0u, 0u);
+    dst[1] = make_uint4(0u, 0u, 0u, 0u);
+  }
+}
+
+__global__ void loss_kernel(long long n, const float* __restrict__ z, int zs, const float* __restrict__ t,
+                            float w0, float w1, float w2, float scale, __nv_bfloat16* __restrict__ dz,
+                            double* __restrict__ loss) {
+  __shared__ double part[32];
+  double acc = 0.0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float e0 = z[q * zs] - t[3 * q], e1 = z[q * zs + 1] - t[3 * q + 1], e2 = z[q * zs + 2] - t[3 * q + 2];
+    acc += (double)(w0 * e0 * e0) + (double)(w1 * e1 * e1) + (double)(w2 * e2 * e2);
+    uint4* dst = reinterpret_cast<uint4*>(dz + q * 16);
+    dst[0] = make_uint4(pack_bf16(2.0f * w0 * e0 * scale, 2.0f * w1 * e1 * scale),
+                        pack_bf16(2.0f * w2 * e2 * scale, 0.0f), 0u, 0u);
+    dst[1] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += part[i];
+    atomicAdd(loss, s * (double)scale);
+  }
+}
+
+__global__ void decode_kernel(long long n, const float* __restrict__ z, int zs, const shy_sg_norm nm,
+                              float* __restrict__ d, float* __restrict__ mx, float* __restrict__ my) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    d[q] = fmaxf(0.0f, expm1f(z[q * zs] * nm.out_scale[0] + nm.out_mean[0]));
+    mx[q] = z[q * zs + 1] * nm.out_scale[1] + nm.out_mean[1];
+    my[q] = z[q * zs + 2] * nm.out_scale[2] + nm.out_mean[2];
+  }
+}
+
+int grid_for(long long n, int block = 256) {
+  const long long g = (n + block - 1) / block;
+  return (int)std::max(1ll, std::min(g, 152ll * 32));
+}
+
+bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+int launch_status(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return SHY_ERR_CUDA;
+  }
+  return SHY_OK;
+}
+
+// Output-channel tile: the largest of 128, 96, 64, 32, 16 dividing cout.
+int pick_ntile(int cout) {
+  for (int t : {128, 96, 64, 32, 16})
+    if (cout % t == 0) return t;
+  return 0;
+}
+
+int pow2_cols(int n) {
+  int c = 32;
+  while (c < n) c <<= 1;
+  return c;
+}
+
+// Dynamic shared memory for a tensor-core CTA: its stages, raised where
+// needed so that the CTAs resident on one SM never ask for more than the
+// 512 TMEM columns together.
+int smem_for(int stage_bytes, int tmem_cols) {
+  const int need = 2 * stage_bytes;
+  const int max_ctas = 512 / tmem_cols;
+  const int floor_bytes = kSmemPerSm / (max_ctas + 1) - kSmemReservedPerCta + 1024;
+  return std::max(need, floor_bytes);
+}
+
+bool check_conv_desc(const shy_sg_conv_desc* d, const char* fn) {
+  if (!d) {
+    set_error("%s: null descriptor", fn);
+    return false;
+  }
+  if (d->batch <= 0 || d->height <= 0 || d->width <= 0 || d->cin <= 0 || d->cout <= 0 ||
+      d->cin % 16 || d->cout % 16 || (d->ksize != 1 && d->ksize != 3)) {
+    set_error("%s: bad shape %dx%dx%d cin %d cout %d ksize %d", fn, d->batch, d->height, d->width, d->cin,
+              d->cout, d->ksize);
+    return false;
+  }
+  const long long npix = (long long)d->batch * d->height * d->width;
+  if (npix > (1ll << 40) / 128) {
+    set_error("%s: too many pixels", fn);
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+}  // namespace shy
+
+using namespace shy;
+
+extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int32_t x_stride, const void* w,
+                                   const float* bias, float* z, int32_t z_stride, int32_t z_offset, void* a,
+                                   int32_t a_stride, int32_t a_offset, int32_t act, void* stream) {
+  static const char* fn = "shy_sg_conv_forward";
+  if (!check_conv_desc(d, fn)) return SHY_ERR_INVALID_ARG;
+  if (!x || !w || (!z && !a) || !aligned16(x) || !aligned16(w) || x_stride < d->cin || x_stride % 8) {
+    set_error("%s: bad input or weight pointer or stride", fn);
+    return SHY_ERR_INVALID_ARG;
+  }
+  if (z && (!aligned16(z) || z_stride % 4 || z_offset % 4 || z_offset < 0 || z_offset + d->cout > z_stride)) {
+    set_error("%s: bad f32 output layout", fn);
+    return SHY_ERR_INVALID_ARG;
+  }
+  if (a && (!aligned16(a) || a_stride % 8 || a_offset % 8 || a_offset < 0 || a_offset + d->cout > a_stride)) {
+    set_error("%s: bad bf16 output layout", fn);
+    return SHY_ERR_INVALID_ARG;
+  }
+  if (act != SHY_SG_ACT_NONE && act != SHY_SG_ACT_GELU) {
+    set_error("%s: unknown activation %d", fn, act);
+    return SHY_ERR_INVALID_ARG;
+  }
+  ConvFwd p{};
+  p.x = static_cast<const __nv_bfloat16*>(x);
+  p.w = static_cast<const __nv_bfloat16*>(w);
+  p.bias = bias;
+  p.z = z;
+  p.a = static_cast<__nv_bfloat16*>(a);
+  p.batch = d->batch;
+  p.h = d->height;
+  p.w_ = d->width;
+  p.cin = d->cin;
+  p.cout = d->cout;
+  p.ks = d->ksize;
+  p.xs = x_stride;
+  p.zs = z_stride;
+  p.zo = z_offset;
+  p.as = a_stride;
+  p.ao = a_offset;
+  p.act = act;
+  p.ntile = pick_ntile(d->cout);
+  p.kc = d->cin % 64 == 0 ? 64 : d->cin % 32 == 0 ? 32 : 16;
+  p.tmem_cols = pow2_cols(p.ntile);
+  const int stage = (kTileM + p.ntile) * p.kc * 2;
+  const int smem = smem_for(stage, p.tmem_cols);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(conv_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  const long long npix = (long long)d->batch * d->height * d->width;
+  dim3 grid((unsigned)((npix + kTileM - 1) / kTileM), (unsigned)(d->cout / p.ntile));
+  conv_fwd_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(p);
+  return launch_status(fn);
+}
+
+extern "C" int shy_sg_conv_wgrad(const shy_sg_conv_desc* d, const void* x, int32_t x_stride, const void* dz,
+                                 int32_t dz_stride, float* dw, void* stream) {
+  static const char* fn = "shy_sg_conv_wgrad";
+  if (!check_conv_desc(d, fn)) return SHY_ERR_INVALID_ARG;
+  if (!x || !dz || !dw || !aligned16(x) || !aligned16(dz) || x_stride < d->cin || x_stride % 8 ||
+      dz_stride < d->cout || dz_stride % 8) {
+    set_error("%s: bad pointer or stride", fn);
+    return SHY_ERR_INVALID_ARG;
+  }
+  ConvWgrad p{};
+  p.x = static_cast<const __nv_bfloat16*>(x);
+  p.dz = static_cast<const __nv_bfloat16*>(dz);
+  p.dw = dw;
+  p.batch = d->batch;
+  p.h = d->height;
+  p.w_ = d->width;
+  p.cin = d->cin;
+  p.cout = d->cout;
+  p.ks = d->ksize;
+  p.xs = x_stride;
+  p.dzs = dz_stride;
+  p.ntile = pick_ntile(d->cout);
+  p.tmem_cols = pow2_cols(p.ntile);
+  const int rows = d->ksize * d->ksize * d->cin;
+  const long long npix = (long long)d->batch * d->height * d->width;
+  const long long nchunks = (npix + kWgradK - 1) / kWgradK;
+  const int tiles = ((rows + kTileM - 1) / kTileM) * (d->cout / p.ntile);
+  long long splits = std::max(1ll, std::min(nchunks, (4ll * 152 + tiles - 1) / tiles));
+  p.chunks_per_split = (nchunks + splits - 1) / splits;
+  splits = (nchunks + p.chunks_per_split - 1) / p.chunks_per_split;
+  const int stage = (kTileM + p.ntile) * kWgradK * 2;
+  const int smem = smem_for(stage, p.tmem_cols);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(conv_wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  dim3 grid((unsigned)((rows + kTileM - 1) / kTileM), (unsigned)(d->cout / p.ntile), (unsigned)splits);
+  conv_wgrad_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(p);
+  return launch_status(fn);
+}
+
+extern "C" int shy_sg_bias_grad(int64_t pixels, int32_t channels, const void* dz, int32_t dz_stride, float* db,
+                                void* stream) {
+  if (pixels <= 0 || channels <= 0 || !dz || !db || dz_stride < channels) {
+    set_error("shy_sg_bias_grad: bad arguments");
+    return SHY_ERR_INVALID_ARG;
+  }
+  const long long per = std::max(64ll, (long long)(pixels + 4 * 152 - 1) / (4 * 152));
+  const int blocks = (int)((pixels + per - 1) / per);
+  bias_grad_kernel<<<blocks, 128, 0, static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const __nv_bfloat16*>(dz), dz_stride, pixels, channels, per, db);
+  return launch_status("shy_sg_bias_grad");
+}
+
+extern "C" int shy_sg_gelu_backward(int64_t pixels, int32_t channels, const float* da, int32_t da_stride,
+                                    int32_t da_offset, const float* z, int32_t z_stride, int32_t z_offset,
+                                    void* dz, void* stream) {
+  if (pixels <= 0 || channels <= 0 || !da || !z || !dz || da_offset < 0 || z_offset < 0 ||
+      da_offset + channels > da_stride || z_offset + channels > z_stride) {
+    set_error("shy_sg_gelu_backward: bad arguments");
+    return SHY_ERR_INVALID_ARG;
+  }
+  const long long n = pixels * channels;
+  gelu_backward_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      n, channels, da, da_stride, da_offset, z, z_stride, z_offset, static_cast<__nv_bfloat16*>(dz));
+  return launch_status("shy_sg_gelu_backward");
+}
+
+namespace {
+bool check_resample(int batch, int h, int w, int c, bool need_even, const char* fn) {
+  if (batch <= 0 || h <= 0 || w <= 0 || c <= 0 || (need_even && ((h | w) & 1))) {
+    shy::set_error("%s: bad shape %dx%dx%d c %d", fn, batch, h, w, c);
+    return false;
+  }
+  return true;
+}
+bool check_vec(const void* p, int stride, int off, int c, const char* fn) {
+  if (!p || !aligned16(p) || stride % 8 || off % 8 || c % 8 || off < 0 || off + c > stride) {
+    shy::set_error("%s: bf16 tensors need 16-byte alignment, strides, offsets and channels in multiples of 8",
+                   fn);
+    return false;
+  }
+  return true;
+}
+bool check_scalar(const void* p, int stride, int off, int c, const char* fn) {
+  if (!p || off < 0 || off + c > stride) {
+    shy::set_error("%s: bad f32 tensor layout", fn);
+    return false;
+  }
+  return true;
+}
+}  // namespace
+
+extern "C" int shy_sg_pool_forward(int32_t batch, int32_t height, int32_t width, int32_t channels, const void* x,
+                                   int32_t x_stride, int32_t x_offset, void* y, int32_t y_stride,
+                                   int32_t y_offset, void* stream) {
+  static const char* fn = "shy_sg_pool_forward";
+  if (!check_resample(batch, height, width, channels, true, fn) ||
+      !check_vec(x, x_stride, x_offset, channels, fn) || !check_vec(y, y_stride, y_offset, channels, fn))
+    return SHY_ERR_INVALID_ARG;
+  const long long n = (long long)batch * (height / 2) * (width / 2) * (channels / 8);
+  pool_fwd_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      batch, height, width, channels, static_cast<const __nv_bfloat16*>(x), x_stride, x_offset,
+      static_cast<__nv_bfloat16*>(y), y_stride, y_offset);
+  return launch_status(fn);
+}
+
+extern "C" int shy_sg_pool_backward(int32_t batch, int32_t height, int32_t width, int32_t channels,
+                                    const float* dy, int32_t dy_stride, int32_t dy_offset, float* dx,
+                                    int32_t dx_stride, int32_t dx_offset, void* stream) {
+  static const char* fn = "shy_sg_pool_backward";
+  if (!check_resample(batch, height, width, channels, true, fn) ||
+      !check_scalar(dy, dy_stride, dy_offset, channels, fn) || !check_scalar(dx, dx_stride, dx_offset, channels, fn))
+    return SHY_ERR_INVALID_ARG;
+  const long long n = (long long)batch * height * width * channels;
+  pool_bwd_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      batch, height, width, channels, dy, dy_stride, dy_offset, dx, dx_stride, dx_offset);
+  return launch_status(fn);
+}
+
+extern "C" int shy_sg_upsample_forward(int32_t batch, int32_t height, int32_t width, int32_t channels,
+                                       const void* x, int32_t x_stride, int32_t x_offset, void* y, int32_t y_stride,
+                                       int32_t y_offset, void* stream) {
+  static const char* fn = "shy_sg_upsample_forward";
+  if (!check_resample(batch, height, width, channels, false, fn) ||
+      !check_vec(x, x_stride, x_offset, channels, fn) || !check_vec(y, y_stride, y_offset, channels, fn))
+    return SHY_ERR_INVALID_ARG;
+  const long long n = (long long)batch * (2 * height) * (2 * width) * (channels / 8);
+  up_fwd_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      batch, height, width, channels, static_cast<const __nv_bfloat16*>(x), x_stride, x_offset,
+      static_cast<__nv_bfloat16*>(y), y_stride, y_offset);
+  return launch_status(fn);
+}
+
+extern "C" int shy_sg_upsample_backward(int32_t batch, int32_t height, int32_t width, int32_t channels,
+                                        const float* dy, int32_t dy_stride, int32_t dy_offset, float* dx,
+                                        int32_t dx_stride, int32_t dx_offset, void* stream) {
+  static const char* fn = "shy_sg_upsample_backward";
+  if (!check_resample(batch, height, width, channels, false, fn) ||
+      !check_scalar(dy, dy_stride, dy_offset, channels, fn) || !check_scalar(dx, dx_stride, dx_offset, channels, fn))
+    return SHY_ERR_INVALID_ARG;
+  const long long n = (long long)batch * height * width * channels;
+  up_bwd_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      batch, height, width, channels, dy, dy_stride, dy_offset, dx, dx_stride, dx_offset);
+  return launch_status(fn);
+}
+
+extern "C" int shy_sg_weight_prep(int32_t cout, int32_t ksize, int32_t cin, const float* w, void* w_bf16,
+                                  void* w_flip, void* stream) {
+  if (cout <= 0 || cin <= 0 || (ksize != 1 && ksize != 3) || !w || !w_bf16) {
+    set_error("shy_sg_weight_prep: bad arguments");
+    return SHY_ERR_INVALID_ARG;
+  }
+  const long long n = (long long)cout * ksize * ksize * cin;
+  weight_prep_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      cout, ksize * ksize, cin, w, static_cast<__nv_bfloat16*>(w_bf16), static_cast<__nv_bfloat16*>(w_flip));
+  return launch_status("shy_sg_weight_prep");
+}
+
+extern "C" int shy_sg_adamw(int64_t n, float* p, const float* g, float* m, float* v, const shy_sg_adamw_args* a,
+                            void* stream) {
+  if (n <= 0 || !p || !g || !m || !v || !a || !(a->bc1 > 0.0f) || !(a->bc2 > 0.0f)) {
+    set_error("shy_sg_adamw: bad arguments");
+    return SHY_ERR_INVALID_ARG;
+  }
+  adamw_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(n, p, g, m, v, *a);
+  return launch_status("shy_sg_adamw");
+}
+
+extern "C" int shy_sg_features(int32_t batch, int32_t height, int32_t width, const float* h, const shy_sg_norm* n,
+                               void* x, void* stream) {
+  if (batch <= 0 || height <= 0 || width <= 0 || !h || !n || !x || !aligned16(x)) {
+    set_error("shy_sg_features: bad arguments");
+    return SHY_ERR_INVALID_ARG;
+  }
+  const long long npix = (long long)batch * height * width;
+  features_kernel<<<grid_for(npix), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      batch, height, width, h, *n, static_cast<__nv_bfloat16*>(x));
+  return launch_status("shy_sg_features");
+}
+
+extern "C" int shy_sg_loss(int64_t pixels, const float* z, int32_t z_stride, const float* target,
+                           const float weights[3], void* dz, double* loss, void* stream) {
+  if (pixels <= 0 || !z || z_stride < 3 || !target || !weights || !dz || !aligned16(dz) || !loss) {
+    set_error("shy_sg_loss: bad arguments");
+    return SHY_ERR_INVALID_ARG;
+  }
+  const float scale = (float)(1.0 / (3.0 * (double)pixels));
+  loss_kernel<<<grid_for(pixels), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      pixels, z, z_stride, target, weights[0], weights[1], weights[2], scale, static_cast<__nv_bfloat16*>(dz),
+      loss);
+  return launch_status("shy_sg_loss");
+}
+
+extern "C" int shy_sg_decode(int64_t pixels, const float* z, int32_t z_stride, const shy_sg_norm* n,
+                             float* discharge, float* momentumx, float* momentumy, void* stream) {
+  if (pixels <= 0 || !z || z_stride < 3 || !n || !discharge || !momentumx || !momentumy) {
+    set_error("shy_sg_decode: bad arguments");
+    return SHY_ERR_INVALID_ARG;
+  }
+  decode_kernel<<<grid_for(pixels), 256, 0, static_cast<cudaStream_t>(stream)>>>(pixels, z, z_stride, *n,
+                                                                                 discharge, momentumx, momentumy);
+  return launch_status("shy_sg_decode");
+}
+
+extern "C" int shy_sg_status(void) {
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    set_error("shy_sg_status: %s", cudaGetErrorString(cudaGetLastError()));
+    return SHY_ERR_CUDA;
+  }
+  int st = 0;
+  const int zero = 0;
+  if (cudaMemcpyFromSymbol(&st, g_sg_status, sizeof(int)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_sg_status, &zero, sizeof(int)) != cudaSuccess) {
+    set_error("shy_sg_status: %s", cudaGetErrorString(cudaGetLastError()));
+    return SHY_ERR_CUDA;
+  }
+  if (st != 0) {
+    set_error("surrogate tensor-core kernel gave up waiting on its MMAs");
+    return st;
+  }
+  return SHY_OK;
+}

@@ -1,5 +1,6 @@
 """The C ABI library without a GPU: it loads, exports every entry point that
-include/shy.h declares, and validates arguments before touching a device."""
+include/shy.h and include/shy_surrogate.h declare, and validates arguments
+before touching a device."""
 import ctypes as C
 import os
 import re
@@ -8,11 +9,11 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-HEADER = os.path.join(ROOT, "include", "shy.h")
+HEADERS = [os.path.join(ROOT, "include", h) for h in ("shy.h", "shy_surrogate.h")]
 
 
 def declared():
-    src = open(HEADER).read()
+    src = "".join(open(h).read() for h in HEADERS)
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\**(shy_\w+)\s*\(", src, flags=re.M)))
 
