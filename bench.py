@@ -9,7 +9,7 @@ scatter, lrate blend and cascade.  One step = one erosion cycle
 dataset; the terrain recipe stands in for the reference's FastNoiseLite map.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload plain|batch|converge|large]
+                  [--workload plain|batch|converge|large|surrogate]
 
 `value` is device throughput with the maps resident in HBM; between timed
 steps the L2 is flushed by writing a 256 MiB buffer (untimed).  `e2e` is the
@@ -26,6 +26,9 @@ end-of-cycle pass over the whole step time.
 
 `--workload converge` measures the plain method's time to converged
 discharge (within 5 % log-L2 of the discharge after 4 x 500 cycles).
+
+`--workload surrogate` trains the learned warm-start on the device and
+compares the time to converged discharge with and without it.
 
 `--workload large` runs the large-scale configuration: 8192^2, 4,194,304
 drops per cycle, per-cell vegetation every cycle.
@@ -541,6 +544,165 @@ def run_converge(args):
     print(json.dumps(out))
 
 
+def _discharge_run(shy, seed, n, drops, cycles, warm=None):
+    """A plain run of `cycles` cycles on the value-noise terrain of `seed`
+    from zero maps, or from the surrogate's maps when `warm` is given.
+    Returns (discharge after each cycle, device ms of each cycle, warm-start
+    seconds: the surrogate's prediction and the map upload, wall clock)."""
+    import torch
+    w = shy.World(n, n, seed=seed)
+    w.generate(seed, 8)
+    t_warm = 0.0
+    if warm is not None:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        warm.warm_start(w)
+        w.sync()
+        t_warm = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(w.stream())
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ds, ms = [], []
+    for _ in range(cycles):
+        ev[0].record(stream)
+        w.erode(drops, 1)
+        ev[1].record(stream)
+        ds.append(w.get_field("discharge"))
+        ms.append(ev[0].elapsed_time(ev[1]))
+    w.close()
+    return ds, ms, t_warm
+
+
+def run_surrogate(args):
+    """The learned warm-start against the plain method: time to converged
+    discharge on 1024^2 terrains.
+
+    The plain method's discharge is a blend with lrate 0.1 of each cycle's
+    tracks (source/world.h:83-85), so from zero maps it takes tens of cycles
+    to settle; after that the terrain's erosion keeps moving it slowly, and
+    single-cycle snapshots differ by about 10 % log-L2 at 65,536 drops on
+    1024^2.  So the reference D* is the mean discharge of cycles
+    horizon+1 .. horizon+10 of the plain run, and a run has converged at
+    the first cycle k where the mean discharge of its last min(k, 10)
+    cycles is within 5 % log-L2 of D*.  The warm run starts from the
+    surrogate's maps and its time includes the prediction.
+
+    The surrogate is trained first, on pairs the batched GPU particle method
+    generates: 256^2 value-noise terrains (seeds 10000+i), input the initial
+    heightmap, targets the maps after `horizon` cycles at the same drop
+    density (4,096 drops per cycle).  Evaluation terrains are 1024^2, seeds
+    20000+i."""
+    import numpy as np
+    import torch
+
+    import simplehydrology_gb300 as shy
+    from simplehydrology_gb300 import build as shybuild
+    from simplehydrology_gb300 import surrogate as sg
+    shybuild.build()
+    torch.cuda.init()
+    clock = ClockSampler(torch.cuda.current_device())
+    clock.__enter__()
+    horizon, theta, n_tr, n_val = args.horizon, 0.05, args.train_terrains, 64
+    t0 = time.perf_counter()
+    H, D, MX, MY = sg.make_pairs(n_tr + n_val, size=256, cycles=horizon, seed0=10000)
+    gen_s = time.perf_counter() - t0
+    norm = sg.Norm.fit(H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr])
+    net = sg.Surrogate(seed=0, norm=norm)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    batch = 16
+    launches0 = net.launches
+    ev[0].record()
+    losses = sg.train(net, H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr], epochs=args.epochs, batch=batch, lr=2e-3)
+    ev[1].record()
+    torch.cuda.synchronize()
+    net.status()
+    train_ms = ev[0].elapsed_time(ev[1])
+    steps = args.epochs * (n_tr // batch)
+    train_flops = steps * batch * 256 * 256 * sg.flops_per_pixel(True)
+    # held-out 256^2 pairs: the prediction against the particle method's maps
+    val_pred, _, _ = net.predict(torch.from_numpy(H[n_tr:]).cuda())
+    vp = val_pred.cpu().numpy()
+    val = {"terrains": n_val, "log_l2_prediction": float(np.mean([sg.log_l2(vp[i], D[n_tr + i])
+                                                                  for i in range(n_val)])),
+           "log_l2_zero_maps": 1.0}
+
+    # the dominant convolution shape alone: dec2a forward (384 -> 128 channels,
+    # 3x3) at the training batch, level 2 of 256^2 (16 x 64 x 64 pixels)
+    ws = net.workspace(batch, 256, 256, True)
+    for _ in range(3):
+        net._conv(ws, "dec2a", 2, ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
+    reps = 20
+    ev[0].record()
+    for _ in range(reps):
+        net._conv(ws, "dec2a", 2, ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
+    ev[1].record()
+    torch.cuda.synchronize()
+    conv_ms = ev[0].elapsed_time(ev[1]) / reps
+    conv_flops = 2.0 * batch * 64 * 64 * 9 * 384 * 128
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            bf16_peak, peak_src = float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        bf16_peak, peak_src = 1900.0, "fallback"
+
+    # warm start against plain on 1024^2 terrains
+    n, drops, total = 1024, 65536, horizon + 10
+    per = []
+    for i in range(args.eval_terrains):
+        seed = 20000 + i
+        dp, mp, _ = _discharge_run(shy, seed, n, drops, total)
+        ref = np.mean(dp[horizon:], axis=0)
+        dw_, mw, t_warm = _discharge_run(shy, seed, n, drops, total, warm=net)
+        pred = net.predict(torch.from_numpy(_initial_height(shy, seed, n)[None]).cuda())[0][0].cpu().numpy()
+
+        def window(ds, k):
+            return np.mean(ds[max(0, k - 10):k], axis=0)
+
+        dist_p = [sg.log_l2(window(dp, k), ref) for k in range(1, total + 1)]
+        dist_w = [sg.log_l2(window(dw_, k), ref) for k in range(1, total + 1)]
+        snap_p = [sg.log_l2(d, ref) for d in dp]
+        kp = next((k + 1 for k, d in enumerate(dist_p) if d <= theta), None)
+        kw = next((k + 1 for k, d in enumerate(dist_w) if d <= theta), None)
+        tp = sum(mp[:kp]) / 1e3 if kp else None
+        tw = t_warm + sum(mw[:kw]) / 1e3 if kw else None
+        per.append({"seed": seed, "cycles_plain": kp, "cycles_warm": kw, "plain_s": tp, "warm_s": tw,
+                    "warm_start_s": t_warm, "log_l2_prediction": sg.log_l2(pred, ref),
+                    "log_l2_plain_window": [round(d, 4) for d in dist_p[::5]],
+                    "log_l2_warm_window": [round(d, 4) for d in dist_w[::5]],
+                    "log_l2_plain_snapshot": [round(d, 4) for d in snap_p[::5]],
+                    "ms_per_cycle": sum(mp) / len(mp)})
+    clock.__exit__()
+    tps = [r["plain_s"] for r in per if r["plain_s"]]
+    tws = [r["warm_s"] for r in per if r["warm_s"]]
+    out = {"metric": "time to converged discharge (<=5% log-L2), plain vs surrogate warm start", "unit": "s",
+           "value": statistics.mean(tws) if tws else None,
+           "plain_s": statistics.mean(tps) if tps else None,
+           "speedup": (statistics.mean(tps) / statistics.mean(tws)) if tps and tws else None,
+           "higher_is_better": False, "n_gpus": 1, "dtype": "bf16 (f32 accumulate)",
+           "data": "synthetic (seeded value-noise terrains; training pairs from the GPU particle method)",
+           "config": {"workload": "learned warm-start: U-Net (1.36 M parameters, 4 levels, channels 32-256) "
+                                  "trained on 256x256 terrains, evaluated on 1024x1024 at 65536 drops/cycle",
+                      "horizon_cycles": horizon, "threshold": theta, "window_cycles": 10,
+                      "train_terrains": n_tr, "epochs": args.epochs, "batch": batch},
+           "training": {"pairs_s": gen_s, "train_s": train_ms / 1e3, "steps": steps,
+                        "tflops": train_flops / (train_ms / 1e3) / 1e12,
+                        "loss_by_epoch": [round(v, 5) for v in losses],
+                        "launches": net.launches - launches0, "validation": val},
+           "roofline": {"bound": "tensor", "kernel": "conv_fwd_kernel (384->128, 3x3, 16x64x64 pixels)",
+                        "achieved": conv_flops / (conv_ms / 1e3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+                        "frac": conv_flops / (conv_ms / 1e3) / 1e12 / bf16_peak, "peak_source": peak_src,
+                        "avg_launch_ms": conv_ms, "traffic": None},
+           "terrains": per, "clocks": clock.summary()}
+    print(json.dumps(out))
+
+
+def _initial_height(shy, seed, n):
+    w = shy.World(n, n, seed=seed)
+    w.generate(seed, 8)
+    h = w.get_field("height")
+    w.close()
+    return h
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -554,10 +716,15 @@ def main():
     ap.add_argument("--drops", type=int, default=DROPS)
     ap.add_argument("--no-e2e", action="store_true")
     # the batched-terrain configuration (not the default bench line)
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "converge", "large"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "converge", "large", "surrogate"])
     ap.add_argument("--ref-cycles", type=int, default=2000)
     ap.add_argument("--check-every", type=int, default=10)
     ap.add_argument("--terrains", type=int, default=64)
+    # --workload surrogate
+    ap.add_argument("--horizon", type=int, default=50)
+    ap.add_argument("--train-terrains", type=int, default=1024)
+    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--eval-terrains", type=int, default=2)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
@@ -565,6 +732,8 @@ def main():
         run_reference(args)
     elif args.workload == "converge":
         run_converge(args)
+    elif args.workload == "surrogate":
+        run_surrogate(args)
     else:
         run_ours(args)
 

@@ -425,5 +425,75 @@ class Surrogate:
                 g[L["b"]:L["b"] + L["cout"]])
 
 
-__all__ = ["Surrogate", "Norm", "LAYERS", "param_count", "flops_per_pixel"]
+def make_pairs(n, size=256, drops=None, cycles=50, seed0=10000, per_launch=64, params=None):
+    """Training pairs from the batched GPU particle method.  Terrain i is
+    the value-noise heightmap of seed seed0 + i.  Its input is the heightmap
+    before erosion.  Its targets are the discharge and momentum maps after
+    `cycles` plain cycles from zero maps, at `drops` drops per cycle (by
+    default size^2 / 16, the density of 65,536 drops on 1024 x 1024).
+    Terrains run `per_launch` at a time in one Batch.  Returns float32
+    arrays (heights, discharge, momentum x, momentum y), each (n, size, size)."""
+    from . import Batch
+    drops = drops or max(1, size * size // 16)
+    out = [np.empty((n, size, size), np.float32) for _ in range(4)]
+    for s in range(0, n, per_launch):
+        k = min(per_launch, n - s)
+        b = Batch([(size, size)] * k, [drops] * k, [seed0 + s + i for i in range(k)], params)
+        try:
+            for i in range(k):
+                b.generate(i, seed0 + s + i, 8)
+                b.get_field(i, "height", out=out[0][s + i])
+            b.erode(cycles)
+            for i in range(k):
+                for j, f in enumerate(("discharge", "momentum_x", "momentum_y")):
+                    b.get_field(i, f, out=out[j + 1][s + i])
+        finally:
+            b.close()
+    return tuple(out)
+
+
+def train(net, heights, discharge, momx, momy, epochs, batch=16, lr=2e-3, seed=0, augment=True):
+    """AdamW over the pairs with a cosine learning-rate schedule.  With
+    `augment`, each batch is flipped along either axis at random (discharge
+    is unchanged and the momentum component along a flipped axis changes
+    sign; a world's x-major map is an image with rows = x).  Returns the
+    mean loss of each epoch."""
+    torch = net.torch
+    H = torch.from_numpy(np.ascontiguousarray(heights, np.float32)).to(net.dev)
+    T = torch.from_numpy(net.norm.targets(discharge, momx, momy)).to(net.dev)
+    sign = torch.tensor(net.norm.out_mean, dtype=torch.float32, device=net.dev)
+    scale = torch.tensor(net.norm.out_scale, dtype=torch.float32, device=net.dev)
+    n = H.shape[0]
+    per_epoch = max(1, n // batch)
+    total = epochs * per_epoch
+    rng = np.random.default_rng(seed)
+    losses, step = [], 0
+    for _ in range(epochs):
+        perm = rng.permutation(n)
+        acc = torch.zeros(1, dtype=torch.float64, device=net.dev)
+        for j in range(per_epoch):
+            idx = torch.from_numpy(perm[j * batch:(j + 1) * batch]).to(net.dev)
+            h, t = H[idx], T[idx]
+            if augment:
+                for axis, comp in ((1, 1), (2, 2)):
+                    if rng.random() < 0.5:
+                        h, t = h.flip(axis), t.flip(axis)
+                        # momentum along the flipped axis: raw -> -raw in normalised units
+                        t[..., comp] = -t[..., comp] - 2.0 * sign[comp] / scale[comp]
+                h, t = h.contiguous(), t.contiguous()
+            lr_t = lr * 0.5 * (1.0 + math.cos(math.pi * step / total))
+            acc += net.train_step(h, t, lr_t)
+            step += 1
+        losses.append(float(acc.item()) / per_epoch)
+    return losses
+
+
+def log_l2(d, ref):
+    """||log1p(d) - log1p(ref)|| / ||log1p(ref)||, the discharge distance."""
+    a = np.log1p(np.asarray(d, np.float64))
+    b = np.log1p(np.asarray(ref, np.float64))
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+__all__ = ["Surrogate", "Norm", "LAYERS", "param_count", "flops_per_pixel", "make_pairs", "train", "log_l2"]
 _ = _capi

@@ -298,3 +298,24 @@ def test_training_reduces_the_loss(sg):
     net.status()
     assert last < 0.1 * first, (first, last)
     _ = rng
+
+
+def test_trained_network_beats_the_method_without_it(sg):
+    """Trained on pairs from the GPU particle method, the network's maps for
+    held-out terrains are closer to the particle method's (log-L2) than zero
+    maps (the plain method's start) and than the training set's mean map
+    (the best terrain-blind guess)."""
+    n_tr, n_te = 96, 8
+    H, D, MX, MY = sg.make_pairs(n_tr + n_te, size=128, cycles=30, seed0=500)
+    norm = sg.Norm.fit(H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr])
+    net = sg.Surrogate(seed=1, norm=norm)
+    losses = sg.train(net, H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr], epochs=12, batch=8, lr=2e-3)
+    net.status()
+    pred = net.predict(torch.from_numpy(H[n_tr:]).cuda())[0].cpu().numpy()
+    err = np.mean([sg.log_l2(pred[i], D[n_tr + i]) for i in range(n_te)])
+    mean_map = D[:n_tr].mean(0)
+    blind = np.mean([sg.log_l2(mean_map, D[n_tr + i]) for i in range(n_te)])
+    zero = np.mean([sg.log_l2(0 * mean_map, D[n_tr + i]) for i in range(n_te)])
+    print({"loss_by_epoch": losses, "prediction": err, "mean_map": blind, "zero_maps": zero})
+    assert losses[-1] < losses[0]
+    assert err < blind < zero == 1.0
