@@ -544,13 +544,14 @@ def run_converge(args):
     print(json.dumps(out))
 
 
-def _discharge_run(shy, seed, n, drops, cycles, warm=None):
+def _discharge_run(shy, seed, n, drops, cycles, warm=None, spawn_seed=None):
     """A plain run of `cycles` cycles on the value-noise terrain of `seed`
-    from zero maps, or from the surrogate's maps when `warm` is given.
+    from zero maps, or from the surrogate's maps when `warm` is given; the
+    spawns follow `spawn_seed` (default `seed`).
     Returns (discharge after each cycle, device ms of each cycle, warm-start
     seconds: the surrogate's prediction and the map upload, wall clock)."""
     import torch
-    w = shy.World(n, n, seed=seed)
+    w = shy.World(n, n, seed=seed if spawn_seed is None else spawn_seed)
     w.generate(seed, 8)
     t_warm = 0.0
     if warm is not None:
@@ -628,16 +629,20 @@ def run_surrogate(args):
     # the dominant convolution shape alone: dec2a forward (384 -> 128 channels,
     # 3x3) at the training batch, level 2 of 256^2 (16 x 64 x 64 pixels)
     ws = net.workspace(batch, 256, 256, True)
-    for _ in range(3):
-        net._conv(ws, "dec2a", 2, ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
-    reps = 20
-    ev[0].record()
-    for _ in range(reps):
-        net._conv(ws, "dec2a", 2, ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
-    ev[1].record()
-    torch.cuda.synchronize()
-    conv_ms = ev[0].elapsed_time(ev[1]) / reps
     conv_flops = 2.0 * batch * 64 * 64 * 9 * 384 * 128
+    reps, conv_paths = 20, {}
+    for path, label in ((1, "staged"), (0, "tma")):
+        shy._capi.check(shy.lib().shy_sg_set_conv_path(path))
+        for _ in range(3):
+            net._conv(ws, "dec2a", 2, ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
+        ev[0].record()
+        for _ in range(reps):
+            net._conv(ws, "dec2a", 2, ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
+        ev[1].record()
+        torch.cuda.synchronize()
+        conv_paths[label] = ev[0].elapsed_time(ev[1]) / reps
+    net.status()
+    conv_ms = conv_paths["tma"]
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             bf16_peak, peak_src = float(json.load(f)["bf16_tflops"]), "measured"
@@ -652,6 +657,8 @@ def run_surrogate(args):
         dp, mp, _ = _discharge_run(shy, seed, n, drops, total)
         ref = np.mean(dp[horizon:], axis=0)
         dw_, mw, t_warm = _discharge_run(shy, seed, n, drops, total, warm=net)
+        # the same terrain with other spawns: how far apart two plain runs end
+        do, _, _ = _discharge_run(shy, seed, n, drops, total, spawn_seed=seed + 7919)
         pred = net.predict(torch.from_numpy(_initial_height(shy, seed, n)[None]).cuda())[0][0].cpu().numpy()
 
         def window(ds, k):
@@ -660,12 +667,17 @@ def run_surrogate(args):
         dist_p = [sg.log_l2(window(dp, k), ref) for k in range(1, total + 1)]
         dist_w = [sg.log_l2(window(dw_, k), ref) for k in range(1, total + 1)]
         snap_p = [sg.log_l2(d, ref) for d in dp]
+        dist_o = [sg.log_l2(window(do, k), ref) for k in range(1, total + 1)]
+        d_pred = sg.log_l2(pred, ref)
+        worth = next((k + 1 for k, d in enumerate(dist_p) if d <= d_pred), None)
         kp = next((k + 1 for k, d in enumerate(dist_p) if d <= theta), None)
         kw = next((k + 1 for k, d in enumerate(dist_w) if d <= theta), None)
         tp = sum(mp[:kp]) / 1e3 if kp else None
         tw = t_warm + sum(mw[:kw]) / 1e3 if kw else None
         per.append({"seed": seed, "cycles_plain": kp, "cycles_warm": kw, "plain_s": tp, "warm_s": tw,
-                    "warm_start_s": t_warm, "log_l2_prediction": sg.log_l2(pred, ref),
+                    "warm_start_s": t_warm, "log_l2_prediction": d_pred,
+                    "prediction_worth_plain_cycles": worth,
+                    "log_l2_other_spawns_window": [round(d, 4) for d in dist_o[::5]],
                     "log_l2_plain_window": [round(d, 4) for d in dist_p[::5]],
                     "log_l2_warm_window": [round(d, 4) for d in dist_w[::5]],
                     "log_l2_plain_snapshot": [round(d, 4) for d in snap_p[::5]],
@@ -690,7 +702,8 @@ def run_surrogate(args):
            "roofline": {"bound": "tensor", "kernel": "conv_fwd_kernel (384->128, 3x3, 16x64x64 pixels)",
                         "achieved": conv_flops / (conv_ms / 1e3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
                         "frac": conv_flops / (conv_ms / 1e3) / 1e12 / bf16_peak, "peak_source": peak_src,
-                        "avg_launch_ms": conv_ms, "traffic": None},
+                        "avg_launch_ms": conv_ms, "traffic": None,
+                        "tflops_by_staging": {k: conv_flops / (v / 1e3) / 1e12 for k, v in conv_paths.items()}},
            "terrains": per, "clocks": clock.summary()}
     print(json.dumps(out))
 

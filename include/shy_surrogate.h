@@ -42,6 +42,19 @@ typedef struct shy_sg_conv_desc {
 #define SHY_SG_ACT_NONE 0
 #define SHY_SG_ACT_GELU 1 /* 0.5 z (1 + erf(z / sqrt 2)) */
 
+/* How shy_sg_conv_forward stages its operands (process-wide):
+ * SHY_SG_CONV_TMA     tensor-memory-accelerator copies into a four-stage
+ *                     pipeline (the default);
+ * SHY_SG_CONV_STAGED  loads by the CTA's threads into two stages. */
+#define SHY_SG_CONV_TMA 0
+#define SHY_SG_CONV_STAGED 1
+int shy_sg_set_conv_path(int32_t path);
+/* Depth of the TMA pipeline, 2..8 stages of one channel chunk each, or 0
+ * (the default) to choose per convolution (process-wide).  Deeper
+ * pipelines keep more loads in flight; shallower ones fit more CTAs on an
+ * SM. */
+int shy_sg_set_conv_stages(int32_t stages);
+
 /* z = conv(x, w) + bias (bias may be NULL); written as f32 to `z` (may be
  * NULL) and as act(z) in bf16 to `a` (may be NULL).  x: bf16, pixel stride
  * x_stride.  w: bf16 [cout][ksize*ksize][cin] (tap = ky*ksize + kx).  The
@@ -64,10 +77,12 @@ int shy_sg_bias_grad(int64_t pixels, int32_t channels, const void* dz, int32_t d
                      float* db, void* stream);
 
 /* dz[pixel][c] = bf16(da * gelu'(z)); da, z: f32 with their own stride and
- * offset; dz: bf16, pixel stride `channels`. */
+ * offset; dz: bf16, pixel stride `channels`.  If db is not NULL (channels
+ * must then divide 256), db[c] += the sum of dz[.][c] over pixels as well:
+ * the bias gradient of the convolution whose output gradient dz is. */
 int shy_sg_gelu_backward(int64_t pixels, int32_t channels, const float* da, int32_t da_stride,
                          int32_t da_offset, const float* z, int32_t z_stride, int32_t z_offset,
-                         void* dz, void* stream);
+                         void* dz, float* db, void* stream);
 
 /* 2 x 2 average pooling, bf16 -> bf16.  height, width: the input's (even). */
 int shy_sg_pool_forward(int32_t batch, int32_t height, int32_t width, int32_t channels,

@@ -167,7 +167,7 @@ SIGNATURES = {
     "shy_sg_conv_wgrad": (C.c_int, [P(SgConvDesc), W, C.c_int32, W, C.c_int32, W, W]),
     "shy_sg_bias_grad": (C.c_int, [C.c_int64, C.c_int32, W, C.c_int32, W, W]),
     "shy_sg_gelu_backward": (C.c_int, [C.c_int64, C.c_int32, W, C.c_int32, C.c_int32, W, C.c_int32, C.c_int32,
-                                       W, W]),
+                                       W, W, W]),
     "shy_sg_pool_forward": (C.c_int, [C.c_int32] * 4 + [W, C.c_int32, C.c_int32, W, C.c_int32, C.c_int32, W]),
     "shy_sg_pool_backward": (C.c_int, [C.c_int32] * 4 + [W, C.c_int32, C.c_int32, W, C.c_int32, C.c_int32, W]),
     "shy_sg_upsample_forward": (C.c_int, [C.c_int32] * 4 + [W, C.c_int32, C.c_int32, W, C.c_int32, C.c_int32,
@@ -179,6 +179,8 @@ SIGNATURES = {
     "shy_sg_features": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, W, P(SgNorm), W, W]),
     "shy_sg_loss": (C.c_int, [C.c_int64, W, C.c_int32, W, FP, W, W, W]),
     "shy_sg_decode": (C.c_int, [C.c_int64, W, C.c_int32, P(SgNorm), W, W, W, W]),
+    "shy_sg_set_conv_path": (C.c_int, [C.c_int32]),
+    "shy_sg_set_conv_stages": (C.c_int, [C.c_int32]),
     "shy_sg_status": (C.c_int, []),
 }
 

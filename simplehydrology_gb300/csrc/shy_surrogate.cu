@@ -31,6 +31,8 @@
 //
 // Every wait on an mbarrier is bounded (2 s); a CTA that gives up records
 // SHY_ERR_TIMEOUT, skips its epilogue and still frees its tensor memory.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include "../../include/shy_surrogate.h"
@@ -311,6 +313,181 @@ __global__ void __launch_bounds__(kThreads) conv_fwd_kernel(const ConvFwd p) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Convolution forward with TMA staging (conv_tma_kernel).
+//
+// The same GEMM as conv_fwd_kernel, but the tile is 8 x 16 pixels of one
+// image and its operands arrive by TMA: A is a box of kc channels x 16 x 8
+// pixels of the input at the tap's offset (the tensor map's zero fill gives
+// the padding at the image border), B a box of kc x ntile weights.  Each
+// box lands as rows of kc * 2 bytes, swizzled by the TMA in the pattern the
+// MMA's descriptor names (128-, 64- or 32-byte swizzle for kc = 64, 32, 16;
+// 8-row groups 8 * kc * 2 bytes apart).  Thread 0 runs a pipeline of 2..8
+// pipeline: loads run stages - 1 chunks ahead of the MMAs, each stage's
+// "full" barrier completes on the loads' byte count and its "empty" barrier
+// on the commit of the MMAs that read it.  All 128 threads then read the
+// accumulator for the epilogue.
+constexpr int kMaxStages = 8;
+constexpr int kTileH = 8, kTileW = 16;
+
+struct ConvTma {
+  const float* bias;
+  float* z;
+  __nv_bfloat16* a;
+  int batch, h, w_, cin, cout, ks;
+  int zs, zo, as, ao, act;
+  int ntile, kc, tmem_cols, tiles_w, tiles_h, stages;
+  uint32_t a_bytes, b_bytes, stage_bytes, layout;
+};
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor, K-major, swizzled: `layout` 2, 4 or 6
+// (128-, 64-, 32-byte swizzle), `sbo` the distance between 8-row groups.
+__device__ __forceinline__ uint64_t smem_desc_sw(uint32_t addr, uint32_t sbo, uint32_t layout) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | (1ull << 16) | ((uint64_t)(sbo >> 4) << 32) | (1ull << 46) |
+         ((uint64_t)layout << 61);
+}
+
+__global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constant__ CUtensorMap map_x,
+                                                           const __grid_constant__ CUtensorMap map_w,
+                                                           const ConvTma p) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_fail;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  int t = blockIdx.x;
+  const int tx = t % p.tiles_w;
+  t /= p.tiles_w;
+  const int ty = t % p.tiles_h, b = t / p.tiles_h;
+  const int x0 = tx * kTileW, y0 = ty * kTileH;
+  const int n0 = blockIdx.y * p.ntile;
+
+  if (warp == 0) tmem_alloc(&tmem_slot, p.tmem_cols);
+  if (tid == 0) {
+    for (int s = 0; s < p.stages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
+    s_fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (tid == 0) {
+    const int taps = p.ks * p.ks, half = p.ks >> 1;
+    const int nchunk = p.cin / p.kc, iters = taps * nchunk;
+    const uint32_t idesc = idesc_bf16_m128(p.ntile);
+    const uint32_t sbo = 16u * p.kc;
+    const int S = p.stages;
+    auto issue = [&](int it) {
+      const int s = it % S;
+      const int tap = it / nchunk, c0 = (it - tap * nchunk) * p.kc;
+      const int dy = tap / p.ks - half, dx = tap % p.ks - half;
+      const uint32_t sa = base + s * p.stage_bytes;
+      mbar_expect_tx(&full[s], p.a_bytes + p.b_bytes);
+      tma_load_4d(sa, &map_x, c0, x0 + dx, y0 + dy, b, &full[s]);
+      tma_load_2d(sa + p.a_bytes, &map_w, tap * p.cin + c0, n0, &full[s]);
+    };
+    int issued = 0, consumed = 0;
+    bool fail = false;
+    for (; issued < S - 1 && issued < iters; ++issued) issue(issued);
+    for (int it = 0; it < iters; ++it) {
+      const int s = it % S;
+      if (!mbar_wait(&full[s], (uint32_t)(it / S) & 1u)) {
+        fail = true;
+        break;
+      }
+      consumed = it + 1;
+      tc_fence_after();
+      const uint32_t sa = base + s * p.stage_bytes, sb = sa + p.a_bytes;
+      for (int kk = 0; kk < (p.kc >> 4); ++kk)
+        mma_bf16(tmem, smem_desc_sw(sa + kk * 32, sbo, p.layout), smem_desc_sw(sb + kk * 32, sbo, p.layout), idesc,
+                 (it | kk) != 0);
+      mma_commit(&empty[s]);
+      if (issued < iters) {
+        const int s2 = issued % S;
+        if (issued >= S && !mbar_wait(&empty[s2], (uint32_t)(issued / S - 1) & 1u)) {
+          fail = true;
+          break;
+        }
+        issue(issued);
+        ++issued;
+      }
+    }
+    // after a failure, wait (bounded) for loads still landing in this CTA's memory
+    for (int it = consumed; it < issued; ++it) mbar_wait(&full[it % S], (uint32_t)(it / S) & 1u);
+    mma_commit(&done);
+    if (fail) s_fail = 1;
+  }
+  const bool fin = mbar_wait(&done, 0);
+  const bool ok = __syncthreads_and(fin) != 0 && s_fail == 0;
+  if (ok) {
+    tc_fence_after();
+    const int y = y0 + (tid >> 4), x = x0 + (tid & 15);
+    const bool valid = y < p.h && x < p.w_;
+    const long long q = ((long long)b * p.h + y) * p.w_ + x;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int nc = 0; nc < p.ntile; nc += 8) {
+      float v[8];
+      tmem_ld8(lane_base + (uint32_t)nc, v);
+      if (!valid) continue;
+      const int n = n0 + nc;
+      if (p.bias)
+        for (int j = 0; j < 8; ++j) v[j] += __ldg(p.bias + n + j);
+      if (p.z) {
+        float4* zp = reinterpret_cast<float4*>(p.z + q * p.zs + p.zo + n);
+        zp[0] = make_float4(v[0], v[1], v[2], v[3]);
+        zp[1] = make_float4(v[4], v[5], v[6], v[7]);
+      }
+      if (p.a) {
+        if (p.act == SHY_SG_ACT_GELU)
+          for (int j = 0; j < 8; ++j) v[j] = gelu(v[j]);
+        uint4 o;
+        o.x = pack_bf16(v[0], v[1]);
+        o.y = pack_bf16(v[2], v[3]);
+        o.z = pack_bf16(v[4], v[5]);
+        o.w = pack_bf16(v[6], v[7]);
+        *reinterpret_cast<uint4*>(p.a + q * p.as + p.ao + n) = o;
+      }
+    }
+  } else if (tid == 0) {
+    atomicCAS(&g_sg_status, 0, SHY_ERR_TIMEOUT);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_free(tmem, p.tmem_cols);
+  }
+}
+
 struct ConvWgrad {
   const __nv_bfloat16* x;
   const __nv_bfloat16* dz;
@@ -436,8 +613,36 @@ __global__ void __launch_bounds__(kThreads) conv_wgrad_kernel(const ConvWgrad p)
   }
 }
 
-__global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ dz, int dzs, long long npix,
-                                 int channels, long long per_block, float* __restrict__ db) {
+// Per-channel sums for channel counts dividing 256: with 256-thread blocks
+// and a grid stride that is a multiple of 256, every element a thread visits
+// has channel threadIdx.x % channels.  The block adds its threads' sums in
+// shared memory and makes one atomic addition per channel.
+__device__ __forceinline__ void flush_channel_sums(float acc, int channels, float* db) {
+  __shared__ float red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  if ((int)threadIdx.x < channels) {
+    float s = 0.0f;
+    for (int t = threadIdx.x; t < (int)blockDim.x; t += channels) s += red[t];
+    atomicAdd(db + threadIdx.x, s);
+  }
+}
+
+__global__ void __launch_bounds__(256) bias_grad_kernel(const __nv_bfloat16* __restrict__ dz, int dzs,
+                                                        long long npix, int channels, float* __restrict__ db) {
+  const long long n = npix * channels;
+  float acc = 0.0f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long q = i / channels;
+    acc += __bfloat162float(dz[q * dzs + (i - q * channels)]);
+  }
+  flush_channel_sums(acc, channels, db);
+}
+
+// any channel count: one thread per channel over a range of pixels
+__global__ void bias_grad_any_kernel(const __nv_bfloat16* __restrict__ dz, int dzs, long long npix, int channels,
+                                     long long per_block, float* __restrict__ db) {
   const long long q0 = (long long)blockIdx.x * per_block;
   const long long q1 = min(q0 + per_block, npix);
   for (int c = threadIdx.x; c < channels; c += blockDim.x) {
@@ -447,15 +652,20 @@ __global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ dz, int dzs, 
   }
 }
 
-__global__ void gelu_backward_kernel(long long n, int channels, const float* __restrict__ da, int das,
-                                     int dao, const float* __restrict__ z, int zs, int zo,
-                                     __nv_bfloat16* __restrict__ dz) {
+__global__ void __launch_bounds__(256) gelu_backward_kernel(long long n, int channels, const float* __restrict__ da,
+                                                            int das, int dao, const float* __restrict__ z, int zs,
+                                                            int zo, __nv_bfloat16* __restrict__ dz,
+                                                            float* __restrict__ db) {
+  float acc = 0.0f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const long long q = i / channels;
     const int c = (int)(i - q * channels);
-    dz[i] = __float2bfloat16_rn(da[q * das + dao + c] * gelu_grad(z[q * zs + zo + c]));
+    const __nv_bfloat16 v = __float2bfloat16_rn(da[q * das + dao + c] * gelu_grad(z[q * zs + zo + c]));
+    dz[i] = v;
+    acc += __bfloat162float(v);
   }
+  if (db) flush_channel_sums(acc, channels, db);
 }
 
 // one thread per (pooled pixel, 8-channel vector)
@@ -666,6 +876,54 @@ int smem_for(int stage_bytes, int tmem_cols) {
   return std::max(need, floor_bytes);
 }
 
+int g_conv_path = SHY_SG_CONV_TMA;
+int g_conv_stages = 0;  // 0: chosen per convolution
+
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime.
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// Tensor maps of one convolution: the input as (channels, width, height,
+// batch) with a box of kc x 16 x 8 x 1, the weights as (taps * cin, cout)
+// with a box of kc x ntile; both bf16, swizzled to the box's row width,
+// zero fill outside.
+bool encode_conv_maps(const shy_sg_conv_desc* d, const void* x, int xs, const void* w, int kc, int ntile,
+                      CUtensorMap* mx, CUtensorMap* mw) {
+  auto fn = encode_tiled();
+  if (!fn) return false;
+  const CUtensorMapSwizzle sw =
+      kc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : kc == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
+  const cuuint64_t row = (cuuint64_t)xs * 2;
+  const cuuint64_t gx[4] = {(cuuint64_t)d->cin, (cuuint64_t)d->width, (cuuint64_t)d->height, (cuuint64_t)d->batch};
+  const cuuint64_t sx[3] = {row, row * d->width, row * d->width * d->height};
+  const cuuint32_t bx[4] = {(cuuint32_t)kc, (cuuint32_t)kTileW, (cuuint32_t)kTileH, 1};
+  const cuuint32_t e4[4] = {1, 1, 1, 1};
+  if (fn(mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), gx, sx, bx, e4, CU_TENSOR_MAP_INTERLEAVE_NONE,
+         sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  const cuuint64_t k = (cuuint64_t)d->ksize * d->ksize * d->cin;
+  const cuuint64_t gw[2] = {k, (cuuint64_t)d->cout};
+  const cuuint64_t sw2[1] = {k * 2};
+  const cuuint32_t bw[2] = {(cuuint32_t)kc, (cuuint32_t)ntile};
+  return fn(mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(w), gw, sw2, bw, e4,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 bool check_conv_desc(const shy_sg_conv_desc* d, const char* fn) {
   if (!d) {
     set_error("%s: null descriptor", fn);
@@ -710,6 +968,59 @@ extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int
   }
   if (act != SHY_SG_ACT_NONE && act != SHY_SG_ACT_GELU) {
     set_error("%s: unknown activation %d", fn, act);
+    return SHY_ERR_INVALID_ARG;
+  }
+  const int ntile = pick_ntile(d->cout);
+  const int kc = d->cin % 64 == 0 ? 64 : d->cin % 32 == 0 ? 32 : 16;
+  CUtensorMap mx, mw;
+  if (g_conv_path == SHY_SG_CONV_TMA && encode_conv_maps(d, x, x_stride, w, kc, ntile, &mx, &mw)) {
+    ConvTma p{};
+    p.bias = bias;
+    p.z = z;
+    p.a = static_cast<__nv_bfloat16*>(a);
+    p.batch = d->batch;
+    p.h = d->height;
+    p.w_ = d->width;
+    p.cin = d->cin;
+    p.cout = d->cout;
+    p.ks = d->ksize;
+    p.zs = z_stride;
+    p.zo = z_offset;
+    p.as = a_stride;
+    p.ao = a_offset;
+    p.act = act;
+    p.ntile = ntile;
+    p.kc = kc;
+    p.tmem_cols = pow2_cols(ntile);
+    p.tiles_w = (d->width + kTileW - 1) / kTileW;
+    p.tiles_h = (d->height + kTileH - 1) / kTileH;
+    p.a_bytes = (uint32_t)kTileM * kc * 2;
+    p.b_bytes = (uint32_t)ntile * kc * 2;
+    p.stage_bytes = p.a_bytes + ((p.b_bytes + 1023u) & ~1023u);
+    p.layout = kc == 64 ? 2u : kc == 32 ? 4u : 6u;
+    // automatic depth: 3 stages (two CTAs an SM) for long 64-channel K loops,
+    // else 2 (measured at the training shapes: 543 vs 476 TFLOP/s on the
+    // 384 -> 128 layer, 269 vs 242 on 96 -> 32)
+    const int iters = d->ksize * d->ksize * (d->cin / kc);
+    const int want = g_conv_stages ? g_conv_stages : (kc == 64 && iters >= 16 ? 3 : 2);
+    p.stages = std::max(2, std::min(want, (200 * 1024 - 1024) / (int)p.stage_bytes));
+    const int smem = smem_for((p.stages * (int)p.stage_bytes + 1024) / 2, p.tmem_cols);
+    static bool attr_tma = false;
+    if (!attr_tma) {
+      cudaFuncSetAttribute(conv_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      attr_tma = true;
+    }
+    const long long tiles = (long long)d->batch * p.tiles_h * p.tiles_w;
+    dim3 grid((unsigned)tiles, (unsigned)(d->cout / ntile));
+    conv_tma_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(mx, mw, p);
+    return launch_status(fn);
+  }
+  if (g_conv_path == SHY_SG_CONV_TMA && !encode_tiled()) {
+    set_error("%s: cuTensorMapEncodeTiled is not available", fn);
+    return SHY_ERR_CUDA;
+  }
+  if (g_conv_path == SHY_SG_CONV_TMA) {
+    set_error("%s: tensor map encoding failed", fn);
     return SHY_ERR_INVALID_ARG;
   }
   ConvFwd p{};
@@ -794,24 +1105,29 @@ extern "C" int shy_sg_bias_grad(int64_t pixels, int32_t channels, const void* dz
     set_error("shy_sg_bias_grad: bad arguments");
     return SHY_ERR_INVALID_ARG;
   }
-  const long long per = std::max(64ll, (long long)(pixels + 4 * 152 - 1) / (4 * 152));
-  const int blocks = (int)((pixels + per - 1) / per);
-  bias_grad_kernel<<<blocks, 128, 0, static_cast<cudaStream_t>(stream)>>>(
-      static_cast<const __nv_bfloat16*>(dz), dz_stride, pixels, channels, per, db);
+  const auto st = static_cast<cudaStream_t>(stream);
+  const __nv_bfloat16* g = static_cast<const __nv_bfloat16*>(dz);
+  if (channels <= 256 && 256 % channels == 0) {
+    bias_grad_kernel<<<grid_for(pixels * channels), 256, 0, st>>>(g, dz_stride, pixels, channels, db);
+  } else {
+    const long long per = std::max(64ll, (long long)(pixels + 4 * 152 - 1) / (4 * 152));
+    bias_grad_any_kernel<<<(int)((pixels + per - 1) / per), 128, 0, st>>>(g, dz_stride, pixels, channels, per, db);
+  }
   return launch_status("shy_sg_bias_grad");
 }
 
 extern "C" int shy_sg_gelu_backward(int64_t pixels, int32_t channels, const float* da, int32_t da_stride,
                                     int32_t da_offset, const float* z, int32_t z_stride, int32_t z_offset,
-                                    void* dz, void* stream) {
+                                    void* dz, float* db, void* stream) {
   if (pixels <= 0 || channels <= 0 || !da || !z || !dz || da_offset < 0 || z_offset < 0 ||
-      da_offset + channels > da_stride || z_offset + channels > z_stride) {
+      da_offset + channels > da_stride || z_offset + channels > z_stride ||
+      (db && (channels > 256 || 256 % channels))) {
     set_error("shy_sg_gelu_backward: bad arguments");
     return SHY_ERR_INVALID_ARG;
   }
   const long long n = pixels * channels;
   gelu_backward_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      n, channels, da, da_stride, da_offset, z, z_stride, z_offset, static_cast<__nv_bfloat16*>(dz));
+      n, channels, da, da_stride, da_offset, z, z_stride, z_offset, static_cast<__nv_bfloat16*>(dz), db);
   return launch_status("shy_sg_gelu_backward");
 }
 
@@ -950,6 +1266,24 @@ extern "C" int shy_sg_decode(int64_t pixels, const float* z, int32_t z_stride, c
   decode_kernel<<<grid_for(pixels), 256, 0, static_cast<cudaStream_t>(stream)>>>(pixels, z, z_stride, *n,
                                                                                  discharge, momentumx, momentumy);
   return launch_status("shy_sg_decode");
+}
+
+extern "C" int shy_sg_set_conv_path(int32_t path) {
+  if (path != SHY_SG_CONV_TMA && path != SHY_SG_CONV_STAGED) {
+    set_error("shy_sg_set_conv_path: unknown path %d", path);
+    return SHY_ERR_INVALID_ARG;
+  }
+  g_conv_path = path;
+  return SHY_OK;
+}
+
+extern "C" int shy_sg_set_conv_stages(int32_t stages) {
+  if (stages != 0 && (stages < 2 || stages > kMaxStages)) {
+    set_error("shy_sg_set_conv_stages: %d stages (0 or 2..%d)", stages, kMaxStages);
+    return SHY_ERR_INVALID_ARG;
+  }
+  g_conv_stages = stages;
+  return SHY_OK;
 }
 
 extern "C" int shy_sg_status(void) {

@@ -270,25 +270,29 @@ class Surrogate:
         self._conv(ws, "head", 0, ws.a["dec0b"], c0, ws.zh, OUT_CH, 0, None, 0, 0, ACT_NONE)
 
     # -- backward -----------------------------------------------------------
-    def _layer_bwd(self, ws, name, level, x_in, xs, dz, dx, dxs):
-        """Weight and bias gradients of one convolution from its output
-        gradient dz (bf16, contiguous); its input gradient into dx (f32,
-        pixel stride dxs) unless dx is None."""
+    def _layer_bwd(self, ws, name, level, x_in, xs, dz, dx, dxs, bias=False):
+        """Weight gradient of one convolution from its output gradient dz
+        (bf16, contiguous), and its bias gradient if `bias` (the GELU
+        backward that made dz adds it otherwise); its input gradient into dx
+        (f32, pixel stride dxs) unless dx is None."""
         L = self.layers[name]
         B, H, W = ws.shape
         d = SgConvDesc(B, H >> level, W >> level, L["cin"], L["cout"], L["k"])
         self._call("shy_sg_conv_wgrad", C.byref(d), self._p(x_in), xs, self._p(dz), L["cout"],
                    self._p(self.grads, L["w"]))
-        self._call("shy_sg_bias_grad", d.batch * d.height * d.width, L["cout"], self._p(dz), L["cout"],
-                   self._p(self.grads, L["b"]))
+        if bias:
+            self._call("shy_sg_bias_grad", d.batch * d.height * d.width, L["cout"], self._p(dz), L["cout"],
+                       self._p(self.grads, L["b"]))
         if dx is not None:
             dd = SgConvDesc(d.batch, d.height, d.width, L["cout"], L["cin"], L["k"])
             self._call("shy_sg_conv_forward", C.byref(dd), self._p(dz), L["cout"], self._p(L["wf"]), None,
                        self._p(dx), dxs, 0, None, 0, 0, ACT_NONE)
 
     def _gelu_bwd(self, ws, level, c, da, das, dao, name):
+        """Output gradient of layer `name` (bf16 into ws.dz[level]) and its
+        bias gradient."""
         self._call("shy_sg_gelu_backward", ws.P[level], c, self._p(da), das, dao, self._p(ws.z[name]), c, 0,
-                   self._p(ws.dz[level]))
+                   self._p(ws.dz[level]), self._p(self.grads, self.layers[name]["b"]))
 
     def backward(self, ws):
         """Gradients of the loss (ws.dzh holds its output gradient) into
@@ -296,7 +300,7 @@ class Surrogate:
         B, H, W = ws.shape
         c0, c1, c2, c3 = CHANNELS
         da, dz, dcat, dp = ws.da, ws.dz, ws.dcat, ws.dpool
-        self._layer_bwd(ws, "head", 0, ws.a["dec0b"], c0, ws.dzh, da[0], c0)
+        self._layer_bwd(ws, "head", 0, ws.a["dec0b"], c0, ws.dzh, da[0], c0, bias=True)
         self._gelu_bwd(ws, 0, c0, da[0], c0, 0, "dec0b")
         self._layer_bwd(ws, "dec0b", 0, ws.a["dec0a"], c0, dz[0], da[0], c0)
         self._gelu_bwd(ws, 0, c0, da[0], c0, 0, "dec0a")

@@ -80,8 +80,16 @@ CONV_CASES = [  # batch, h, w, cin, cout, k, x pixel stride
 ]
 
 
+@pytest.fixture(params=[0, 1], ids=["tma", "staged"])
+def conv_path(request, sg):
+    """Both operand-staging paths of shy_sg_conv_forward; the TMA path is restored after."""
+    ok(lib().shy_sg_set_conv_path(request.param))
+    yield request.param
+    ok(lib().shy_sg_set_conv_path(0))
+
+
 @pytest.mark.parametrize("case", CONV_CASES)
-def test_conv_forward_matches_oracle(sg, case):
+def test_conv_forward_matches_oracle(sg, conv_path, case):
     B, H, W, ci, co, k, xs = case
     rng = np.random.default_rng(sum(case))
     x = so.bf16(rng.standard_normal((B, H, W, xs)))
@@ -129,7 +137,7 @@ def test_weight_gradient_matches_oracle(sg, case):
 
 
 @pytest.mark.parametrize("case", CONV_CASES[:4])
-def test_input_gradient_through_flipped_weights(sg, case):
+def test_input_gradient_through_flipped_weights(sg, conv_path, case):
     B, H, W, ci, co, k, _ = case
     rng = np.random.default_rng(sum(case) + 2)
     w32 = rng.standard_normal((co, k * k, ci)).astype(np.float32)
@@ -188,16 +196,20 @@ def test_elementwise_kernels_match_oracle(sg):
     da = rng.standard_normal((P, 3 * c)).astype(np.float32).astype(np.float64)
     z = (rng.standard_normal((P, c)) * 3).astype(np.float32).astype(np.float64)
     dz = torch.empty((P, c), dtype=torch.bfloat16, device="cuda")
+    dbg = dev(np.full(c, 0.5), torch.float32)
     ok(lib().shy_sg_gelu_backward(P, c, p(dev(da, torch.float32)), 3 * c, c, p(dev(z, torch.float32)), c, 0, p(dz),
-                                  None))
+                                  p(dbg), None))
     want = da[:, c:2 * c] * so.gelu_grad(z)
-    assert np.all(np.abs(host(dz) - want) <= BF16_REL * np.abs(want) + 1e-6 * np.abs(da[:, c:2 * c]))
+    got = host(dz)
+    assert np.all(np.abs(got - want) <= BF16_REL * np.abs(want) + 1e-6 * np.abs(da[:, c:2 * c]))
+    np.testing.assert_allclose(host(dbg), 0.5 + got.sum(0), rtol=1e-5, atol=1e-4)
     # bias gradient
     g = so.bf16(rng.standard_normal((P, 48)))
-    db0 = np.ones(32)
-    db = dev(db0, torch.float32)
-    ok(lib().shy_sg_bias_grad(P, 32, p(dev(g, torch.bfloat16)), 48, p(db), None))
-    np.testing.assert_allclose(host(db), db0 + g[:, :32].sum(0), rtol=1e-5, atol=1e-4)
+    for ch in (32, 48, 16):  # dividing 256 or not
+        db0 = np.ones(ch)
+        db = dev(db0, torch.float32)
+        ok(lib().shy_sg_bias_grad(P, ch, p(dev(g, torch.bfloat16)), 48, p(db), None))
+        np.testing.assert_allclose(host(db), db0 + g[:, :ch].sum(0), rtol=1e-5, atol=1e-4)
     status()
 
 
