@@ -735,8 +735,8 @@ def main():
     ap.add_argument("--terrains", type=int, default=64)
     # --workload surrogate
     ap.add_argument("--horizon", type=int, default=50)
-    ap.add_argument("--train-terrains", type=int, default=1024)
-    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--train-terrains", type=int, default=2048)
+    ap.add_argument("--epochs", type=int, default=24)
     ap.add_argument("--eval-terrains", type=int, default=2)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -369,6 +369,14 @@ __device__ __forceinline__ uint64_t smem_desc_sw(uint32_t addr, uint32_t sbo, ui
          ((uint64_t)layout << 61);
 }
 
+// Shared-memory matrix descriptor, MN-major, swizzled: `lbo` the distance
+// between blocks of one swizzle width along M (or N), `sbo` between 8-row
+// groups along K.
+__device__ __forceinline__ uint64_t smem_desc_mn(uint32_t addr, uint32_t lbo, uint32_t sbo, uint32_t layout) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+         (1ull << 46) | ((uint64_t)layout << 61);
+}
+
 __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constant__ CUtensorMap map_x,
                                                            const __grid_constant__ CUtensorMap map_w,
                                                            const ConvTma p) {
@@ -478,6 +486,140 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
       }
     }
   } else if (tid == 0) {
+    atomicCAS(&g_sg_status, 0, SHY_ERR_TIMEOUT);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_free(tmem, p.tmem_cols);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Weight gradient with TMA staging (wgrad_tma_kernel).
+//
+// D[m = (tap, ci)][n = co] += sum over pixels k of X[k + tap][ci] * dZ[k][co]:
+// M = 128 weight rows, N = a cout tile, K = pixels, one 16 x 8 pixel tile
+// (128 pixels) per pipeline stage.  Both operands keep their channel index
+// contiguous, so the MMA reads them MN-major.  A is 128 / kcm boxes of kcm
+// input channels x 16 x 8 pixels at one tap's offset (box i holds weight
+// rows m0 + i * kcm .., all of one tap); B is ntile / kcn boxes of kcn
+// channels of dZ.  A box lands as 128 pixel rows of kcm * 2 bytes, swizzled
+// to that row width, so its 8-row groups (the swizzle atoms) are 16 * kcm
+// bytes apart (the descriptor's stride byte offset) and consecutive boxes,
+// the next kcm channels along M (or N), 256 * kcm bytes apart (its leading
+// byte offset).  Each CTA sums a range of pixel tiles in tensor memory and
+// adds the result to dw with atomics.
+struct WgradTma {
+  float* dw;
+  int batch, h, w_, cin, cout, ks;
+  int ntile, kcm, kcn, tmem_cols, tiles_w, tiles_h, stages;
+  long long tiles_per_split;
+  uint32_t a_bytes, b_bytes, stage_bytes, la, lb;
+};
+
+__global__ void __launch_bounds__(kThreads) wgrad_tma_kernel(const __grid_constant__ CUtensorMap map_x,
+                                                            const __grid_constant__ CUtensorMap map_dz,
+                                                            const WgradTma p) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_fail;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int taps = p.ks * p.ks, half = p.ks >> 1;
+  const int rows = taps * p.cin;
+  const int m0 = blockIdx.x * kTileM, n0 = blockIdx.y * p.ntile;
+  const long long ntiles = (long long)p.batch * p.tiles_h * p.tiles_w;
+  const long long t_begin = (long long)blockIdx.z * p.tiles_per_split;
+  const long long t_end = min(t_begin + p.tiles_per_split, ntiles);
+  const int iters = (int)max(0ll, t_end - t_begin);
+
+  if (warp == 0) tmem_alloc(&tmem_slot, p.tmem_cols);
+  if (tid == 0) {
+    for (int s = 0; s < p.stages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
+    s_fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (tid == 0) {
+    const int S = p.stages;
+    // MN-major operands: bits 15 and 16 of the instruction descriptor
+    const uint32_t idesc = idesc_bf16_m128(p.ntile) | (1u << 15) | (1u << 16);
+    const int na = kTileM / p.kcm, nb = p.ntile / p.kcn;
+    int na_live = 0;  // boxes of A inside the weight rows (the rest of the tile's rows are never stored)
+    for (int i = 0; i < na; ++i) na_live += (m0 + i * p.kcm < rows);
+    const uint32_t tx_bytes = (uint32_t)na_live * 256u * p.kcm + (uint32_t)nb * 256u * p.kcn;
+    auto issue = [&](int it) {
+      const int s = it % S;
+      long long t = t_begin + it;
+      const int tx = (int)(t % p.tiles_w);
+      t /= p.tiles_w;
+      const int ty = (int)(t % p.tiles_h), b = (int)(t / p.tiles_h);
+      const int x0 = tx * kTileW, y0 = ty * kTileH;
+      const uint32_t sa = base + s * p.stage_bytes, sb = sa + p.a_bytes;
+      mbar_expect_tx(&full[s], tx_bytes);
+      for (int i = 0; i < na; ++i) {
+        const int r = m0 + i * p.kcm;
+        if (r >= rows) break;
+        const int tap = r / p.cin, c0 = r - tap * p.cin;
+        tma_load_4d(sa + i * 256u * p.kcm, &map_x, c0, x0 + tap % p.ks - half, y0 + tap / p.ks - half, b,
+                    &full[s]);
+      }
+      for (int j = 0; j < nb; ++j) tma_load_4d(sb + j * 256u * p.kcn, &map_dz, n0 + j * p.kcn, x0, y0, b, &full[s]);
+    };
+    int issued = 0, consumed = 0;
+    bool fail = false;
+    for (; issued < S - 1 && issued < iters; ++issued) issue(issued);
+    for (int it = 0; it < iters; ++it) {
+      const int s = it % S;
+      if (!mbar_wait(&full[s], (uint32_t)(it / S) & 1u)) {
+        fail = true;
+        break;
+      }
+      consumed = it + 1;
+      tc_fence_after();
+      const uint32_t sa = base + s * p.stage_bytes, sb = sa + p.a_bytes;
+      for (int kk = 0; kk < kTileM / 16; ++kk)
+        mma_bf16(tmem, smem_desc_mn(sa + kk * 32u * p.kcm, 256u * p.kcm, 16u * p.kcm, p.la),
+                 smem_desc_mn(sb + kk * 32u * p.kcn, 256u * p.kcn, 16u * p.kcn, p.lb), idesc, (it | kk) != 0);
+      mma_commit(&empty[s]);
+      if (issued < iters) {
+        const int s2 = issued % S;
+        if (issued >= S && !mbar_wait(&empty[s2], (uint32_t)(issued / S - 1) & 1u)) {
+          fail = true;
+          break;
+        }
+        issue(issued);
+        ++issued;
+      }
+    }
+    for (int it = consumed; it < issued; ++it) mbar_wait(&full[it % S], (uint32_t)(it / S) & 1u);
+    mma_commit(&done);
+    if (fail) s_fail = 1;
+  }
+  const bool fin = mbar_wait(&done, 0);
+  const bool ok = __syncthreads_and(fin) != 0 && s_fail == 0;
+  if (ok && iters > 0) {
+    tc_fence_after();
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const int r = m0 + tid;
+    for (int nc = 0; nc < p.ntile; nc += 8) {
+      float v[8];
+      tmem_ld8(lane_base + (uint32_t)nc, v);
+      if (r >= rows) continue;
+      for (int j = 0; j < 8; ++j) atomicAdd(p.dw + (long long)(n0 + nc + j) * rows + r, v[j]);
+    }
+  } else if (!ok && tid == 0) {
     atomicCAS(&g_sg_status, 0, SHY_ERR_TIMEOUT);
   }
   tc_fence_before();
@@ -897,30 +1039,40 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
   return fn;
 }
 
-// Tensor maps of one convolution: the input as (channels, width, height,
-// batch) with a box of kc x 16 x 8 x 1, the weights as (taps * cin, cout)
-// with a box of kc x ntile; both bf16, swizzled to the box's row width,
-// zero fill outside.
+CUtensorMapSwizzle swizzle_for(int kc) {
+  return kc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : kc == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
+}
+
+// An NHWC bf16 activation tensor (channels, width, height, batch) with a
+// box of kc channels x 16 x 8 pixels x 1 image, swizzled to the box's row
+// width, zero fill outside.
+bool encode_act_map(CUtensorMap* m, const void* ptr, int channels, int width, int height, int batch, int stride,
+                    int kc) {
+  auto fn = encode_tiled();
+  if (!fn) return false;
+  const cuuint64_t row = (cuuint64_t)stride * 2;
+  const cuuint64_t g[4] = {(cuuint64_t)channels, (cuuint64_t)width, (cuuint64_t)height, (cuuint64_t)batch};
+  const cuuint64_t st[3] = {row, row * width, row * width * height};
+  const cuuint32_t box[4] = {(cuuint32_t)kc, (cuuint32_t)kTileW, (cuuint32_t)kTileH, 1};
+  const cuuint32_t e[4] = {1, 1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(ptr), g, st, box, e,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(kc), CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Tensor maps of one convolution: the input (encode_act_map) and the
+// weights as (taps * cin, cout) with a box of kc x ntile.
 bool encode_conv_maps(const shy_sg_conv_desc* d, const void* x, int xs, const void* w, int kc, int ntile,
                       CUtensorMap* mx, CUtensorMap* mw) {
   auto fn = encode_tiled();
-  if (!fn) return false;
-  const CUtensorMapSwizzle sw =
-      kc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : kc == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
-  const cuuint64_t row = (cuuint64_t)xs * 2;
-  const cuuint64_t gx[4] = {(cuuint64_t)d->cin, (cuuint64_t)d->width, (cuuint64_t)d->height, (cuuint64_t)d->batch};
-  const cuuint64_t sx[3] = {row, row * d->width, row * d->width * d->height};
-  const cuuint32_t bx[4] = {(cuuint32_t)kc, (cuuint32_t)kTileW, (cuuint32_t)kTileH, 1};
-  const cuuint32_t e4[4] = {1, 1, 1, 1};
-  if (fn(mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), gx, sx, bx, e4, CU_TENSOR_MAP_INTERLEAVE_NONE,
-         sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-    return false;
+  if (!fn || !encode_act_map(mx, x, d->cin, d->width, d->height, d->batch, xs, kc)) return false;
   const cuuint64_t k = (cuuint64_t)d->ksize * d->ksize * d->cin;
   const cuuint64_t gw[2] = {k, (cuuint64_t)d->cout};
   const cuuint64_t sw2[1] = {k * 2};
   const cuuint32_t bw[2] = {(cuuint32_t)kc, (cuuint32_t)ntile};
-  return fn(mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(w), gw, sw2, bw, e4,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+  const cuuint32_t e[2] = {1, 1};
+  return fn(mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(w), gw, sw2, bw, e,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(kc), CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -1066,6 +1218,52 @@ extern "C" int shy_sg_conv_wgrad(const shy_sg_conv_desc* d, const void* x, int32
     set_error("%s: bad pointer or stride", fn);
     return SHY_ERR_INVALID_ARG;
   }
+  const int ntile = pick_ntile(d->cout);
+  const int rows = d->ksize * d->ksize * d->cin;
+  if (g_conv_path == SHY_SG_CONV_TMA) {
+    WgradTma q{};
+    q.kcm = d->cin % 64 == 0 ? 64 : d->cin % 32 == 0 ? 32 : 16;
+    q.kcn = ntile % 64 == 0 ? 64 : ntile % 32 == 0 ? 32 : 16;
+    CUtensorMap mx, mdz;
+    if (!encode_act_map(&mx, x, d->cin, d->width, d->height, d->batch, x_stride, q.kcm) ||
+        !encode_act_map(&mdz, dz, d->cout, d->width, d->height, d->batch, dz_stride, q.kcn)) {
+      set_error("%s: tensor map encoding failed", fn);
+      return encode_tiled() ? SHY_ERR_INVALID_ARG : SHY_ERR_CUDA;
+    }
+    q.dw = dw;
+    q.batch = d->batch;
+    q.h = d->height;
+    q.w_ = d->width;
+    q.cin = d->cin;
+    q.cout = d->cout;
+    q.ks = d->ksize;
+    q.ntile = ntile;
+    q.tmem_cols = pow2_cols(ntile);
+    q.tiles_w = (d->width + kTileW - 1) / kTileW;
+    q.tiles_h = (d->height + kTileH - 1) / kTileH;
+    q.a_bytes = 256u * kTileM;                    // 128 / kcm boxes of 256 * kcm bytes
+    q.b_bytes = 256u * ntile;
+    q.stage_bytes = q.a_bytes + ((q.b_bytes + 1023u) & ~1023u);
+    q.la = q.kcm == 64 ? 2u : q.kcm == 32 ? 4u : 6u;
+    q.lb = q.kcn == 64 ? 2u : q.kcn == 32 ? 4u : 6u;
+    q.stages = 2;
+    // 16 KiB beyond the last stage: the MMAs' operand reads stay inside the
+    // allocation for either order of the descriptor's two strides
+    const int smem = smem_for((q.stages * (int)q.stage_bytes + 1024 + 16384) / 2, q.tmem_cols);
+    const long long tiles = (long long)d->batch * q.tiles_h * q.tiles_w;
+    const int ctas_mn = ((rows + kTileM - 1) / kTileM) * (d->cout / ntile);
+    long long splits = std::max(1ll, std::min(tiles, (2ll * 152 + ctas_mn - 1) / ctas_mn));
+    q.tiles_per_split = (tiles + splits - 1) / splits;
+    splits = (tiles + q.tiles_per_split - 1) / q.tiles_per_split;
+    static bool attr_w = false;
+    if (!attr_w) {
+      cudaFuncSetAttribute(wgrad_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      attr_w = true;
+    }
+    dim3 grid((unsigned)((rows + kTileM - 1) / kTileM), (unsigned)(d->cout / ntile), (unsigned)splits);
+    wgrad_tma_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(mx, mdz, q);
+    return launch_status(fn);
+  }
   ConvWgrad p{};
   p.x = static_cast<const __nv_bfloat16*>(x);
   p.dz = static_cast<const __nv_bfloat16*>(dz);
@@ -1080,7 +1278,6 @@ extern "C" int shy_sg_conv_wgrad(const shy_sg_conv_desc* d, const void* x, int32
   p.dzs = dz_stride;
   p.ntile = pick_ntile(d->cout);
   p.tmem_cols = pow2_cols(p.ntile);
-  const int rows = d->ksize * d->ksize * d->cin;
   const long long npix = (long long)d->batch * d->height * d->width;
   const long long nchunks = (npix + kWgradK - 1) / kWgradK;
   const int tiles = ((rows + kTileM - 1) / kTileM) * (d->cout / p.ntile);

@@ -116,7 +116,7 @@ def test_conv_forward_matches_oracle(sg, conv_path, case):
 
 
 @pytest.mark.parametrize("case", CONV_CASES)
-def test_weight_gradient_matches_oracle(sg, case):
+def test_weight_gradient_matches_oracle(sg, conv_path, case):
     B, H, W, ci, co, k, xs = case
     rng = np.random.default_rng(sum(case) + 1)
     x = so.bf16(rng.standard_normal((B, H, W, xs)))
