@@ -9,7 +9,7 @@ scatter, lrate blend and cascade.  One step = one erosion cycle
 dataset; the terrain recipe stands in for the reference's FastNoiseLite map.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload plain|batch|converge|large|surrogate]
+                  [--workload plain|batch|converge|large|surrogate|surrogate-step]
 
 `value` is device throughput with the maps resident in HBM; between timed
 steps the L2 is flushed by writing a 256 MiB buffer (untimed).  `e2e` is the
@@ -28,7 +28,8 @@ end-of-cycle pass over the whole step time.
 discharge (within 5 % log-L2 of the discharge after 4 x 500 cycles).
 
 `--workload surrogate` trains the learned warm-start on the device and
-compares the time to converged discharge with and without it.
+compares the time to converged discharge with and without it;
+`--workload surrogate-step` times its training step alone (TFLOP/s).
 
 `--workload large` runs the large-scale configuration: 8192^2, 4,194,304
 drops per cycle, per-cell vegetation every cycle.
@@ -537,7 +538,7 @@ def run_converge(args):
            "data": "synthetic (seeded value-noise terrain, counter-based spawns)",
            "config": {"workload": f"plain method, GPU batched: {n}x{n} value-noise terrain, {drops} drops/cycle",
                       "check_every_cycles": every},
-           "surrogate": "not built (no reference counterpart)"}
+           "surrogate": "compared in --workload surrogate"}
     if degenerate:
         out["degenerate"] = ("after %d cycles no cell is at height >= 0.1, so every spawn is skipped "
                              "(source/world.h:71) and the reference discharge D* has decayed to ~0" % args.ref_cycles)
@@ -708,6 +709,56 @@ def run_surrogate(args):
     print(json.dumps(out))
 
 
+def run_surrogate_step(args):
+    """Training throughput of the surrogate: one step = forward, loss,
+    backward and AdamW on a batch of 16 256^2 maps (seeded random heights
+    and targets; the kernels' work does not depend on the values).  FLOPs
+    are the convolutions' 2 x multiply-adds (forward, input and weight
+    gradients)."""
+    import torch
+
+    import simplehydrology_gb300 as shy
+    from simplehydrology_gb300 import build as shybuild
+    from simplehydrology_gb300 import surrogate as sg
+    shybuild.build()
+    batch, side = 16, 256
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    h = torch.rand((batch, side, side), device="cuda", generator=g)
+    t = torch.randn((batch, side, side, 3), device="cuda", generator=g)
+    net = sg.Surrogate(seed=SEED)
+    for _ in range(args.warmup):
+        net.train_step(h, t, 1e-4)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    launches0 = net.launches
+    with ClockSampler(torch.cuda.current_device()) as clock:
+        ev[0].record()
+        for _ in range(args.steps):
+            net.train_step(h, t, 1e-4)
+        ev[1].record()
+        torch.cuda.synchronize()
+    net.status()
+    ms = ev[0].elapsed_time(ev[1]) / args.steps
+    flops = batch * side * side * sg.flops_per_pixel(True)
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, src = float(json.load(f)["bf16_tflops_sustained"]), "measured (sustained)"
+    except Exception:
+        peak, src = 1700.0, "fallback (sustained)"
+    tf = flops / (ms / 1e3) / 1e12
+    print(json.dumps({
+        "metric": "surrogate training throughput", "value": tf, "unit": "TFLOP/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "dtype": "bf16 (f32 accumulate)", "data": "synthetic (seeded random heights and targets)",
+        "config": {"workload": "surrogate U-Net training step, 16 x 256x256 maps, AdamW",
+                   "params": sg.param_count(), "gflop_per_step": flops / 1e9},
+        "gpu_launches": (net.launches - launches0),
+        "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
+                     "peak_source": src, "kernel": "whole training step (convolutions 80 % of its time)",
+                     "traffic": None},
+        "clocks": clock.summary()}))
+
+
 def _initial_height(shy, seed, n):
     w = shy.World(n, n, seed=seed)
     w.generate(seed, 8)
@@ -729,7 +780,8 @@ def main():
     ap.add_argument("--drops", type=int, default=DROPS)
     ap.add_argument("--no-e2e", action="store_true")
     # the batched-terrain configuration (not the default bench line)
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "converge", "large", "surrogate"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "converge", "large", "surrogate",
+                                                              "surrogate-step"])
     ap.add_argument("--ref-cycles", type=int, default=2000)
     ap.add_argument("--check-every", type=int, default=10)
     ap.add_argument("--terrains", type=int, default=64)
@@ -747,6 +799,8 @@ def main():
         run_converge(args)
     elif args.workload == "surrogate":
         run_surrogate(args)
+    elif args.workload == "surrogate-step":
+        run_surrogate_step(args)
     else:
         run_ours(args)
 
