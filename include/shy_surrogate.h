@@ -77,9 +77,10 @@ int shy_sg_bias_grad(int64_t pixels, int32_t channels, const void* dz, int32_t d
                      float* db, void* stream);
 
 /* dz[pixel][c] = bf16(da * gelu'(z)); da, z: f32 with their own stride and
- * offset; dz: bf16, pixel stride `channels`.  If db is not NULL (channels
- * must then divide 256), db[c] += the sum of dz[.][c] over pixels as well:
- * the bias gradient of the convolution whose output gradient dz is. */
+ * offset (16-byte aligned, multiples of 4); dz: bf16, pixel stride
+ * `channels`, a multiple of 8 with channels / 8 dividing 256.  If db is not
+ * NULL, db[c] += the sum of dz[.][c] over pixels as well: the bias gradient
+ * of the convolution whose output gradient dz is. */
 int shy_sg_gelu_backward(int64_t pixels, int32_t channels, const float* da, int32_t da_stride,
                          int32_t da_offset, const float* z, int32_t z_stride, int32_t z_offset,
                          void* dz, float* db, void* stream);

@@ -794,20 +794,47 @@ __global__ void bias_grad_any_kernel(const __nv_bfloat16* __restrict__ dz, int d
   }
 }
 
-__global__ void __launch_bounds__(256) gelu_backward_kernel(long long n, int channels, const float* __restrict__ da,
+// One thread per (pixel, 8 channels): two 16-byte loads each of da and z,
+// one 16-byte store of dz.  Channel groups per pixel (channels / 8) divide
+// 256, so with a grid stride that is a multiple of 256 each thread keeps one
+// channel group and its 8 bias sums; the block adds them in shared memory.
+__global__ void __launch_bounds__(256) gelu_backward_kernel(int n8, int groups, const float* __restrict__ da,
                                                             int das, int dao, const float* __restrict__ z, int zs,
                                                             int zo, __nv_bfloat16* __restrict__ dz,
                                                             float* __restrict__ db) {
-  float acc = 0.0f;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long q = i / channels;
-    const int c = (int)(i - q * channels);
-    const __nv_bfloat16 v = __float2bfloat16_rn(da[q * das + dao + c] * gelu_grad(z[q * zs + zo + c]));
-    dz[i] = v;
-    acc += __bfloat162float(v);
+  float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += gridDim.x * blockDim.x) {
+    const int q = i / groups, c = (i - q * groups) * 8;
+    const float4* ap = reinterpret_cast<const float4*>(da + (long long)q * das + dao + c);
+    const float4* zp = reinterpret_cast<const float4*>(z + (long long)q * zs + zo + c);
+    const float4 a0 = ap[0], a1 = ap[1], z0 = zp[0], z1 = zp[1];
+    const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+    const float zv[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
+    float g[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      g[e] = __bfloat162float(__float2bfloat16_rn(av[e] * gelu_grad(zv[e])));
+      acc[e] += g[e];
+    }
+    uint4 o;
+    o.x = pack_bf16(g[0], g[1]);
+    o.y = pack_bf16(g[2], g[3]);
+    o.z = pack_bf16(g[4], g[5]);
+    o.w = pack_bf16(g[6], g[7]);
+    *reinterpret_cast<uint4*>(dz + (long long)i * 8) = o;
   }
-  if (db) flush_channel_sums(acc, channels, db);
+  if (!db) return;
+  __shared__ float red[8][256];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) red[e][threadIdx.x] = acc[e];
+  __syncthreads();
+  const int channels = groups * 8;
+  if ((int)threadIdx.x < channels) {
+    const int gi = threadIdx.x >> 3, e = threadIdx.x & 7;
+    float sum = 0.0f;
+    for (int t = gi; t < (int)blockDim.x; t += groups) sum += red[e][t];
+    atomicAdd(db + threadIdx.x, sum);
+  }
 }
 
 // one thread per (pooled pixel, 8-channel vector)
@@ -1316,15 +1343,17 @@ extern "C" int shy_sg_bias_grad(int64_t pixels, int32_t channels, const void* dz
 extern "C" int shy_sg_gelu_backward(int64_t pixels, int32_t channels, const float* da, int32_t da_stride,
                                     int32_t da_offset, const float* z, int32_t z_stride, int32_t z_offset,
                                     void* dz, float* db, void* stream) {
-  if (pixels <= 0 || channels <= 0 || !da || !z || !dz || da_offset < 0 || z_offset < 0 ||
-      da_offset + channels > da_stride || z_offset + channels > z_stride ||
-      (db && (channels > 256 || 256 % channels))) {
-    set_error("shy_sg_gelu_backward: bad arguments");
+  if (pixels <= 0 || channels <= 0 || channels % 8 || channels > 2048 || 256 % (channels / 8) || !da || !z ||
+      !dz || !aligned16(da) || !aligned16(z) || !aligned16(dz) || da_stride % 4 || da_offset % 4 ||
+      z_stride % 4 || z_offset % 4 || da_offset < 0 || z_offset < 0 || da_offset + channels > da_stride ||
+      z_offset + channels > z_stride || pixels * (channels / 8) >= (1ll << 31)) {
+    set_error("shy_sg_gelu_backward: bad arguments (channels a multiple of 8 with channels / 8 dividing 256; "
+              "16-byte aligned tensors, strides and offsets multiples of 4)");
     return SHY_ERR_INVALID_ARG;
   }
-  const long long n = pixels * channels;
-  gelu_backward_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      n, channels, da, da_stride, da_offset, z, z_stride, z_offset, static_cast<__nv_bfloat16*>(dz), db);
+  const long long n8 = pixels * (channels / 8);
+  gelu_backward_kernel<<<grid_for(n8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      (int)n8, channels / 8, da, da_stride, da_offset, z, z_stride, z_offset, static_cast<__nv_bfloat16*>(dz), db);
   return launch_status("shy_sg_gelu_backward");
 }
 
