@@ -54,6 +54,10 @@ int shy_sg_set_conv_path(int32_t path);
  * pipelines keep more loads in flight; shallower ones fit more CTAs on an
  * SM. */
 int shy_sg_set_conv_stages(int32_t stages);
+/* Pipeline of the TMA weight gradient (process-wide): pixels per stage (64
+ * or 128, a tile of 16 x 4 or 16 x 8) and stages (2..8); 0 for either (the
+ * default) chooses per convolution. */
+int shy_sg_set_wgrad_tile(int32_t pixels, int32_t stages);
 
 /* z = conv(x, w) + bias (bias may be NULL); written as f32 to `z` (may be
  * NULL) and as act(z) in bf16 to `a` (may be NULL).  x: bf16, pixel stride

@@ -115,8 +115,18 @@ def test_conv_forward_matches_oracle(sg, conv_path, case):
     assert np.all(ag[:, :ao] == 0) and np.all(ag[:, ao + co:] == 0)
 
 
+@pytest.fixture(params=[(0, 0), (64, 3), (128, 2)], ids=["auto", "64px", "128px"])
+def wgrad_tile(request, sg):
+    """The TMA weight gradient's pixel tiles and depths; the automatic choice is restored after."""
+    ok(lib().shy_sg_set_wgrad_tile(*request.param))
+    yield request.param
+    ok(lib().shy_sg_set_wgrad_tile(0, 0))
+
+
 @pytest.mark.parametrize("case", CONV_CASES)
-def test_weight_gradient_matches_oracle(sg, conv_path, case):
+def test_weight_gradient_matches_oracle(sg, conv_path, wgrad_tile, case):
+    if conv_path == 1 and wgrad_tile != (0, 0):
+        pytest.skip("the tile applies to the TMA path only")
     B, H, W, ci, co, k, xs = case
     rng = np.random.default_rng(sum(case) + 1)
     x = so.bf16(rng.standard_normal((B, H, W, xs)))
