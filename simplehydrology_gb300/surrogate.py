@@ -473,10 +473,12 @@ def train(net, heights, discharge, momx, momy, epochs, batch=16, lr=2e-3, seed=0
     rng = np.random.default_rng(seed)
     losses, step = [], 0
     for _ in range(epochs):
-        perm = rng.permutation(n)
+        # one upload per epoch: a per-step host-to-device copy would make the
+        # host wait for the device every step
+        perm = torch.from_numpy(rng.permutation(n)).to(net.dev)
         acc = torch.zeros(1, dtype=torch.float64, device=net.dev)
         for j in range(per_epoch):
-            idx = torch.from_numpy(perm[j * batch:(j + 1) * batch]).to(net.dev)
+            idx = perm[j * batch:(j + 1) * batch]
             h, t = H[idx], T[idx]
             if augment:
                 for axis, comp in ((1, 1), (2, 2)):

@@ -341,3 +341,24 @@ def test_trained_network_beats_the_method_without_it(sg):
     print({"loss_by_epoch": losses, "prediction": err, "mean_map": blind, "zero_maps": zero})
     assert losses[-1] < losses[0]
     assert err < blind < zero == 1.0
+
+
+def test_cpp_host_runs_the_c_abi(sg, tmp_path):
+    """tests/cpp/surrogate_conv.cpp: a C++ program (CUDA runtime for memory,
+    libshy for the kernels) runs a convolution and its weight gradient and
+    checks them against host loops."""
+    import os
+    import subprocess
+    from simplehydrology_gb300 import _capi
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.dirname(_capi.LIB_PATH)
+    cuda = "/usr/local/cuda"
+    exe = tmp_path / "surrogate_conv"
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(root, "include"), "-I" + cuda + "/include",
+                        os.path.join(root, "tests", "cpp", "surrogate_conv.cpp"), "-L" + libdir, "-lshy",
+                        "-L" + cuda + "/lib64", "-lcudart", "-Wl,-rpath," + libdir, "-Wl,-rpath," + cuda + "/lib64",
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.startswith("ok")

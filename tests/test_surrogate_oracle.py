@@ -171,3 +171,36 @@ def test_entry_points_validate_before_touching_a_device(shy):
     assert lib.shy_sg_pool_forward(1, 7, 8, 16, C.c_void_p(16), 16, 0, C.c_void_p(32), 16, 0,
                                    None) == shy._capi.SHY_ERR_INVALID_ARG
     assert "shy_sg_pool_forward" in lib.shy_last_error().decode()
+
+
+def test_unet_gradients_match_finite_differences():
+    """Central differences of the oracle's loss against its backward pass,
+    for a few weights and biases of the first, middle and last layers."""
+    params = so.init_params(9)
+    rng = np.random.default_rng(10)
+    x = so.features(rng.random((1, 16, 16)), {"height_mean": 0.5, "height_scale": 3.0, "slope_scale": 20.0})
+    target = rng.standard_normal((1, 16, 16, 3))
+
+    def loss_of(p):
+        net = so.Net(p)
+        return so.loss(net.forward(x), target, (1.0, 1.0, 1.0))[0]
+
+    net = so.Net(params)
+    zh = net.forward(x)
+    _, g = so.loss(zh, target, (1.0, 1.0, 1.0))
+    grads = net.backward(g)
+    eps = 1e-6
+    for name in ("enc0a", "mid", "dec1a", "head"):
+        w, b = params[name]
+        for idx in [tuple(rng.integers(0, n) for n in w.shape) for _ in range(3)]:
+            wp, wm = w.copy(), w.copy()
+            wp[idx] += eps
+            wm[idx] -= eps
+            fd = (loss_of({**params, name: (wp, b)}) - loss_of({**params, name: (wm, b)})) / (2 * eps)
+            assert fd == pytest.approx(grads[name][0][idx], rel=1e-5, abs=1e-9), (name, idx)
+        j = int(rng.integers(0, b.size))
+        bp, bm = b.copy(), b.copy()
+        bp[j] += eps
+        bm[j] -= eps
+        fd = (loss_of({**params, name: (w, bp)}) - loss_of({**params, name: (w, bm)})) / (2 * eps)
+        assert fd == pytest.approx(grads[name][1][j], rel=1e-5, abs=1e-9), (name, j)
