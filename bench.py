@@ -611,6 +611,7 @@ def run_surrogate(args):
     net = sg.Surrogate(seed=0, norm=norm)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     batch = 16
+    net.autotune(batch, 256, 256)
     launches0 = net.launches
     ev[0].record()
     losses = sg.train(net, H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr], epochs=args.epochs, batch=batch, lr=2e-3)
@@ -726,6 +727,7 @@ def run_surrogate_step(args):
     h = torch.rand((batch, side, side), device="cuda", generator=g)
     t = torch.randn((batch, side, side, 3), device="cuda", generator=g)
     net = sg.Surrogate(seed=SEED)
+    tuned = net.autotune(batch, side, side)
     for _ in range(args.warmup):
         net.train_step(h, t, 1e-4)
     torch.cuda.synchronize()
@@ -753,6 +755,7 @@ def run_surrogate_step(args):
         "config": {"workload": "surrogate U-Net training step, 16 x 256x256 maps, AdamW",
                    "params": sg.param_count(), "gflop_per_step": flops / 1e9},
         "gpu_launches": (net.launches - launches0),
+        "autotune": {f"{n}/{k}": f"{v[0]}px x{v[1]}" for (n, k), v in tuned.items()},
         "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
                      "peak_source": src, "kernel": "whole training step (convolutions 80 % of its time)",
                      "traffic": None},

@@ -33,10 +33,14 @@ extern "C" {
 
 /* Shape of one convolution: input and output share batch x height x width
  * (zero padding keeps the size); ksize is 1 or 3; cin and cout are
- * multiples of 16. */
+ * multiples of 16.  tile and stages tune the TMA pipeline for this call
+ * (0: the process-wide setting, see shy_sg_set_conv_tile and
+ * shy_sg_set_wgrad_tile): pixels per tile (forward 128 or 256, weight
+ * gradient 64 or 128) and stages (2..8). */
 typedef struct shy_sg_conv_desc {
   int32_t batch, height, width;
   int32_t cin, cout, ksize;
+  int32_t tile, stages;
 } shy_sg_conv_desc;
 
 #define SHY_SG_ACT_NONE 0
@@ -49,11 +53,12 @@ typedef struct shy_sg_conv_desc {
 #define SHY_SG_CONV_TMA 0
 #define SHY_SG_CONV_STAGED 1
 int shy_sg_set_conv_path(int32_t path);
-/* Depth of the TMA pipeline, 2..8 stages of one channel chunk each, or 0
- * (the default) to choose per convolution (process-wide).  Deeper
- * pipelines keep more loads in flight; shallower ones fit more CTAs on an
- * SM. */
-int shy_sg_set_conv_stages(int32_t stages);
+/* Tile and depth of the TMA pipeline (process-wide): pixels per tile (128,
+ * or 256 with two accumulators sharing each weight chunk) and stages
+ * (2..8, one channel chunk each); 0 for either (the default) chooses per
+ * convolution.  Deeper pipelines keep more loads in flight; shallower ones
+ * fit more CTAs on an SM. */
+int shy_sg_set_conv_tile(int32_t pixels, int32_t stages);
 /* Pipeline of the TMA weight gradient (process-wide): pixels per stage (64
  * or 128, a tile of 16 x 4 or 16 x 8) and stages (2..8); 0 for either (the
  * default) chooses per convolution. */

@@ -89,7 +89,8 @@ class ShyError(RuntimeError):
 
 class SgConvDesc(C.Structure):
     _fields_ = [("batch", C.c_int32), ("height", C.c_int32), ("width", C.c_int32),
-                ("cin", C.c_int32), ("cout", C.c_int32), ("ksize", C.c_int32)]
+                ("cin", C.c_int32), ("cout", C.c_int32), ("ksize", C.c_int32),
+                ("tile", C.c_int32), ("stages", C.c_int32)]
 
 
 class SgAdamw(C.Structure):
@@ -180,7 +181,7 @@ SIGNATURES = {
     "shy_sg_loss": (C.c_int, [C.c_int64, W, C.c_int32, W, FP, W, W, W]),
     "shy_sg_decode": (C.c_int, [C.c_int64, W, C.c_int32, P(SgNorm), W, W, W, W]),
     "shy_sg_set_conv_path": (C.c_int, [C.c_int32]),
-    "shy_sg_set_conv_stages": (C.c_int, [C.c_int32]),
+    "shy_sg_set_conv_tile": (C.c_int, [C.c_int32, C.c_int32]),
     "shy_sg_set_wgrad_tile": (C.c_int, [C.c_int32, C.c_int32]),
     "shy_sg_status": (C.c_int, []),
 }

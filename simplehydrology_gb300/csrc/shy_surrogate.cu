@@ -336,7 +336,7 @@ struct ConvTma {
   __nv_bfloat16* a;
   int batch, h, w_, cin, cout, ks;
   int zs, zo, as, ao, act;
-  int ntile, kc, tmem_cols, tiles_w, tiles_h, stages;
+  int ntile, kc, tmem_cols, tiles_w, tiles_h, stages, mt;  // mt: 128-pixel sub-tiles (1 or 2)
   uint32_t a_bytes, b_bytes, stage_bytes, layout;
 };
 
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
   const int tx = t % p.tiles_w;
   t /= p.tiles_w;
   const int ty = t % p.tiles_h, b = t / p.tiles_h;
-  const int x0 = tx * kTileW, y0 = ty * kTileH;
+  const int x0 = tx * kTileW, y0 = ty * kTileH * p.mt;
   const int n0 = blockIdx.y * p.ntile;
 
   if (warp == 0) tmem_alloc(&tmem_slot, p.tmem_cols);
@@ -407,6 +407,7 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
+  const uint32_t sub_bytes = (uint32_t)kTileM * p.kc * 2;  // one 128-pixel sub-tile of A
 
   if (tid == 0) {
     const int taps = p.ks * p.ks, half = p.ks >> 1;
@@ -435,9 +436,12 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
       consumed = it + 1;
       tc_fence_after();
       const uint32_t sa = base + s * p.stage_bytes, sb = sa + p.a_bytes;
+      // each 128-pixel sub-tile has its own accumulator (ntile columns apart)
+      // and shares the stage's weights
       for (int kk = 0; kk < (p.kc >> 4); ++kk)
-        mma_bf16(tmem, smem_desc_sw(sa + kk * 32, sbo, p.layout), smem_desc_sw(sb + kk * 32, sbo, p.layout), idesc,
-                 (it | kk) != 0);
+        for (int u = 0; u < p.mt; ++u)
+          mma_bf16(tmem + (uint32_t)(u * p.ntile), smem_desc_sw(sa + u * sub_bytes + kk * 32, sbo, p.layout),
+                   smem_desc_sw(sb + kk * 32, sbo, p.layout), idesc, (it | kk) != 0);
       mma_commit(&empty[s]);
       if (issued < iters) {
         const int s2 = issued % S;
@@ -458,31 +462,33 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
   const bool ok = __syncthreads_and(fin) != 0 && s_fail == 0;
   if (ok) {
     tc_fence_after();
-    const int y = y0 + (tid >> 4), x = x0 + (tid & 15);
-    const bool valid = y < p.h && x < p.w_;
-    const long long q = ((long long)b * p.h + y) * p.w_ + x;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int nc = 0; nc < p.ntile; nc += 8) {
-      float v[8];
-      tmem_ld8(lane_base + (uint32_t)nc, v);
-      if (!valid) continue;
-      const int n = n0 + nc;
-      if (p.bias)
-        for (int j = 0; j < 8; ++j) v[j] += __ldg(p.bias + n + j);
-      if (p.z) {
-        float4* zp = reinterpret_cast<float4*>(p.z + q * p.zs + p.zo + n);
-        zp[0] = make_float4(v[0], v[1], v[2], v[3]);
-        zp[1] = make_float4(v[4], v[5], v[6], v[7]);
-      }
-      if (p.a) {
-        if (p.act == SHY_SG_ACT_GELU)
-          for (int j = 0; j < 8; ++j) v[j] = gelu(v[j]);
-        uint4 o;
-        o.x = pack_bf16(v[0], v[1]);
-        o.y = pack_bf16(v[2], v[3]);
-        o.z = pack_bf16(v[4], v[5]);
-        o.w = pack_bf16(v[6], v[7]);
-        *reinterpret_cast<uint4*>(p.a + q * p.as + p.ao + n) = o;
+    for (int u = 0; u < p.mt; ++u) {
+      const int y = y0 + u * kTileH + (tid >> 4), x = x0 + (tid & 15);
+      const bool valid = y < p.h && x < p.w_;
+      const long long q = ((long long)b * p.h + y) * p.w_ + x;
+      const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(u * p.ntile);
+      for (int nc = 0; nc < p.ntile; nc += 8) {
+        float v[8];
+        tmem_ld8(lane_base + (uint32_t)nc, v);
+        if (!valid) continue;
+        const int n = n0 + nc;
+        if (p.bias)
+          for (int j = 0; j < 8; ++j) v[j] += __ldg(p.bias + n + j);
+        if (p.z) {
+          float4* zp = reinterpret_cast<float4*>(p.z + q * p.zs + p.zo + n);
+          zp[0] = make_float4(v[0], v[1], v[2], v[3]);
+          zp[1] = make_float4(v[4], v[5], v[6], v[7]);
+        }
+        if (p.a) {
+          if (p.act == SHY_SG_ACT_GELU)
+            for (int j = 0; j < 8; ++j) v[j] = gelu(v[j]);
+          uint4 o;
+          o.x = pack_bf16(v[0], v[1]);
+          o.y = pack_bf16(v[2], v[3]);
+          o.z = pack_bf16(v[4], v[5]);
+          o.w = pack_bf16(v[6], v[7]);
+          *reinterpret_cast<uint4*>(p.a + q * p.as + p.ao + n) = o;
+        }
       }
     }
   } else if (tid == 0) {
@@ -1048,6 +1054,7 @@ int smem_for(int stage_bytes, int tmem_cols) {
 
 int g_conv_path = SHY_SG_CONV_TMA;
 int g_conv_stages = 0;  // 0: chosen per convolution
+int g_conv_pixels = 0;  // pixels per tile, 128 or 256; 0: chosen per convolution
 int g_wgrad_pixels = 0, g_wgrad_stages = 0;  // 0: chosen per convolution
 
 // cuTensorMapEncodeTiled from the driver, looked up once through the runtime.
@@ -1091,10 +1098,10 @@ bool encode_act_map(CUtensorMap* m, const void* ptr, int channels, int width, in
 
 // Tensor maps of one convolution: the input (encode_act_map) and the
 // weights as (taps * cin, cout) with a box of kc x ntile.
-bool encode_conv_maps(const shy_sg_conv_desc* d, const void* x, int xs, const void* w, int kc, int ntile,
+bool encode_conv_maps(const shy_sg_conv_desc* d, const void* x, int xs, const void* w, int kc, int ntile, int mt,
                       CUtensorMap* mx, CUtensorMap* mw) {
   auto fn = encode_tiled();
-  if (!fn || !encode_act_map(mx, x, d->cin, d->width, d->height, d->batch, xs, kc)) return false;
+  if (!fn || !encode_act_map(mx, x, d->cin, d->width, d->height, d->batch, xs, kc, kTileH * mt)) return false;
   const cuuint64_t k = (cuuint64_t)d->ksize * d->ksize * d->cin;
   const cuuint64_t gw[2] = {k, (cuuint64_t)d->cout};
   const cuuint64_t sw2[1] = {k * 2};
@@ -1111,7 +1118,8 @@ bool check_conv_desc(const shy_sg_conv_desc* d, const char* fn) {
     return false;
   }
   if (d->batch <= 0 || d->height <= 0 || d->width <= 0 || d->cin <= 0 || d->cout <= 0 ||
-      d->cin % 16 || d->cout % 16 || (d->ksize != 1 && d->ksize != 3)) {
+      d->cin % 16 || d->cout % 16 || (d->ksize != 1 && d->ksize != 3) ||
+      (d->stages != 0 && (d->stages < 2 || d->stages > kMaxStages))) {
     set_error("%s: bad shape %dx%dx%d cin %d cout %d ksize %d", fn, d->batch, d->height, d->width, d->cin,
               d->cout, d->ksize);
     return false;
@@ -1154,7 +1162,14 @@ extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int
   const int ntile = pick_ntile(d->cout);
   const int kc = d->cin % 64 == 0 ? 64 : d->cin % 32 == 0 ? 32 : 16;
   CUtensorMap mx, mw;
-  if (g_conv_path == SHY_SG_CONV_TMA && encode_conv_maps(d, x, x_stride, w, kc, ntile, &mx, &mw)) {
+  // tile: the call's own choice, else the process-wide one, else 128 pixels
+  if (d->tile != 0 && d->tile != 128 && d->tile != 256) {
+    set_error("%s: tile %d (0, 128 or 256 pixels)", fn, d->tile);
+    return SHY_ERR_INVALID_ARG;
+  }
+  const int pix = d->tile ? d->tile : g_conv_pixels;
+  const int mt = pix ? pix / kTileM : 1;
+  if (g_conv_path == SHY_SG_CONV_TMA && encode_conv_maps(d, x, x_stride, w, kc, ntile, mt, &mx, &mw)) {
     ConvTma p{};
     p.bias = bias;
     p.z = z;
@@ -1172,10 +1187,11 @@ extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int
     p.act = act;
     p.ntile = ntile;
     p.kc = kc;
-    p.tmem_cols = pow2_cols(ntile);
+    p.mt = mt;
+    p.tmem_cols = pow2_cols(ntile * mt);
     p.tiles_w = (d->width + kTileW - 1) / kTileW;
-    p.tiles_h = (d->height + kTileH - 1) / kTileH;
-    p.a_bytes = (uint32_t)kTileM * kc * 2;
+    p.tiles_h = (d->height + kTileH * mt - 1) / (kTileH * mt);
+    p.a_bytes = (uint32_t)kTileM * mt * kc * 2;
     p.b_bytes = (uint32_t)ntile * kc * 2;
     p.stage_bytes = p.a_bytes + ((p.b_bytes + 1023u) & ~1023u);
     p.layout = kc == 64 ? 2u : kc == 32 ? 4u : 6u;
@@ -1183,7 +1199,8 @@ extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int
     // else 2 (measured at the training shapes: 543 vs 476 TFLOP/s on the
     // 384 -> 128 layer, 269 vs 242 on 96 -> 32)
     const int iters = d->ksize * d->ksize * (d->cin / kc);
-    const int want = g_conv_stages ? g_conv_stages : (kc == 64 && iters >= 16 ? 3 : 2);
+    const int st = d->stages ? d->stages : g_conv_stages;
+    const int want = st ? st : (kc == 64 && iters >= 16 && mt == 1 ? 3 : 2);
     p.stages = std::max(2, std::min(want, (200 * 1024 - 1024) / (int)p.stage_bytes));
     const int smem = smem_for((p.stages * (int)p.stage_bytes + 1024) / 2, p.tmem_cols);
     static bool attr_tma = false;
@@ -1259,7 +1276,12 @@ extern "C" int shy_sg_conv_wgrad(const shy_sg_conv_desc* d, const void* x, int32
     // 192 -> 64 layer at 128^2), else 128
     const long long npix = (long long)d->batch * d->width * d->height;
     const int ctas_mn = ((rows + kTileM - 1) / kTileM) * (d->cout / ntile);
-    const int pixels = g_wgrad_pixels ? g_wgrad_pixels : (npix < (1ll << 19) && ctas_mn < 16 ? 64 : 128);
+    if (d->tile != 0 && d->tile != 64 && d->tile != 128) {
+      set_error("%s: tile %d (0, 64 or 128 pixels)", fn, d->tile);
+      return SHY_ERR_INVALID_ARG;
+    }
+    const int pix = d->tile ? d->tile : g_wgrad_pixels;
+    const int pixels = pix ? pix : (npix < (1ll << 19) && ctas_mn < 16 ? 64 : 128);
     q.box_h = pixels / kTileW;
     if (!encode_act_map(&mx, x, d->cin, d->width, d->height, d->batch, x_stride, q.kcm, q.box_h) ||
         !encode_act_map(&mdz, dz, d->cout, d->width, d->height, d->batch, dz_stride, q.kcn, q.box_h)) {
@@ -1282,7 +1304,8 @@ extern "C" int shy_sg_conv_wgrad(const shy_sg_conv_desc* d, const void* x, int32
     q.stage_bytes = q.a_bytes + ((q.b_bytes + 1023u) & ~1023u);
     q.la = q.kcm == 64 ? 2u : q.kcm == 32 ? 4u : 6u;
     q.lb = q.kcn == 64 ? 2u : q.kcn == 32 ? 4u : 6u;
-    q.stages = std::max(2, std::min(g_wgrad_stages ? g_wgrad_stages : 2, (200 * 1024 - 1024 - 16384) / (int)q.stage_bytes));
+    const int st = d->stages ? d->stages : g_wgrad_stages;
+    q.stages = std::max(2, std::min(st ? st : 2, (200 * 1024 - 1024 - 16384) / (int)q.stage_bytes));
     // 16 KiB beyond the last stage: the MMAs' operand reads stay inside the
     // allocation for either order of the descriptor's two strides
     const int smem = smem_for((q.stages * (int)q.stage_bytes + 1024 + 16384) / 2, q.tmem_cols);
@@ -1511,11 +1534,13 @@ extern "C" int shy_sg_set_conv_path(int32_t path) {
   return SHY_OK;
 }
 
-extern "C" int shy_sg_set_conv_stages(int32_t stages) {
-  if (stages != 0 && (stages < 2 || stages > kMaxStages)) {
-    set_error("shy_sg_set_conv_stages: %d stages (0 or 2..%d)", stages, kMaxStages);
+extern "C" int shy_sg_set_conv_tile(int32_t pixels, int32_t stages) {
+  if ((pixels != 0 && pixels != 128 && pixels != 256) || (stages != 0 && (stages < 2 || stages > kMaxStages))) {
+    set_error("shy_sg_set_conv_tile: %d pixels (0, 128 or 256), %d stages (0 or 2..%d)", pixels, stages,
+              kMaxStages);
     return SHY_ERR_INVALID_ARG;
   }
+  g_conv_pixels = pixels;
   g_conv_stages = stages;
   return SHY_OK;
 }

@@ -53,6 +53,11 @@ LAYERS = (
 )
 CHANNELS = (32, 64, 128, 256)
 ACT_NONE, ACT_GELU = 0, 1
+LEVEL = {"enc0a": 0, "enc0b": 0, "enc1a": 1, "enc1b": 1, "enc2a": 2, "enc2b": 2, "mid": 3,
+         "dec2a": 2, "dec2b": 2, "dec1a": 1, "dec1b": 1, "dec0a": 0, "dec0b": 0, "head": 0}
+# TMA pipeline candidates (pixels per tile, stages) the autotuner times
+CONV_TILES = ((128, 2), (128, 3), (256, 2), (256, 3))
+WGRAD_TILES = ((64, 2), (64, 3), (128, 2), (128, 3))
 
 
 def _torch():
@@ -192,6 +197,7 @@ class Surrogate:
         self._ws = {}
         self._prepped = False
         self.launches = 0
+        self.tune = {}  # (layer, "fwd" | "dgrad" | "wgrad") -> (pixels per tile, stages)
 
     # -- plumbing ---------------------------------------------------------
     def _stream(self):
@@ -221,10 +227,20 @@ class Surrogate:
                        self._p(L["wb"]), self._p(L["wf"]))
         self._prepped = True
 
-    def _conv(self, ws, name, level, x, xs, z, zs, zo, a, as_, ao, act):
+    def _desc(self, ws, name, kind):
+        """Convolution descriptor of one layer's forward ("fwd"), input
+        gradient ("dgrad", channels swapped) or weight gradient ("wgrad"),
+        with the autotuned tile if there is one."""
         L = self.layers[name]
         B, H, W = ws.shape
-        d = SgConvDesc(B, H >> level, W >> level, L["cin"], L["cout"], L["k"])
+        lv = LEVEL[name]
+        ci, co = (L["cout"], L["cin"]) if kind == "dgrad" else (L["cin"], L["cout"])
+        tile, stages = self.tune.get((name, kind), (0, 0))
+        return SgConvDesc(B, H >> lv, W >> lv, ci, co, L["k"], tile, stages)
+
+    def _conv(self, ws, name, level, x, xs, z, zs, zo, a, as_, ao, act):
+        L = self.layers[name]
+        d = self._desc(ws, name, "fwd")
         self._call("shy_sg_conv_forward", C.byref(d), self._p(x), xs, self._p(L["wb"]),
                    self._p(self.params, L["b"]), self._p(z), zs, zo, self._p(a), as_, ao, act)
 
@@ -276,15 +292,14 @@ class Surrogate:
         backward that made dz adds it otherwise); its input gradient into dx
         (f32, pixel stride dxs) unless dx is None."""
         L = self.layers[name]
-        B, H, W = ws.shape
-        d = SgConvDesc(B, H >> level, W >> level, L["cin"], L["cout"], L["k"])
+        d = self._desc(ws, name, "wgrad")
         self._call("shy_sg_conv_wgrad", C.byref(d), self._p(x_in), xs, self._p(dz), L["cout"],
                    self._p(self.grads, L["w"]))
         if bias:
             self._call("shy_sg_bias_grad", d.batch * d.height * d.width, L["cout"], self._p(dz), L["cout"],
                        self._p(self.grads, L["b"]))
         if dx is not None:
-            dd = SgConvDesc(d.batch, d.height, d.width, L["cout"], L["cin"], L["k"])
+            dd = self._desc(ws, name, "dgrad")
             self._call("shy_sg_conv_forward", C.byref(dd), self._p(dz), L["cout"], self._p(L["wf"]), None,
                        self._p(dx), dxs, 0, None, 0, 0, ACT_NONE)
 
@@ -343,6 +358,65 @@ class Surrogate:
         self._layer_bwd(ws, "enc0b", 0, ws.a["enc0a"], c0, dz[0], da[0], c0)
         self._gelu_bwd(ws, 0, c0, da[0], c0, 0, "enc0a")
         self._layer_bwd(ws, "enc0a", 0, ws.x0, IN_CH, dz[0], None, 0)
+
+    # -- autotuning ---------------------------------------------------------
+    def _layer_inputs(self, ws):
+        """Each convolution's input tensor in the workspace and its pixel stride."""
+        c0, c1, c2, c3 = CHANNELS
+        return {"enc0a": (ws.x0, IN_CH), "enc0b": (ws.a["enc0a"], c0), "enc1a": (ws.pool[1], c0),
+                "enc1b": (ws.a["enc1a"], c1), "enc2a": (ws.pool[2], c1), "enc2b": (ws.a["enc2a"], c2),
+                "mid": (ws.pool[3], c2), "dec2a": (ws.cat[2], 3 * c2), "dec2b": (ws.a["dec2a"], c2),
+                "dec1a": (ws.cat[1], 3 * c1), "dec1b": (ws.a["dec1a"], c1), "dec0a": (ws.cat[0], 3 * c0),
+                "dec0b": (ws.a["dec0a"], c0), "head": (ws.a["dec0b"], c0)}
+
+    def autotune(self, B, H, W, reps=5):
+        """Time every TMA tile candidate for each layer's forward, input- and
+        weight-gradient convolution at this batch shape (CUDA events, scratch
+        outputs) and keep the fastest for later calls.  Returns
+        {(layer, kind): (pixels, stages, ms)}."""
+        torch = self.torch
+        if not self._prepped:
+            self.prep_weights()
+        ws = self.workspace(B, H, W, True)
+        ins = self._layer_inputs(ws)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        stream = torch.cuda.current_stream(self.dev)
+        out = {}
+        for name, ci, co, k in LAYERS:
+            P = ws.P[LEVEL[name]]
+            L = self.layers[name]
+            x, xs = ins[name]
+            dz = torch.zeros((P, co), dtype=torch.bfloat16, device=self.dev)
+            zf = torch.empty((P, max(ci, co)), dtype=torch.float32, device=self.dev)
+            gw = torch.zeros(L["nw"], dtype=torch.float32, device=self.dev)
+            kinds = ("fwd", "wgrad") if name == "enc0a" else ("fwd", "dgrad", "wgrad")
+            for kind in kinds:
+                best = None
+                for tile, stages in (WGRAD_TILES if kind == "wgrad" else CONV_TILES):
+                    self.tune[(name, kind)] = (tile, stages)
+                    d = self._desc(ws, name, kind)
+                    if kind == "fwd":
+                        fn = lambda: self._call("shy_sg_conv_forward", C.byref(d), self._p(x), xs,  # noqa: E731
+                                                self._p(L["wb"]), None, self._p(zf), co, 0, None, 0, 0, ACT_NONE)
+                    elif kind == "dgrad":
+                        fn = lambda: self._call("shy_sg_conv_forward", C.byref(d), self._p(dz), co,  # noqa: E731
+                                                self._p(L["wf"]), None, self._p(zf), ci, 0, None, 0, 0, ACT_NONE)
+                    else:
+                        fn = lambda: self._call("shy_sg_conv_wgrad", C.byref(d), self._p(x), xs,  # noqa: E731
+                                                self._p(dz), co, self._p(gw))
+                    fn()
+                    ev[0].record(stream)
+                    for _ in range(reps):
+                        fn()
+                    ev[1].record(stream)
+                    ev[1].synchronize()
+                    ms = ev[0].elapsed_time(ev[1]) / reps
+                    if best is None or ms < best[2]:
+                        best = (tile, stages, ms)
+                self.tune[(name, kind)] = best[:2]
+                out[(name, kind)] = best
+        self.status()
+        return out
 
     # -- training -----------------------------------------------------------
     def loss_and_grads(self, ws, weights=(1.0, 1.0, 1.0)):

@@ -88,8 +88,18 @@ def conv_path(request, sg):
     ok(lib().shy_sg_set_conv_path(0))
 
 
+@pytest.fixture(params=[(0, 0), (256, 2), (256, 3), (128, 4)], ids=["auto", "256px2", "256px3", "128px4"])
+def conv_tile(request, sg):
+    """The TMA convolution's pixel tiles and depths; the automatic choice is restored after."""
+    ok(lib().shy_sg_set_conv_tile(*request.param))
+    yield request.param
+    ok(lib().shy_sg_set_conv_tile(0, 0))
+
+
 @pytest.mark.parametrize("case", CONV_CASES)
-def test_conv_forward_matches_oracle(sg, conv_path, case):
+def test_conv_forward_matches_oracle(sg, conv_path, conv_tile, case):
+    if conv_path == 1 and conv_tile != (0, 0):
+        pytest.skip("the tile applies to the TMA path only")
     B, H, W, ci, co, k, xs = case
     rng = np.random.default_rng(sum(case))
     x = so.bf16(rng.standard_normal((B, H, W, xs)))
@@ -362,3 +372,21 @@ def test_cpp_host_runs_the_c_abi(sg, tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.startswith("ok")
+
+
+def test_autotune_picks_a_tile_per_call(sg):
+    """The autotuner times the candidates of every convolution call and the
+    step afterwards runs on its choices (each candidate's numerics are
+    checked above)."""
+    net = sg.Surrogate(seed=4, norm=sg.Norm(0.5, 3.0, 20.0))
+    tuned = net.autotune(2, 32, 32, reps=2)
+    assert len(tuned) == 3 * len(sg.LAYERS) - 1
+    for (name, kind), (tile, stages, ms) in tuned.items():
+        assert (tile, stages) in (sg.WGRAD_TILES if kind == "wgrad" else sg.CONV_TILES)
+        assert ms > 0
+        assert net.tune[(name, kind)] == (tile, stages)
+    h = torch.rand((2, 32, 32), device="cuda")
+    t = torch.randn((2, 32, 32, 3), device="cuda")
+    loss = float(net.train_step(h, t, 1e-3).item())
+    net.status()
+    assert np.isfinite(loss)
