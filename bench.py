@@ -604,8 +604,12 @@ def run_surrogate(args):
     clock = ClockSampler(torch.cuda.current_device())
     clock.__enter__()
     horizon, theta, n_tr, n_val = args.horizon, 0.05, args.train_terrains, 64
+    side = args.train_side
+    if side != 256:  # fewer, larger terrains, trained on random 256^2 crops
+        n_tr, n_val = max(1, n_tr * 256 * 256 // (side * side)), max(1, 64 * 256 * 256 // (side * side))
     t0 = time.perf_counter()
-    H, D, MX, MY = sg.make_pairs(n_tr + n_val, size=256, cycles=horizon, seed0=10000)
+    H, D, MX, MY = sg.make_pairs(n_tr + n_val, size=side, cycles=horizon, seed0=10000,
+                                 per_launch=max(16, 64 * 256 * 256 // (side * side)))
     gen_s = time.perf_counter() - t0
     norm = sg.Norm.fit(H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr])
     net = sg.Surrogate(seed=0, norm=norm)
@@ -614,12 +618,13 @@ def run_surrogate(args):
     net.autotune(batch, 256, 256)
     launches0 = net.launches
     ev[0].record()
-    losses = sg.train(net, H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr], epochs=args.epochs, batch=batch, lr=2e-3)
+    losses = sg.train(net, H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr], epochs=args.epochs, batch=batch, lr=2e-3,
+                      crop=256 if side != 256 else None, steps_per_epoch=args.train_terrains // batch)
     ev[1].record()
     torch.cuda.synchronize()
     net.status()
     train_ms = ev[0].elapsed_time(ev[1])
-    steps = args.epochs * (n_tr // batch)
+    steps = args.epochs * (args.train_terrains // batch)
     train_flops = steps * batch * 256 * 256 * sg.flops_per_pixel(True)
     # held-out 256^2 pairs: the prediction against the particle method's maps
     val_pred, _, _ = net.predict(torch.from_numpy(H[n_tr:]).cuda())
@@ -696,7 +701,7 @@ def run_surrogate(args):
            "config": {"workload": "learned warm-start: U-Net (1.36 M parameters, 4 levels, channels 32-256) "
                                   "trained on 256x256 terrains, evaluated on 1024x1024 at 65536 drops/cycle",
                       "horizon_cycles": horizon, "threshold": theta, "window_cycles": 10,
-                      "train_terrains": n_tr, "epochs": args.epochs, "batch": batch},
+                      "train_terrains": n_tr, "train_side": side, "epochs": args.epochs, "batch": batch},
            "training": {"pairs_s": gen_s, "train_s": train_ms / 1e3, "steps": steps,
                         "tflops": train_flops / (train_ms / 1e3) / 1e12,
                         "loss_by_epoch": [round(v, 5) for v in losses],
@@ -793,6 +798,7 @@ def main():
     ap.add_argument("--train-terrains", type=int, default=2048)
     ap.add_argument("--epochs", type=int, default=24)
     ap.add_argument("--eval-terrains", type=int, default=2)
+    ap.add_argument("--train-side", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

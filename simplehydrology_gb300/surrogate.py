@@ -530,30 +530,41 @@ def make_pairs(n, size=256, drops=None, cycles=50, seed0=10000, per_launch=64, p
     return tuple(out)
 
 
-def train(net, heights, discharge, momx, momy, epochs, batch=16, lr=2e-3, seed=0, augment=True):
+def train(net, heights, discharge, momx, momy, epochs, batch=16, lr=2e-3, seed=0, augment=True, crop=None,
+          steps_per_epoch=None):
     """AdamW over the pairs with a cosine learning-rate schedule.  With
     `augment`, each batch is flipped along either axis at random (discharge
     is unchanged and the momentum component along a flipped axis changes
-    sign; a world's x-major map is an image with rows = x).  Returns the
-    mean loss of each epoch."""
+    sign; a world's x-major map is an image with rows = x).  With `crop`,
+    each sample is a random crop x crop window of its map (offsets multiples
+    of 8), and an epoch is `steps_per_epoch` batches.  Returns the mean loss
+    of each epoch."""
     torch = net.torch
     H = torch.from_numpy(np.ascontiguousarray(heights, np.float32)).to(net.dev)
     T = torch.from_numpy(net.norm.targets(discharge, momx, momy)).to(net.dev)
     sign = torch.tensor(net.norm.out_mean, dtype=torch.float32, device=net.dev)
     scale = torch.tensor(net.norm.out_scale, dtype=torch.float32, device=net.dev)
-    n = H.shape[0]
-    per_epoch = max(1, n // batch)
+    n, side = H.shape[0], H.shape[-1]
+    per_epoch = steps_per_epoch or max(1, n // batch)
     total = epochs * per_epoch
     rng = np.random.default_rng(seed)
     losses, step = [], 0
     for _ in range(epochs):
         # one upload per epoch: a per-step host-to-device copy would make the
         # host wait for the device every step
-        perm = torch.from_numpy(rng.permutation(n)).to(net.dev)
+        order = np.concatenate([rng.permutation(n) for _ in range((per_epoch * batch + n - 1) // n)])
+        perm = torch.from_numpy(order).to(net.dev)
         acc = torch.zeros(1, dtype=torch.float64, device=net.dev)
         for j in range(per_epoch):
             idx = perm[j * batch:(j + 1) * batch]
-            h, t = H[idx], T[idx]
+            if crop and crop < side:
+                offs = rng.integers(0, (side - crop) // 8 + 1, size=(batch, 2)) * 8
+                h = torch.stack([H[int(order[j * batch + i])][oy:oy + crop, ox:ox + crop]
+                                 for i, (oy, ox) in enumerate(offs)])
+                t = torch.stack([T[int(order[j * batch + i])][oy:oy + crop, ox:ox + crop]
+                                 for i, (oy, ox) in enumerate(offs)])
+            else:
+                h, t = H[idx], T[idx]
             if augment:
                 for axis, comp in ((1, 1), (2, 2)):
                     if rng.random() < 0.5:
