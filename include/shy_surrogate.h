@@ -46,12 +46,18 @@ typedef struct shy_sg_conv_desc {
 #define SHY_SG_ACT_NONE 0
 #define SHY_SG_ACT_GELU 1 /* 0.5 z (1 + erf(z / sqrt 2)) */
 
-/* How shy_sg_conv_forward stages its operands (process-wide):
- * SHY_SG_CONV_TMA     tensor-memory-accelerator copies into a four-stage
- *                     pipeline (the default);
- * SHY_SG_CONV_STAGED  loads by the CTA's threads into two stages. */
+/* How the convolutions stage their operands (process-wide):
+ * SHY_SG_CONV_TMA         tensor-memory-accelerator copies into a 2- to
+ *                         8-stage pipeline, one CTA per tile (the default);
+ * SHY_SG_CONV_STAGED      loads by the CTA's threads into two stages;
+ * SHY_SG_CONV_PERSISTENT  the TMA pipeline in a persistent CTA per SM with
+ *                         separate load, MMA and epilogue warps and two
+ *                         accumulators, so one tile's epilogue runs under
+ *                         the next tile's main loop (forward and input
+ *                         gradient; the weight gradient runs as with TMA). */
 #define SHY_SG_CONV_TMA 0
 #define SHY_SG_CONV_STAGED 1
+#define SHY_SG_CONV_PERSISTENT 2
 int shy_sg_set_conv_path(int32_t path);
 /* Tile and depth of the TMA pipeline (process-wide): pixels per tile (128,
  * or 256 with two accumulators sharing each weight chunk) and stages

@@ -377,6 +377,28 @@ __device__ __forceinline__ uint64_t smem_desc_mn(uint32_t addr, uint32_t lbo, ui
          (1ull << 46) | ((uint64_t)layout << 61);
 }
 
+// Epilogue of the TMA convolutions: 8 accumulator columns of one pixel,
+// plus bias, to f32 and/or bf16 (GELU'd) outputs.
+__device__ __forceinline__ void store_out8(const ConvTma& p, long long q, int n, float v[8]) {
+  if (p.bias)
+    for (int j = 0; j < 8; ++j) v[j] += __ldg(p.bias + n + j);
+  if (p.z) {
+    float4* zp = reinterpret_cast<float4*>(p.z + q * p.zs + p.zo + n);
+    zp[0] = make_float4(v[0], v[1], v[2], v[3]);
+    zp[1] = make_float4(v[4], v[5], v[6], v[7]);
+  }
+  if (p.a) {
+    if (p.act == SHY_SG_ACT_GELU)
+      for (int j = 0; j < 8; ++j) v[j] = gelu(v[j]);
+    uint4 o;
+    o.x = pack_bf16(v[0], v[1]);
+    o.y = pack_bf16(v[2], v[3]);
+    o.z = pack_bf16(v[4], v[5]);
+    o.w = pack_bf16(v[6], v[7]);
+    *reinterpret_cast<uint4*>(p.a + q * p.as + p.ao + n) = o;
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constant__ CUtensorMap map_x,
                                                            const __grid_constant__ CUtensorMap map_w,
                                                            const ConvTma p) {
@@ -471,29 +493,188 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
         float v[8];
         tmem_ld8(lane_base + (uint32_t)nc, v);
         if (!valid) continue;
-        const int n = n0 + nc;
-        if (p.bias)
-          for (int j = 0; j < 8; ++j) v[j] += __ldg(p.bias + n + j);
-        if (p.z) {
-          float4* zp = reinterpret_cast<float4*>(p.z + q * p.zs + p.zo + n);
-          zp[0] = make_float4(v[0], v[1], v[2], v[3]);
-          zp[1] = make_float4(v[4], v[5], v[6], v[7]);
-        }
-        if (p.a) {
-          if (p.act == SHY_SG_ACT_GELU)
-            for (int j = 0; j < 8; ++j) v[j] = gelu(v[j]);
-          uint4 o;
-          o.x = pack_bf16(v[0], v[1]);
-          o.y = pack_bf16(v[2], v[3]);
-          o.z = pack_bf16(v[4], v[5]);
-          o.w = pack_bf16(v[6], v[7]);
-          *reinterpret_cast<uint4*>(p.a + q * p.as + p.ao + n) = o;
-        }
+        store_out8(p, q, n0 + nc, v);
       }
     }
   } else if (tid == 0) {
     atomicCAS(&g_sg_status, 0, SHY_ERR_TIMEOUT);
   }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_free(tmem, p.tmem_cols);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent, warp-specialised convolution (conv_ws_kernel).
+//
+// The GEMM of conv_tma_kernel with one CTA per SM walking the tiles
+// t = blockIdx.x, + gridDim.x, ...  Warp 4 (one lane) issues the TMA loads
+// into a ring of stages that runs on from tile to tile; warp 5 (one lane)
+// issues the MMAs into one of two accumulators in tensor memory, alternating
+// by tile; warps 0-3 read the other accumulator back and store it, so a
+// tile's epilogue runs under the next tile's loads and MMAs.  Barriers:
+// full / empty per stage (TMA bytes / MMA commit), acc_full per accumulator
+// (MMA commit), acc_empty per accumulator (the 128 epilogue threads).  Every
+// wait is bounded; a role that gives up raises an abort flag the others poll,
+// and the CTA still waits for its own loads and frees its tensor memory.
+constexpr int kWsThreads = 192;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// mbar_wait that also gives up when *abort is raised, and raises it on timeout.
+__device__ bool mbar_wait_abort(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = now_ns();
+  while (!mbar_try(bar, parity)) {
+    if (*abort) return false;
+    if (now_ns() - t0 > kWaitLimitNs) {
+      *abort = 1;
+      return false;
+    }
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(kWsThreads, 1) conv_ws_kernel(const __grid_constant__ CUtensorMap map_x,
+                                                               const __grid_constant__ CUtensorMap map_w,
+                                                               const ConvTma p) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], accf[2], acce[2], done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_abort, s_issued, s_consumed;
+  const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n_tiles = p.cout / p.ntile;
+  const int total = p.batch * p.tiles_h * p.tiles_w * n_tiles;
+  const int S = p.stages;
+  volatile int* abort = &s_abort;
+
+  if (warp == 0) tmem_alloc(&tmem_slot, p.tmem_cols);
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(&accf[a], 1);
+      mbar_init(&acce[a], 128);
+    }
+    mbar_init(&done, 1);
+    s_abort = 0;
+    s_issued = 0;
+    s_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const int taps = p.ks * p.ks, half = p.ks >> 1;
+  const int nchunk = p.cin / p.kc, iters = taps * nchunk;
+  const uint32_t acc_cols = (uint32_t)(p.mt * p.ntile);
+  const uint32_t sub_bytes = (uint32_t)kTileM * p.kc * 2;
+  // tile t: output-channel tile t % n_tiles of pixel tile t / n_tiles
+  auto decode = [&](int t, int& b, int& x0, int& y0, int& n0) {
+    n0 = (t % n_tiles) * p.ntile;
+    int r = t / n_tiles;
+    x0 = (r % p.tiles_w) * kTileW;
+    r /= p.tiles_w;
+    y0 = (r % p.tiles_h) * kTileH * p.mt;
+    b = r / p.tiles_h;
+  };
+
+  if (warp == 4) {
+    if (lane == 0) {
+      int g = 0;
+      for (int t = blockIdx.x; t < total && !*abort; t += gridDim.x) {
+        int b, x0, y0, n0;
+        decode(t, b, x0, y0, n0);
+        bool ok = true;
+        for (int it = 0; it < iters; ++it) {
+          const int s = g % S;
+          if (g >= S && !mbar_wait_abort(&empty[s], (uint32_t)(g / S - 1) & 1u, abort)) {
+            ok = false;
+            break;
+          }
+          const int tap = it / nchunk, c0 = (it - tap * nchunk) * p.kc;
+          const uint32_t sa = base + s * p.stage_bytes;
+          mbar_expect_tx(&full[s], p.a_bytes + p.b_bytes);
+          tma_load_4d(sa, &map_x, c0, x0 + tap % p.ks - half, y0 + tap / p.ks - half, b, &full[s]);
+          tma_load_2d(sa + p.a_bytes, &map_w, tap * p.cin + c0, n0, &full[s]);
+          ++g;
+        }
+        if (!ok) break;
+      }
+      s_issued = g;
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_m128(p.ntile);
+      const uint32_t sbo = 16u * p.kc;
+      int g = 0, j = 0;
+      for (int t = blockIdx.x; t < total && !*abort; t += gridDim.x, ++j) {
+        const int a = j & 1;
+        if (j >= 2 && !mbar_wait_abort(&acce[a], (uint32_t)(j / 2 - 1) & 1u, abort)) break;
+        tc_fence_after();
+        const uint32_t d0 = tmem + (uint32_t)a * acc_cols;
+        bool ok = true;
+        for (int it = 0; it < iters; ++it) {
+          const int s = g % S;
+          if (!mbar_wait_abort(&full[s], (uint32_t)(g / S) & 1u, abort)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = base + s * p.stage_bytes, sb = sa + p.a_bytes;
+          for (int kk = 0; kk < (p.kc >> 4); ++kk)
+            for (int u = 0; u < p.mt; ++u)
+              mma_bf16(d0 + (uint32_t)(u * p.ntile), smem_desc_sw(sa + u * sub_bytes + kk * 32, sbo, p.layout),
+                       smem_desc_sw(sb + kk * 32, sbo, p.layout), idesc, (it | kk) != 0);
+          mma_commit(&empty[s]);
+          ++g;
+        }
+        if (!ok) break;
+        mma_commit(&accf[a]);
+      }
+      s_consumed = g;
+      mma_commit(&done);
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32w..32w+31, the tile rows of its threads
+    int j = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++j) {
+      const int a = j & 1;
+      if (!__all_sync(0xFFFFFFFFu, mbar_wait_abort(&accf[a], (uint32_t)(j / 2) & 1u, abort))) break;
+      tc_fence_after();
+      int b, x0, y0, n0;
+      decode(t, b, x0, y0, n0);
+      for (int u = 0; u < p.mt; ++u) {
+        const int y = y0 + u * kTileH + (tid >> 4), x = x0 + (tid & 15);
+        const bool valid = y < p.h && x < p.w_;
+        const long long q = ((long long)b * p.h + y) * p.w_ + x;
+        const uint32_t lane_base =
+            tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)a * acc_cols + (uint32_t)(u * p.ntile);
+        for (int nc = 0; nc < p.ntile; nc += 8) {
+          float v[8];
+          tmem_ld8(lane_base + (uint32_t)nc, v);
+          if (valid) store_out8(p, q, n0 + nc, v);
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acce[a]);
+    }
+  }
+  __syncthreads();
+  // loads issued but never consumed (after an abort): wait for them to land
+  if (tid == 128)
+    for (int g = s_consumed; g < s_issued; ++g) mbar_wait(&full[g % S], (uint32_t)(g / S) & 1u);
+  const bool fin = mbar_wait(&done, 0);
+  if (tid == 0 && (!fin || s_abort)) atomicCAS(&g_sg_status, 0, SHY_ERR_TIMEOUT);
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
@@ -1169,7 +1350,8 @@ extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int
   }
   const int pix = d->tile ? d->tile : g_conv_pixels;
   const int mt = pix ? pix / kTileM : 1;
-  if (g_conv_path == SHY_SG_CONV_TMA && encode_conv_maps(d, x, x_stride, w, kc, ntile, mt, &mx, &mw)) {
+  const bool tma_path = g_conv_path == SHY_SG_CONV_TMA || g_conv_path == SHY_SG_CONV_PERSISTENT;
+  if (tma_path && encode_conv_maps(d, x, x_stride, w, kc, ntile, mt, &mx, &mw)) {
     ConvTma p{};
     p.bias = bias;
     p.z = z;
@@ -1209,15 +1391,36 @@ extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int
       attr_tma = true;
     }
     const long long tiles = (long long)d->batch * p.tiles_h * p.tiles_w;
+    if (g_conv_path == SHY_SG_CONV_PERSISTENT) {
+      // one CTA per SM, two accumulators, the deepest ring that fits
+      p.tmem_cols = pow2_cols(2 * ntile * mt);
+      const int max_smem = 227 * 1024 - 1024;
+      p.stages = d->stages ? d->stages : std::min(6, (max_smem - 1024) / (int)p.stage_bytes);
+      p.stages = std::max(2, std::min(p.stages, (max_smem - 1024) / (int)p.stage_bytes));
+      const int ws_smem = std::max(p.stages * (int)p.stage_bytes + 1024, 120 * 1024);
+      static bool attr_ws = false;
+      static int sms = 0;
+      if (!attr_ws) {
+        cudaFuncSetAttribute(conv_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        attr_ws = true;
+      }
+      const long long work = tiles * (d->cout / ntile);
+      const unsigned grid = (unsigned)std::max(1ll, std::min(work, (long long)std::max(sms, 1)));
+      conv_ws_kernel<<<grid, kWsThreads, ws_smem, static_cast<cudaStream_t>(stream)>>>(mx, mw, p);
+      return launch_status(fn);
+    }
     dim3 grid((unsigned)tiles, (unsigned)(d->cout / ntile));
     conv_tma_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(mx, mw, p);
     return launch_status(fn);
   }
-  if (g_conv_path == SHY_SG_CONV_TMA && !encode_tiled()) {
+  if (tma_path && !encode_tiled()) {
     set_error("%s: cuTensorMapEncodeTiled is not available", fn);
     return SHY_ERR_CUDA;
   }
-  if (g_conv_path == SHY_SG_CONV_TMA) {
+  if (tma_path) {
     set_error("%s: tensor map encoding failed", fn);
     return SHY_ERR_INVALID_ARG;
   }
@@ -1266,7 +1469,7 @@ extern "C" int shy_sg_conv_wgrad(const shy_sg_conv_desc* d, const void* x, int32
   }
   const int ntile = pick_ntile(d->cout);
   const int rows = d->ksize * d->ksize * d->cin;
-  if (g_conv_path == SHY_SG_CONV_TMA) {
+  if (g_conv_path == SHY_SG_CONV_TMA || g_conv_path == SHY_SG_CONV_PERSISTENT) {
     WgradTma q{};
     q.kcm = d->cin % 64 == 0 ? 64 : d->cin % 32 == 0 ? 32 : 16;
     q.kcn = ntile % 64 == 0 ? 64 : ntile % 32 == 0 ? 32 : 16;
@@ -1526,7 +1729,7 @@ extern "C" int shy_sg_decode(int64_t pixels, const float* z, int32_t z_stride, c
 }
 
 extern "C" int shy_sg_set_conv_path(int32_t path) {
-  if (path != SHY_SG_CONV_TMA && path != SHY_SG_CONV_STAGED) {
+  if (path != SHY_SG_CONV_TMA && path != SHY_SG_CONV_STAGED && path != SHY_SG_CONV_PERSISTENT) {
     set_error("shy_sg_set_conv_path: unknown path %d", path);
     return SHY_ERR_INVALID_ARG;
   }

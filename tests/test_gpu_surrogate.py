@@ -80,9 +80,9 @@ CONV_CASES = [  # batch, h, w, cin, cout, k, x pixel stride
 ]
 
 
-@pytest.fixture(params=[0, 1], ids=["tma", "staged"])
+@pytest.fixture(params=[0, 1, 2], ids=["tma", "staged", "persistent"])
 def conv_path(request, sg):
-    """Both operand-staging paths of shy_sg_conv_forward; the TMA path is restored after."""
+    """The operand-staging paths of the convolutions; the TMA path is restored after."""
     ok(lib().shy_sg_set_conv_path(request.param))
     yield request.param
     ok(lib().shy_sg_set_conv_path(0))
@@ -99,7 +99,7 @@ def conv_tile(request, sg):
 @pytest.mark.parametrize("case", CONV_CASES)
 def test_conv_forward_matches_oracle(sg, conv_path, conv_tile, case):
     if conv_path == 1 and conv_tile != (0, 0):
-        pytest.skip("the tile applies to the TMA path only")
+        pytest.skip("the tile applies to the TMA paths only")
     B, H, W, ci, co, k, xs = case
     rng = np.random.default_rng(sum(case))
     x = so.bf16(rng.standard_normal((B, H, W, xs)))
@@ -135,8 +135,8 @@ def wgrad_tile(request, sg):
 
 @pytest.mark.parametrize("case", CONV_CASES)
 def test_weight_gradient_matches_oracle(sg, conv_path, wgrad_tile, case):
-    if conv_path == 1 and wgrad_tile != (0, 0):
-        pytest.skip("the tile applies to the TMA path only")
+    if conv_path != 0 and wgrad_tile != (0, 0):
+        pytest.skip("the weight gradient's tile is covered on the TMA path")
     B, H, W, ci, co, k, xs = case
     rng = np.random.default_rng(sum(case) + 1)
     x = so.bf16(rng.standard_normal((B, H, W, xs)))
@@ -279,9 +279,18 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30))
 
 
-def test_network_gradients_match_oracle(sg):
+@pytest.mark.parametrize("path", [0, 2], ids=["tma", "persistent"])
+def test_network_gradients_match_oracle(sg, path):
     """One training step's loss and every layer's gradient, device against
     the oracle with bf16 storage emulated (and against pure FP64)."""
+    ok(lib().shy_sg_set_conv_path(path))
+    try:
+        _network_gradients_match_oracle(sg)
+    finally:
+        ok(lib().shy_sg_set_conv_path(0))
+
+
+def _network_gradients_match_oracle(sg):
     params = so.init_params(21)
     rng = np.random.default_rng(22)
     B, H, W = 2, 32, 16
