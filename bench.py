@@ -641,10 +641,10 @@ def run_surrogate(args):
     for path, label in ((1, "staged"), (0, "tma")):
         shy._capi.check(shy.lib().shy_sg_set_conv_path(path))
         for _ in range(3):
-            net._conv(ws, "dec2a", 2, ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
+            net._conv(ws, "dec2a", ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
         ev[0].record()
         for _ in range(reps):
-            net._conv(ws, "dec2a", 2, ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
+            net._conv(ws, "dec2a", ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
         ev[1].record()
         torch.cuda.synchronize()
         conv_paths[label] = ev[0].elapsed_time(ev[1]) / reps

@@ -35,7 +35,6 @@ import math
 
 import numpy as np
 
-from . import _capi
 from ._capi import SgAdamw, SgConvDesc, SgNorm, check, lib
 
 IN_CH = 16
@@ -238,7 +237,7 @@ class Surrogate:
         tile, stages = self.tune.get((name, kind), (0, 0))
         return SgConvDesc(B, H >> lv, W >> lv, ci, co, L["k"], tile, stages)
 
-    def _conv(self, ws, name, level, x, xs, z, zs, zo, a, as_, ao, act):
+    def _conv(self, ws, name, x, xs, z, zs, zo, a, as_, ao, act):
         L = self.layers[name]
         d = self._desc(ws, name, "fwd")
         self._call("shy_sg_conv_forward", C.byref(d), self._p(x), xs, self._p(L["wb"]),
@@ -258,35 +257,35 @@ class Surrogate:
         c0, c1, c2, c3 = CHANNELS
         z = ws.z.get
         G = ACT_GELU
-        self._conv(ws, "enc0a", 0, ws.x0, IN_CH, z("enc0a"), c0, 0, ws.a["enc0a"], c0, 0, G)
-        self._conv(ws, "enc0b", 0, ws.a["enc0a"], c0, z("enc0b"), c0, 0, ws.cat[0], 3 * c0, 2 * c0, G)
+        self._conv(ws, "enc0a", ws.x0, IN_CH, z("enc0a"), c0, 0, ws.a["enc0a"], c0, 0, G)
+        self._conv(ws, "enc0b", ws.a["enc0a"], c0, z("enc0b"), c0, 0, ws.cat[0], 3 * c0, 2 * c0, G)
         self._call("shy_sg_pool_forward", B, H, W, c0, self._p(ws.cat[0]), 3 * c0, 2 * c0,
                    self._p(ws.pool[1]), c0, 0)
-        self._conv(ws, "enc1a", 1, ws.pool[1], c0, z("enc1a"), c1, 0, ws.a["enc1a"], c1, 0, G)
-        self._conv(ws, "enc1b", 1, ws.a["enc1a"], c1, z("enc1b"), c1, 0, ws.cat[1], 3 * c1, 2 * c1, G)
+        self._conv(ws, "enc1a", ws.pool[1], c0, z("enc1a"), c1, 0, ws.a["enc1a"], c1, 0, G)
+        self._conv(ws, "enc1b", ws.a["enc1a"], c1, z("enc1b"), c1, 0, ws.cat[1], 3 * c1, 2 * c1, G)
         self._call("shy_sg_pool_forward", B, H >> 1, W >> 1, c1, self._p(ws.cat[1]), 3 * c1, 2 * c1,
                    self._p(ws.pool[2]), c1, 0)
-        self._conv(ws, "enc2a", 2, ws.pool[2], c1, z("enc2a"), c2, 0, ws.a["enc2a"], c2, 0, G)
-        self._conv(ws, "enc2b", 2, ws.a["enc2a"], c2, z("enc2b"), c2, 0, ws.cat[2], 3 * c2, 2 * c2, G)
+        self._conv(ws, "enc2a", ws.pool[2], c1, z("enc2a"), c2, 0, ws.a["enc2a"], c2, 0, G)
+        self._conv(ws, "enc2b", ws.a["enc2a"], c2, z("enc2b"), c2, 0, ws.cat[2], 3 * c2, 2 * c2, G)
         self._call("shy_sg_pool_forward", B, H >> 2, W >> 2, c2, self._p(ws.cat[2]), 3 * c2, 2 * c2,
                    self._p(ws.pool[3]), c2, 0)
-        self._conv(ws, "mid", 3, ws.pool[3], c2, z("mid"), c3, 0, ws.a["mid"], c3, 0, G)
+        self._conv(ws, "mid", ws.pool[3], c2, z("mid"), c3, 0, ws.a["mid"], c3, 0, G)
         self._call("shy_sg_upsample_forward", B, H >> 3, W >> 3, c3, self._p(ws.a["mid"]), c3, 0,
                    self._p(ws.cat[2]), 3 * c2, 0)
-        self._conv(ws, "dec2a", 2, ws.cat[2], 3 * c2, z("dec2a"), c2, 0, ws.a["dec2a"], c2, 0, G)
-        self._conv(ws, "dec2b", 2, ws.a["dec2a"], c2, z("dec2b"), c2, 0, ws.a["dec2b"], c2, 0, G)
+        self._conv(ws, "dec2a", ws.cat[2], 3 * c2, z("dec2a"), c2, 0, ws.a["dec2a"], c2, 0, G)
+        self._conv(ws, "dec2b", ws.a["dec2a"], c2, z("dec2b"), c2, 0, ws.a["dec2b"], c2, 0, G)
         self._call("shy_sg_upsample_forward", B, H >> 2, W >> 2, c2, self._p(ws.a["dec2b"]), c2, 0,
                    self._p(ws.cat[1]), 3 * c1, 0)
-        self._conv(ws, "dec1a", 1, ws.cat[1], 3 * c1, z("dec1a"), c1, 0, ws.a["dec1a"], c1, 0, G)
-        self._conv(ws, "dec1b", 1, ws.a["dec1a"], c1, z("dec1b"), c1, 0, ws.a["dec1b"], c1, 0, G)
+        self._conv(ws, "dec1a", ws.cat[1], 3 * c1, z("dec1a"), c1, 0, ws.a["dec1a"], c1, 0, G)
+        self._conv(ws, "dec1b", ws.a["dec1a"], c1, z("dec1b"), c1, 0, ws.a["dec1b"], c1, 0, G)
         self._call("shy_sg_upsample_forward", B, H >> 1, W >> 1, c1, self._p(ws.a["dec1b"]), c1, 0,
                    self._p(ws.cat[0]), 3 * c0, 0)
-        self._conv(ws, "dec0a", 0, ws.cat[0], 3 * c0, z("dec0a"), c0, 0, ws.a["dec0a"], c0, 0, G)
-        self._conv(ws, "dec0b", 0, ws.a["dec0a"], c0, z("dec0b"), c0, 0, ws.a["dec0b"], c0, 0, G)
-        self._conv(ws, "head", 0, ws.a["dec0b"], c0, ws.zh, OUT_CH, 0, None, 0, 0, ACT_NONE)
+        self._conv(ws, "dec0a", ws.cat[0], 3 * c0, z("dec0a"), c0, 0, ws.a["dec0a"], c0, 0, G)
+        self._conv(ws, "dec0b", ws.a["dec0a"], c0, z("dec0b"), c0, 0, ws.a["dec0b"], c0, 0, G)
+        self._conv(ws, "head", ws.a["dec0b"], c0, ws.zh, OUT_CH, 0, None, 0, 0, ACT_NONE)
 
     # -- backward -----------------------------------------------------------
-    def _layer_bwd(self, ws, name, level, x_in, xs, dz, dx, dxs, bias=False):
+    def _layer_bwd(self, ws, name, x_in, xs, dz, dx, dxs, bias=False):
         """Weight gradient of one convolution from its output gradient dz
         (bf16, contiguous), and its bias gradient if `bias` (the GELU
         backward that made dz adds it otherwise); its input gradient into dx
@@ -315,49 +314,49 @@ class Surrogate:
         B, H, W = ws.shape
         c0, c1, c2, c3 = CHANNELS
         da, dz, dcat, dp = ws.da, ws.dz, ws.dcat, ws.dpool
-        self._layer_bwd(ws, "head", 0, ws.a["dec0b"], c0, ws.dzh, da[0], c0, bias=True)
+        self._layer_bwd(ws, "head", ws.a["dec0b"], c0, ws.dzh, da[0], c0, bias=True)
         self._gelu_bwd(ws, 0, c0, da[0], c0, 0, "dec0b")
-        self._layer_bwd(ws, "dec0b", 0, ws.a["dec0a"], c0, dz[0], da[0], c0)
+        self._layer_bwd(ws, "dec0b", ws.a["dec0a"], c0, dz[0], da[0], c0)
         self._gelu_bwd(ws, 0, c0, da[0], c0, 0, "dec0a")
-        self._layer_bwd(ws, "dec0a", 0, ws.cat[0], 3 * c0, dz[0], dcat[0], 3 * c0)
+        self._layer_bwd(ws, "dec0a", ws.cat[0], 3 * c0, dz[0], dcat[0], 3 * c0)
         da[1].zero_()
         self._call("shy_sg_upsample_backward", B, H >> 1, W >> 1, c1, self._p(dcat[0]), 3 * c0, 0,
                    self._p(da[1]), c1, 0)
         self._gelu_bwd(ws, 1, c1, da[1], c1, 0, "dec1b")
-        self._layer_bwd(ws, "dec1b", 1, ws.a["dec1a"], c1, dz[1], da[1], c1)
+        self._layer_bwd(ws, "dec1b", ws.a["dec1a"], c1, dz[1], da[1], c1)
         self._gelu_bwd(ws, 1, c1, da[1], c1, 0, "dec1a")
-        self._layer_bwd(ws, "dec1a", 1, ws.cat[1], 3 * c1, dz[1], dcat[1], 3 * c1)
+        self._layer_bwd(ws, "dec1a", ws.cat[1], 3 * c1, dz[1], dcat[1], 3 * c1)
         da[2].zero_()
         self._call("shy_sg_upsample_backward", B, H >> 2, W >> 2, c2, self._p(dcat[1]), 3 * c1, 0,
                    self._p(da[2]), c2, 0)
         self._gelu_bwd(ws, 2, c2, da[2], c2, 0, "dec2b")
-        self._layer_bwd(ws, "dec2b", 2, ws.a["dec2a"], c2, dz[2], da[2], c2)
+        self._layer_bwd(ws, "dec2b", ws.a["dec2a"], c2, dz[2], da[2], c2)
         self._gelu_bwd(ws, 2, c2, da[2], c2, 0, "dec2a")
-        self._layer_bwd(ws, "dec2a", 2, ws.cat[2], 3 * c2, dz[2], dcat[2], 3 * c2)
+        self._layer_bwd(ws, "dec2a", ws.cat[2], 3 * c2, dz[2], dcat[2], 3 * c2)
         da[3].zero_()
         self._call("shy_sg_upsample_backward", B, H >> 3, W >> 3, c3, self._p(dcat[2]), 3 * c2, 0,
                    self._p(da[3]), c3, 0)
         self._gelu_bwd(ws, 3, c3, da[3], c3, 0, "mid")
-        self._layer_bwd(ws, "mid", 3, ws.pool[3], c2, dz[3], dp[3], c2)
+        self._layer_bwd(ws, "mid", ws.pool[3], c2, dz[3], dp[3], c2)
         # level 2 encoder: skip gradient from dec2a plus the pooled path
         self._call("shy_sg_pool_backward", B, H >> 2, W >> 2, c2, self._p(dp[3]), c2, 0, self._p(dcat[2]),
                    3 * c2, 2 * c2)
         self._gelu_bwd(ws, 2, c2, dcat[2], 3 * c2, 2 * c2, "enc2b")
-        self._layer_bwd(ws, "enc2b", 2, ws.a["enc2a"], c2, dz[2], da[2], c2)
+        self._layer_bwd(ws, "enc2b", ws.a["enc2a"], c2, dz[2], da[2], c2)
         self._gelu_bwd(ws, 2, c2, da[2], c2, 0, "enc2a")
-        self._layer_bwd(ws, "enc2a", 2, ws.pool[2], c1, dz[2], dp[2], c1)
+        self._layer_bwd(ws, "enc2a", ws.pool[2], c1, dz[2], dp[2], c1)
         self._call("shy_sg_pool_backward", B, H >> 1, W >> 1, c1, self._p(dp[2]), c1, 0, self._p(dcat[1]),
                    3 * c1, 2 * c1)
         self._gelu_bwd(ws, 1, c1, dcat[1], 3 * c1, 2 * c1, "enc1b")
-        self._layer_bwd(ws, "enc1b", 1, ws.a["enc1a"], c1, dz[1], da[1], c1)
+        self._layer_bwd(ws, "enc1b", ws.a["enc1a"], c1, dz[1], da[1], c1)
         self._gelu_bwd(ws, 1, c1, da[1], c1, 0, "enc1a")
-        self._layer_bwd(ws, "enc1a", 1, ws.pool[1], c0, dz[1], dp[1], c0)
+        self._layer_bwd(ws, "enc1a", ws.pool[1], c0, dz[1], dp[1], c0)
         self._call("shy_sg_pool_backward", B, H, W, c0, self._p(dp[1]), c0, 0, self._p(dcat[0]), 3 * c0,
                    2 * c0)
         self._gelu_bwd(ws, 0, c0, dcat[0], 3 * c0, 2 * c0, "enc0b")
-        self._layer_bwd(ws, "enc0b", 0, ws.a["enc0a"], c0, dz[0], da[0], c0)
+        self._layer_bwd(ws, "enc0b", ws.a["enc0a"], c0, dz[0], da[0], c0)
         self._gelu_bwd(ws, 0, c0, da[0], c0, 0, "enc0a")
-        self._layer_bwd(ws, "enc0a", 0, ws.x0, IN_CH, dz[0], None, 0)
+        self._layer_bwd(ws, "enc0a", ws.x0, IN_CH, dz[0], None, 0)
 
     # -- autotuning ---------------------------------------------------------
     def _layer_inputs(self, ws):
@@ -587,4 +586,3 @@ def log_l2(d, ref):
 
 
 __all__ = ["Surrogate", "Norm", "LAYERS", "param_count", "flops_per_pixel", "make_pairs", "train", "log_l2"]
-_ = _capi

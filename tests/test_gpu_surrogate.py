@@ -325,7 +325,6 @@ def _network_gradients_match_oracle(sg):
 
 def test_training_reduces_the_loss(sg):
     """AdamW on the device fits a fixed batch: the loss falls tenfold."""
-    rng = np.random.default_rng(31)
     B, H, W = 4, 32, 32
     yy, xx = np.meshgrid(np.linspace(0, 1, H), np.linspace(0, 1, W), indexing="ij")
     h = np.stack([0.5 + 0.3 * np.sin(3 * xx + i) * np.cos(2 * yy - i) for i in range(B)]).astype(np.float32)
@@ -338,7 +337,6 @@ def test_training_reduces_the_loss(sg):
     first, last = float(losses[0].item()), float(losses[-1].item())
     net.status()
     assert last < 0.1 * first, (first, last)
-    _ = rng
 
 
 def test_trained_network_beats_the_method_without_it(sg):
