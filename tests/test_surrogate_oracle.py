@@ -204,3 +204,61 @@ def test_unet_gradients_match_finite_differences():
         bm[j] -= eps
         fd = (loss_of({**params, name: (w, bp)}) - loss_of({**params, name: (w, bm)})) / (2 * eps)
         assert fd == pytest.approx(grads[name][1][j], rel=1e-5, abs=1e-9), (name, j)
+
+
+class _StubNet:
+    """Stands in for Surrogate in train(): records each step's batch on the CPU."""
+
+    def __init__(self, norm):
+        self.torch = torch
+        self.dev = torch.device("cpu")
+        self.norm = norm
+        self.steps = []
+
+    def train_step(self, h, t, lr):
+        self.steps.append((h.clone(), t.clone(), lr))
+        return torch.zeros(1, dtype=torch.float64)
+
+
+def test_training_loop_crops_flips_and_schedule():
+    from simplehydrology_gb300 import surrogate as sg
+    rng = np.random.default_rng(11)
+    n, side = 3, 32
+    H = rng.random((n, side, side)).astype(np.float32)
+    D = rng.random((n, side, side)).astype(np.float32) * 3
+    MX, MY = rng.standard_normal((2, n, side, side)).astype(np.float32)
+    norm = sg.Norm.fit(H, D, MX, MY)
+    net = _StubNet(norm)
+    losses = sg.train(net, H, D, MX, MY, epochs=2, batch=4, lr=1e-3, seed=5, crop=16, steps_per_epoch=3)
+    assert len(losses) == 2 and len(net.steps) == 6
+    mean, scale = np.asarray(norm.out_mean), np.asarray(norm.out_scale)
+    for h, t, lr in net.steps:
+        assert tuple(h.shape) == (4, 16, 16) and tuple(t.shape) == (4, 16, 16, 3)
+        for i in range(4):
+            hi, raw = h[i].numpy(), t[i].numpy() * scale + mean
+            # the crop is a window at a multiple of 8 of some map, flipped along rows and/or columns
+            found = False
+            for k in range(n):
+                for oy in range(0, side - 15, 8):
+                    for ox in range(0, side - 15, 8):
+                        for fy in (False, True):
+                            for fx in (False, True):
+                                w = H[k, oy:oy + 16, ox:ox + 16]
+                                w = w[::-1] if fy else w
+                                w = w[:, ::-1] if fx else w
+                                if not np.array_equal(w, hi):
+                                    continue
+                                sl = (k, slice(oy, oy + 16), slice(ox, ox + 16))
+                                mx, my = MX[sl], MY[sl]
+                                d = D[sl]
+                                if fy:
+                                    d, mx, my = d[::-1], -mx[::-1], my[::-1]
+                                if fx:
+                                    d, mx, my = d[:, ::-1], mx[:, ::-1], -my[:, ::-1]
+                                np.testing.assert_allclose(np.expm1(raw[..., 0]), d, rtol=1e-4, atol=1e-5)
+                                np.testing.assert_allclose(raw[..., 1], mx, rtol=1e-4, atol=1e-5)
+                                np.testing.assert_allclose(raw[..., 2], my, rtol=1e-4, atol=1e-5)
+                                found = True
+            assert found
+    lrs = [lr for _, _, lr in net.steps]
+    assert lrs[0] == pytest.approx(1e-3) and all(a > b for a, b in zip(lrs, lrs[1:])) and lrs[-1] > 0
