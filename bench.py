@@ -747,6 +747,16 @@ def run_surrogate_step(args):
     net.status()
     ms = ev[0].elapsed_time(ev[1]) / args.steps
     flops = batch * side * side * sg.flops_per_pixel(True)
+    # inference on one 1024^2 map: features, forward, decode (device time)
+    h1 = torch.rand((1, 1024, 1024), device="cuda", generator=g)
+    for _ in range(2):
+        net.predict(h1)
+    ev[0].record()
+    for _ in range(10):
+        net.predict(h1)
+    ev[1].record()
+    torch.cuda.synchronize()
+    infer_ms = ev[0].elapsed_time(ev[1]) / 10
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             peak, src = float(json.load(f)["bf16_tflops_sustained"]), "measured (sustained)"
@@ -760,6 +770,8 @@ def run_surrogate_step(args):
         "config": {"workload": "surrogate U-Net training step, 16 x 256x256 maps, AdamW",
                    "params": sg.param_count(), "gflop_per_step": flops / 1e9},
         "gpu_launches": (net.launches - launches0),
+        "inference_1024": {"ms": infer_ms,
+                           "tflops": 1024 * 1024 * sg.flops_per_pixel(False) / (infer_ms / 1e3) / 1e12},
         "autotune": {f"{n}/{k}": f"{v[0]}px x{v[1]}" for (n, k), v in tuned.items()},
         "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
                      "peak_source": src, "kernel": "whole training step (convolutions 80 % of its time)",
