@@ -81,6 +81,18 @@ int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int32_t x_stri
                         int32_t z_offset, void* a, int32_t a_stride, int32_t a_offset,
                         int32_t act, void* stream);
 
+/* The input gradient of a convolution whose input is a GELU layer's output,
+ * fused with that layer's backward pass: with d the input-gradient
+ * convolution (cin = the forward's cout, cout = the forward's cin) and
+ * w_flip from shy_sg_weight_prep,
+ *   dz_prev[pixel][c] = bf16(conv(dz, w_flip)[pixel][c] * gelu'(z_prev[pixel][c]))
+ * (bf16, pixel stride d->cout).  z_prev is f32 with its own stride and
+ * offset (16-byte aligned, multiples of 4).  The GELU layer's bias gradient
+ * is shy_sg_bias_grad of dz_prev. */
+int shy_sg_conv_input_grad(const shy_sg_conv_desc* d, const void* dz, int32_t dz_stride,
+                           const void* w_flip, const float* z_prev, int32_t zp_stride,
+                           int32_t zp_offset, void* dz_prev, void* stream);
+
 /* dw[cout][tap][cin] += sum over pixels of dz[pixel][cout] * x[pixel + tap][cin]
  * (x zero outside the image).  x, dz: bf16; dw: f32, accumulated with
  * atomics, so the summation order varies from run to run. */

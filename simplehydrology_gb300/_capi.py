@@ -166,6 +166,7 @@ SIGNATURES = {
     "shy_sg_conv_forward": (C.c_int, [P(SgConvDesc), W, C.c_int32, W, W, W, C.c_int32, C.c_int32, W,
                                       C.c_int32, C.c_int32, C.c_int32, W]),
     "shy_sg_conv_wgrad": (C.c_int, [P(SgConvDesc), W, C.c_int32, W, C.c_int32, W, W]),
+    "shy_sg_conv_input_grad": (C.c_int, [P(SgConvDesc), W, C.c_int32, W, W, C.c_int32, C.c_int32, W, W]),
     "shy_sg_bias_grad": (C.c_int, [C.c_int64, C.c_int32, W, C.c_int32, W, W]),
     "shy_sg_gelu_backward": (C.c_int, [C.c_int64, C.c_int32, W, C.c_int32, C.c_int32, W, C.c_int32, C.c_int32,
                                        W, W, W]),

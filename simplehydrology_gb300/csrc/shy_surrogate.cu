@@ -183,14 +183,64 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 __device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
 __device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
 
+// Epilogue of the convolutions: 8 accumulator columns of one pixel, plus
+// bias, to f32 and/or bf16 (GELU'd) outputs.
+template <class P>
+__device__ __forceinline__ void store_out8(const P& p, long long q, int n, float v[8]) {
+  if (p.bias)
+    for (int j = 0; j < 8; ++j) v[j] += __ldg(p.bias + n + j);
+  if (p.z) {
+    float4* zp = reinterpret_cast<float4*>(p.z + q * p.zs + p.zo + n);
+    zp[0] = make_float4(v[0], v[1], v[2], v[3]);
+    zp[1] = make_float4(v[4], v[5], v[6], v[7]);
+  }
+  if (p.a) {
+    if (p.act == SHY_SG_ACT_GELU)
+      for (int j = 0; j < 8; ++j) v[j] = gelu(v[j]);
+    uint4 o;
+    o.x = pack_bf16(v[0], v[1]);
+    o.y = pack_bf16(v[2], v[3]);
+    o.z = pack_bf16(v[4], v[5]);
+    o.w = pack_bf16(v[6], v[7]);
+    *reinterpret_cast<uint4*>(p.a + q * p.as + p.ao + n) = o;
+  }
+}
+
+// The epilogue of 8 columns of one pixel.  In input-gradient mode (p.gz
+// set) the columns are the gradient of a GELU layer's output:
+// dz = bf16(v * gelu'(z_prev)) goes to p.a.  Otherwise store_out8.
+template <class P>
+__device__ __forceinline__ void epilogue8(const P& p, bool valid, long long q, int n, float v[8]) {
+  if (!valid) return;
+  if (!p.gz) {
+    store_out8(p, q, n, v);
+    return;
+  }
+  float g[8];
+  {
+    const float4* zp = reinterpret_cast<const float4*>(p.gz + q * p.gzs + p.gzo + n);
+    const float4 z0 = zp[0], z1 = zp[1];
+    const float zv[8] = {z0.x, z0.y, z0.z, z0.w, z1.x, z1.y, z1.z, z1.w};
+#pragma unroll
+    for (int j = 0; j < 8; ++j) g[j] = __bfloat162float(__float2bfloat16_rn(v[j] * gelu_grad(zv[j])));
+    uint4 o;
+    o.x = pack_bf16(g[0], g[1]);
+    o.y = pack_bf16(g[2], g[3]);
+    o.z = pack_bf16(g[4], g[5]);
+    o.w = pack_bf16(g[6], g[7]);
+    *reinterpret_cast<uint4*>(p.a + q * p.as + p.ao + n) = o;
+  }
+}
+
 struct ConvFwd {
   const __nv_bfloat16* x;
   const __nv_bfloat16* w;
   const float* bias;
   float* z;
   __nv_bfloat16* a;
+  const float* gz;
   int batch, h, w_, cin, cout, ks;
-  int xs, zs, zo, as, ao, act;
+  int xs, zs, zo, as, ao, act, gzs, gzo;
   int ntile, kc, tmem_cols;
 };
 
@@ -282,25 +332,7 @@ __global__ void __launch_bounds__(kThreads) conv_fwd_kernel(const ConvFwd p) {
     for (int nc = 0; nc < p.ntile; nc += 8) {
       float v[8];
       tmem_ld8(lane_base + (uint32_t)nc, v);
-      if (!valid) continue;
-      const int n = n0 + nc;
-      if (p.bias)
-        for (int j = 0; j < 8; ++j) v[j] += __ldg(p.bias + n + j);
-      if (p.z) {
-        float4* zp = reinterpret_cast<float4*>(p.z + q * p.zs + p.zo + n);
-        zp[0] = make_float4(v[0], v[1], v[2], v[3]);
-        zp[1] = make_float4(v[4], v[5], v[6], v[7]);
-      }
-      if (p.a) {
-        if (p.act == SHY_SG_ACT_GELU)
-          for (int j = 0; j < 8; ++j) v[j] = gelu(v[j]);
-        uint4 o;
-        o.x = pack_bf16(v[0], v[1]);
-        o.y = pack_bf16(v[2], v[3]);
-        o.z = pack_bf16(v[4], v[5]);
-        o.w = pack_bf16(v[6], v[7]);
-        *reinterpret_cast<uint4*>(p.a + q * p.as + p.ao + n) = o;
-      }
+      epilogue8(p, valid, q, n0 + nc, v);
     }
   } else if (tid == 0) {
     atomicCAS(&g_sg_status, 0, SHY_ERR_TIMEOUT);
@@ -334,8 +366,9 @@ struct ConvTma {
   const float* bias;
   float* z;
   __nv_bfloat16* a;
+  const float* gz;  // input-gradient mode: the previous layer's pre-activation (else NULL)
   int batch, h, w_, cin, cout, ks;
-  int zs, zo, as, ao, act;
+  int zs, zo, as, ao, act, gzs, gzo;
   int ntile, kc, tmem_cols, tiles_w, tiles_h, stages, mt;  // mt: 128-pixel sub-tiles (1 or 2)
   uint32_t a_bytes, b_bytes, stage_bytes, layout;
 };
@@ -375,28 +408,6 @@ __device__ __forceinline__ uint64_t smem_desc_sw(uint32_t addr, uint32_t sbo, ui
 __device__ __forceinline__ uint64_t smem_desc_mn(uint32_t addr, uint32_t lbo, uint32_t sbo, uint32_t layout) {
   return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
          (1ull << 46) | ((uint64_t)layout << 61);
-}
-
-// Epilogue of the TMA convolutions: 8 accumulator columns of one pixel,
-// plus bias, to f32 and/or bf16 (GELU'd) outputs.
-__device__ __forceinline__ void store_out8(const ConvTma& p, long long q, int n, float v[8]) {
-  if (p.bias)
-    for (int j = 0; j < 8; ++j) v[j] += __ldg(p.bias + n + j);
-  if (p.z) {
-    float4* zp = reinterpret_cast<float4*>(p.z + q * p.zs + p.zo + n);
-    zp[0] = make_float4(v[0], v[1], v[2], v[3]);
-    zp[1] = make_float4(v[4], v[5], v[6], v[7]);
-  }
-  if (p.a) {
-    if (p.act == SHY_SG_ACT_GELU)
-      for (int j = 0; j < 8; ++j) v[j] = gelu(v[j]);
-    uint4 o;
-    o.x = pack_bf16(v[0], v[1]);
-    o.y = pack_bf16(v[2], v[3]);
-    o.z = pack_bf16(v[4], v[5]);
-    o.w = pack_bf16(v[6], v[7]);
-    *reinterpret_cast<uint4*>(p.a + q * p.as + p.ao + n) = o;
-  }
 }
 
 __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constant__ CUtensorMap map_x,
@@ -492,8 +503,7 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
       for (int nc = 0; nc < p.ntile; nc += 8) {
         float v[8];
         tmem_ld8(lane_base + (uint32_t)nc, v);
-        if (!valid) continue;
-        store_out8(p, q, n0 + nc, v);
+        epilogue8(p, valid, q, n0 + nc, v);
       }
     }
   } else if (tid == 0) {
@@ -662,7 +672,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) conv_ws_kernel(const __grid_con
         for (int nc = 0; nc < p.ntile; nc += 8) {
           float v[8];
           tmem_ld8(lane_base + (uint32_t)nc, v);
-          if (valid) store_out8(p, q, n0 + nc, v);
+          epilogue8(p, valid, q, n0 + nc, v);
         }
       }
       tc_fence_before();
@@ -1319,10 +1329,13 @@ bool check_conv_desc(const shy_sg_conv_desc* d, const char* fn) {
 
 using namespace shy;
 
-extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int32_t x_stride, const void* w,
-                                   const float* bias, float* z, int32_t z_stride, int32_t z_offset, void* a,
-                                   int32_t a_stride, int32_t a_offset, int32_t act, void* stream) {
-  static const char* fn = "shy_sg_conv_forward";
+namespace {
+// Both convolution entry points: a forward (gz NULL) or an input gradient
+// through a GELU (gz the previous layer's pre-activation, output bf16 to a).
+int conv_launch(const char* fn, const shy_sg_conv_desc* d, const void* x, int32_t x_stride, const void* w,
+                const float* bias, float* z, int32_t z_stride, int32_t z_offset, void* a, int32_t a_stride,
+                int32_t a_offset, int32_t act, const float* gz, int32_t gz_stride, int32_t gz_offset,
+                void* stream) {
   if (!check_conv_desc(d, fn)) return SHY_ERR_INVALID_ARG;
   if (!x || !w || (!z && !a) || !aligned16(x) || !aligned16(w) || x_stride < d->cin || x_stride % 8) {
     set_error("%s: bad input or weight pointer or stride", fn);
@@ -1356,6 +1369,9 @@ extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int
     p.bias = bias;
     p.z = z;
     p.a = static_cast<__nv_bfloat16*>(a);
+    p.gz = gz;
+    p.gzs = gz_stride;
+    p.gzo = gz_offset;
     p.batch = d->batch;
     p.h = d->height;
     p.w_ = d->width;
@@ -1430,6 +1446,9 @@ extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int
   p.bias = bias;
   p.z = z;
   p.a = static_cast<__nv_bfloat16*>(a);
+  p.gz = gz;
+  p.gzs = gz_stride;
+  p.gzo = gz_offset;
   p.batch = d->batch;
   p.h = d->height;
   p.w_ = d->width;
@@ -1456,6 +1475,28 @@ extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int
   dim3 grid((unsigned)((npix + kTileM - 1) / kTileM), (unsigned)(d->cout / p.ntile));
   conv_fwd_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(p);
   return launch_status(fn);
+}
+
+}  // namespace
+
+extern "C" int shy_sg_conv_forward(const shy_sg_conv_desc* d, const void* x, int32_t x_stride, const void* w,
+                                   const float* bias, float* z, int32_t z_stride, int32_t z_offset, void* a,
+                                   int32_t a_stride, int32_t a_offset, int32_t act, void* stream) {
+  return conv_launch("shy_sg_conv_forward", d, x, x_stride, w, bias, z, z_stride, z_offset, a, a_stride, a_offset,
+                     act, nullptr, 0, 0, stream);
+}
+
+extern "C" int shy_sg_conv_input_grad(const shy_sg_conv_desc* d, const void* dz, int32_t dz_stride,
+                                      const void* w_flip, const float* z_prev, int32_t zp_stride,
+                                      int32_t zp_offset, void* dz_prev, void* stream) {
+  static const char* fn = "shy_sg_conv_input_grad";
+  if (!d || !z_prev || !dz_prev || !aligned16(z_prev) || zp_stride % 4 || zp_offset % 4 || zp_offset < 0 ||
+      zp_offset + d->cout > zp_stride) {
+    set_error("%s: bad pre-activation or output (16-byte aligned, stride and offset multiples of 4)", fn);
+    return SHY_ERR_INVALID_ARG;
+  }
+  return conv_launch(fn, d, dz, dz_stride, w_flip, nullptr, nullptr, 0, 0, dz_prev, d->cout, 0, SHY_SG_ACT_NONE,
+                     z_prev, zp_stride, zp_offset, stream);
 }
 
 extern "C" int shy_sg_conv_wgrad(const shy_sg_conv_desc* d, const void* x, int32_t x_stride, const void* dz,

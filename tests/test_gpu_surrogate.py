@@ -181,6 +181,36 @@ def test_input_gradient_through_flipped_weights(sg, conv_path, case):
     assert np.all(np.abs(host(dx) - want) <= 1e-5 * bound + 1e-6)
 
 
+@pytest.mark.parametrize("case", [CONV_CASES[0], CONV_CASES[2], CONV_CASES[4]])
+def test_input_gradient_fused_with_gelu_backward(sg, conv_path, case):
+    """shy_sg_conv_input_grad: the input gradient times gelu'(z_prev), in bf16."""
+    B, H, W, ci, co, k, _ = case
+    rng = np.random.default_rng(sum(case) + 3)
+    w32 = rng.standard_normal((co, k * k, ci)).astype(np.float32) / np.sqrt(k * k * co)
+    dz = so.bf16(rng.standard_normal((B, H, W, co)))
+    P = B * H * W
+    zs = ci + 4
+    zprev = (rng.standard_normal((P, zs)) * 2).astype(np.float32).astype(np.float64)
+    wd = dev(w32.ravel(), torch.float32)
+    wb = torch.empty(w32.size, dtype=torch.bfloat16, device="cuda")
+    wf = torch.empty(w32.size, dtype=torch.bfloat16, device="cuda")
+    ok(lib().shy_sg_weight_prep(co, k, ci, p(wd), p(wb), p(wf), None))
+    out = torch.zeros((P, ci), dtype=torch.bfloat16, device="cuda")
+    from simplehydrology_gb300._capi import SgConvDesc
+    d = SgConvDesc(B, H, W, co, ci, k)
+    ok(lib().shy_sg_conv_input_grad(C.byref(d), p(dev(dz.reshape(P, co), torch.bfloat16)), co, p(wf),
+                                    p(dev(zprev, torch.float32)), zs, 4, p(out), None))
+    status()
+    dx = so.conv_dgrad(dz, so.bf16(w32)).reshape(P, ci)
+    bound = so.conv_dgrad(np.abs(dz), np.abs(so.bf16(w32))).reshape(P, ci)
+    gg = so.gelu_grad(zprev[:, 4:4 + ci])
+    want = dx * gg
+    got = host(out)
+    # gelu' in f32 carries an absolute error of ~1e-7 where 1 + erf cancels (z << 0)
+    assert np.all(np.abs(got - want) <= BF16_REL * np.abs(want) + (1e-5 * bound + 1e-6) * np.abs(gg)
+                  + 1e-6 * np.abs(dx))
+
+
 def test_elementwise_kernels_match_oracle(sg):
     rng = np.random.default_rng(11)
     B, H, W, c = 2, 8, 12, 32
