@@ -65,6 +65,10 @@ int shy_sg_set_conv_path(int32_t path);
  * convolution.  Deeper pipelines keep more loads in flight; shallower ones
  * fit more CTAs on an SM. */
 int shy_sg_set_conv_tile(int32_t pixels, int32_t stages);
+/* Taps per pipeline stage of a 3x3 convolution on SHY_SG_CONV_TMA
+ * (process-wide): 3 (the default: one input box two rows taller than the
+ * tile serves a whole kernel column) or 1 (one box per tap). */
+int shy_sg_set_conv_tap_rows(int32_t rows);
 /* Pipeline of the TMA weight gradient (process-wide): pixels per stage (64
  * or 128, a tile of 16 x 4 or 16 x 8) and stages (2..8); 0 for either (the
  * default) chooses per convolution. */

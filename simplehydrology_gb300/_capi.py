@@ -183,6 +183,7 @@ SIGNATURES = {
     "shy_sg_decode": (C.c_int, [C.c_int64, W, C.c_int32, P(SgNorm), W, W, W, W]),
     "shy_sg_set_conv_path": (C.c_int, [C.c_int32]),
     "shy_sg_set_conv_tile": (C.c_int, [C.c_int32, C.c_int32]),
+    "shy_sg_set_conv_tap_rows": (C.c_int, [C.c_int32]),
     "shy_sg_set_wgrad_tile": (C.c_int, [C.c_int32, C.c_int32]),
     "shy_sg_status": (C.c_int, []),
 }

@@ -370,7 +370,9 @@ struct ConvTma {
   int batch, h, w_, cin, cout, ks;
   int zs, zo, as, ao, act, gzs, gzo;
   int ntile, kc, tmem_cols, tiles_w, tiles_h, stages, mt;  // mt: 128-pixel sub-tiles (1 or 2)
+  int tap_rows;  // taps per stage: 3 (one column of a 3x3 kernel, one taller input box) or 1
   uint32_t a_bytes, b_bytes, stage_bytes, layout;
+  uint32_t a_box, b_box;  // bytes of the input box and of one weight box (b_bytes: all weight boxes)
 };
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
@@ -444,18 +446,28 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
 
   if (tid == 0) {
     const int taps = p.ks * p.ks, half = p.ks >> 1;
-    const int nchunk = p.cin / p.kc, iters = taps * nchunk;
+    const int nchunk = p.cin / p.kc, iters = (taps / p.tap_rows) * nchunk;
     const uint32_t idesc = idesc_bf16_m128(p.ntile);
     const uint32_t sbo = 16u * p.kc;
     const int S = p.stages;
+    // iteration it: channel chunk it % nchunk of tap group it / nchunk; with
+    // tap_rows = 3 a group is one column kx of the 3x3 kernel: one input box
+    // two rows taller than the tile, and the weights of taps (0, kx), (1, kx),
+    // (2, kx)
     auto issue = [&](int it) {
       const int s = it % S;
-      const int tap = it / nchunk, c0 = (it - tap * nchunk) * p.kc;
-      const int dy = tap / p.ks - half, dx = tap % p.ks - half;
+      const int grp = it / nchunk, c0 = (it - grp * nchunk) * p.kc;
       const uint32_t sa = base + s * p.stage_bytes;
-      mbar_expect_tx(&full[s], p.a_bytes + p.b_bytes);
-      tma_load_4d(sa, &map_x, c0, x0 + dx, y0 + dy, b, &full[s]);
-      tma_load_2d(sa + p.a_bytes, &map_w, tap * p.cin + c0, n0, &full[s]);
+      mbar_expect_tx(&full[s], p.a_box + p.b_bytes);
+      if (p.tap_rows == 3) {
+        tma_load_4d(sa, &map_x, c0, x0 + grp - 1, y0 - 1, b, &full[s]);
+        for (int r = 0; r < 3; ++r)
+          tma_load_2d(sa + p.a_bytes + r * p.b_box, &map_w, (r * 3 + grp) * p.cin + c0, n0, &full[s]);
+      } else {
+        const int dy = grp / p.ks - half, dx = grp % p.ks - half;
+        tma_load_4d(sa, &map_x, c0, x0 + dx, y0 + dy, b, &full[s]);
+        tma_load_2d(sa + p.a_bytes, &map_w, grp * p.cin + c0, n0, &full[s]);
+      }
     };
     int issued = 0, consumed = 0;
     bool fail = false;
@@ -470,11 +482,15 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
       tc_fence_after();
       const uint32_t sa = base + s * p.stage_bytes, sb = sa + p.a_bytes;
       // each 128-pixel sub-tile has its own accumulator (ntile columns apart)
-      // and shares the stage's weights
+      // and shares the stage's weights; tap row r of a column group reads the
+      // input box from row r of the tile (16 pixel rows, two swizzle atoms,
+      // further on)
       for (int kk = 0; kk < (p.kc >> 4); ++kk)
-        for (int u = 0; u < p.mt; ++u)
-          mma_bf16(tmem + (uint32_t)(u * p.ntile), smem_desc_sw(sa + u * sub_bytes + kk * 32, sbo, p.layout),
-                   smem_desc_sw(sb + kk * 32, sbo, p.layout), idesc, (it | kk) != 0);
+        for (int r = 0; r < p.tap_rows; ++r)
+          for (int u = 0; u < p.mt; ++u)
+            mma_bf16(tmem + (uint32_t)(u * p.ntile),
+                     smem_desc_sw(sa + u * sub_bytes + r * 16u * 2u * p.kc + kk * 32, sbo, p.layout),
+                     smem_desc_sw(sb + r * p.b_box + kk * 32, sbo, p.layout), idesc, (it | kk | r) != 0);
       mma_commit(&empty[s]);
       if (issued < iters) {
         const int s2 = issued % S;
@@ -613,7 +629,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) conv_ws_kernel(const __grid_con
           }
           const int tap = it / nchunk, c0 = (it - tap * nchunk) * p.kc;
           const uint32_t sa = base + s * p.stage_bytes;
-          mbar_expect_tx(&full[s], p.a_bytes + p.b_bytes);
+          mbar_expect_tx(&full[s], p.a_box + p.b_bytes);
           tma_load_4d(sa, &map_x, c0, x0 + tap % p.ks - half, y0 + tap / p.ks - half, b, &full[s]);
           tma_load_2d(sa + p.a_bytes, &map_w, tap * p.cin + c0, n0, &full[s]);
           ++g;
@@ -1246,6 +1262,7 @@ int smem_for(int stage_bytes, int tmem_cols) {
 int g_conv_path = SHY_SG_CONV_TMA;
 int g_conv_stages = 0;  // 0: chosen per convolution
 int g_conv_pixels = 0;  // pixels per tile, 128 or 256; 0: chosen per convolution
+int g_conv_tap_rows = 3;  // 3x3 taps per stage on the TMA path: 3 (a kernel column) or 1
 int g_wgrad_pixels = 0, g_wgrad_stages = 0;  // 0: chosen per convolution
 
 // cuTensorMapEncodeTiled from the driver, looked up once through the runtime.
@@ -1290,9 +1307,10 @@ bool encode_act_map(CUtensorMap* m, const void* ptr, int channels, int width, in
 // Tensor maps of one convolution: the input (encode_act_map) and the
 // weights as (taps * cin, cout) with a box of kc x ntile.
 bool encode_conv_maps(const shy_sg_conv_desc* d, const void* x, int xs, const void* w, int kc, int ntile, int mt,
-                      CUtensorMap* mx, CUtensorMap* mw) {
+                      int tap_rows, CUtensorMap* mx, CUtensorMap* mw) {
   auto fn = encode_tiled();
-  if (!fn || !encode_act_map(mx, x, d->cin, d->width, d->height, d->batch, xs, kc, kTileH * mt)) return false;
+  if (!fn || !encode_act_map(mx, x, d->cin, d->width, d->height, d->batch, xs, kc, kTileH * mt + tap_rows - 1))
+    return false;
   const cuuint64_t k = (cuuint64_t)d->ksize * d->ksize * d->cin;
   const cuuint64_t gw[2] = {k, (cuuint64_t)d->cout};
   const cuuint64_t sw2[1] = {k * 2};
@@ -1364,7 +1382,9 @@ int conv_launch(const char* fn, const shy_sg_conv_desc* d, const void* x, int32_
   const int pix = d->tile ? d->tile : g_conv_pixels;
   const int mt = pix ? pix / kTileM : 1;
   const bool tma_path = g_conv_path == SHY_SG_CONV_TMA || g_conv_path == SHY_SG_CONV_PERSISTENT;
-  if (tma_path && encode_conv_maps(d, x, x_stride, w, kc, ntile, mt, &mx, &mw)) {
+  // 3x3 on the one-CTA-per-tile TMA path: one input box per kernel column
+  const int tap_rows = (g_conv_path == SHY_SG_CONV_TMA && d->ksize == 3 && g_conv_tap_rows == 3) ? 3 : 1;
+  if (tma_path && encode_conv_maps(d, x, x_stride, w, kc, ntile, mt, tap_rows, &mx, &mw)) {
     ConvTma p{};
     p.bias = bias;
     p.z = z;
@@ -1389,14 +1409,17 @@ int conv_launch(const char* fn, const shy_sg_conv_desc* d, const void* x, int32_
     p.tmem_cols = pow2_cols(ntile * mt);
     p.tiles_w = (d->width + kTileW - 1) / kTileW;
     p.tiles_h = (d->height + kTileH * mt - 1) / (kTileH * mt);
-    p.a_bytes = (uint32_t)kTileM * mt * kc * 2;
-    p.b_bytes = (uint32_t)ntile * kc * 2;
-    p.stage_bytes = p.a_bytes + ((p.b_bytes + 1023u) & ~1023u);
+    p.tap_rows = tap_rows;
+    p.a_box = (uint32_t)kTileW * (kTileH * mt + tap_rows - 1) * kc * 2;
+    p.a_bytes = (p.a_box + 1023u) & ~1023u;
+    p.b_box = ((uint32_t)ntile * kc * 2 + 1023u) & ~1023u;
+    p.b_bytes = (uint32_t)tap_rows * ntile * kc * 2;
+    p.stage_bytes = p.a_bytes + tap_rows * p.b_box;
     p.layout = kc == 64 ? 2u : kc == 32 ? 4u : 6u;
     // automatic depth: 3 stages (two CTAs an SM) for long 64-channel K loops,
     // else 2 (measured at the training shapes: 543 vs 476 TFLOP/s on the
     // 384 -> 128 layer, 269 vs 242 on 96 -> 32)
-    const int iters = d->ksize * d->ksize * (d->cin / kc);
+    const int iters = d->ksize * d->ksize / tap_rows * (d->cin / kc);
     const int st = d->stages ? d->stages : g_conv_stages;
     const int want = st ? st : (kc == 64 && iters >= 16 && mt == 1 ? 3 : 2);
     p.stages = std::max(2, std::min(want, (200 * 1024 - 1024) / (int)p.stage_bytes));
@@ -1797,6 +1820,15 @@ extern "C" int shy_sg_set_wgrad_tile(int32_t pixels, int32_t stages) {
   }
   g_wgrad_pixels = pixels;
   g_wgrad_stages = stages;
+  return SHY_OK;
+}
+
+extern "C" int shy_sg_set_conv_tap_rows(int32_t rows) {
+  if (rows != 1 && rows != 3) {
+    set_error("shy_sg_set_conv_tap_rows: %d (1 or 3)", rows);
+    return SHY_ERR_INVALID_ARG;
+  }
+  g_conv_tap_rows = rows;
   return SHY_OK;
 }
 

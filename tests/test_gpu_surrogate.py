@@ -80,12 +80,16 @@ CONV_CASES = [  # batch, h, w, cin, cout, k, x pixel stride
 ]
 
 
-@pytest.fixture(params=[0, 1, 2], ids=["tma", "staged", "persistent"])
+@pytest.fixture(params=[0, 3, 1, 2], ids=["tma", "tma-tap-by-tap", "staged", "persistent"])
 def conv_path(request, sg):
-    """The operand-staging paths of the convolutions; the TMA path is restored after."""
-    ok(lib().shy_sg_set_conv_path(request.param))
-    yield request.param
+    """The operand-staging paths of the convolutions (3: the TMA path with one
+    input box per tap); the TMA path is restored after."""
+    path = 0 if request.param == 3 else request.param
+    ok(lib().shy_sg_set_conv_path(path))
+    ok(lib().shy_sg_set_conv_tap_rows(1 if request.param == 3 else 3))
+    yield path
     ok(lib().shy_sg_set_conv_path(0))
+    ok(lib().shy_sg_set_conv_tap_rows(3))
 
 
 @pytest.fixture(params=[(0, 0), (256, 2), (256, 3), (128, 4)], ids=["auto", "256px2", "256px3", "128px4"])
