@@ -262,3 +262,24 @@ def test_training_loop_crops_flips_and_schedule():
             assert found
     lrs = [lr for _, _, lr in net.steps]
     assert lrs[0] == pytest.approx(1e-3) and all(a > b for a, b in zip(lrs, lrs[1:])) and lrs[-1] > 0
+
+
+def test_tuning_settings_reject_bad_values(shy):
+    lib = shy._capi.lib()
+    bad = shy._capi.SHY_ERR_INVALID_ARG
+    assert lib.shy_sg_set_conv_path(7) == bad
+    assert lib.shy_sg_set_conv_tile(100, 0) == bad and lib.shy_sg_set_conv_tile(128, 9) == bad
+    assert lib.shy_sg_set_wgrad_tile(32, 0) == bad and lib.shy_sg_set_wgrad_tile(64, 1) == bad
+    assert lib.shy_sg_set_conv_tap_rows(2) == bad
+    assert "shy_sg_set_conv_tap_rows" in lib.shy_last_error().decode()
+    # valid values are accepted, and the defaults put back
+    for call in ((lib.shy_sg_set_conv_tile, (256, 3)), (lib.shy_sg_set_wgrad_tile, (64, 2)),
+                 (lib.shy_sg_set_conv_tap_rows, (1,)), (lib.shy_sg_set_conv_path, (2,))):
+        assert call[0](*call[1]) == shy._capi.SHY_OK
+    assert lib.shy_sg_set_conv_tile(0, 0) == 0 and lib.shy_sg_set_wgrad_tile(0, 0) == 0
+    assert lib.shy_sg_set_conv_tap_rows(3) == 0 and lib.shy_sg_set_conv_path(0) == 0
+    # a descriptor's own tile is checked per call, before any device work
+    import ctypes as C
+    d = shy._capi.SgConvDesc(1, 8, 8, 16, 16, 3, 96, 0)
+    assert lib.shy_sg_conv_forward(C.byref(d), C.c_void_p(16), 16, C.c_void_p(16), None, C.c_void_p(16), 16, 0,
+                                   None, 0, 0, 0, None) == bad
