@@ -772,7 +772,7 @@ def run_surrogate_step(args):
         "gpu_launches": (net.launches - launches0),
         "inference_1024": {"ms": infer_ms,
                            "tflops": 1024 * 1024 * sg.flops_per_pixel(False) / (infer_ms / 1e3) / 1e12},
-        "autotune": {f"{n}/{k}": f"{v[0]}px x{v[1]}" for (n, k), v in tuned.items()},
+        "autotune": {f"{n}/{k}": "x".join(str(c) for c in v[0]) for (n, k), v in tuned.items()},
         "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
                      "peak_source": src, "kernel": "whole training step (convolutions 80 % of its time)",
                      "traffic": None},

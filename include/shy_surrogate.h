@@ -33,14 +33,15 @@ extern "C" {
 
 /* Shape of one convolution: input and output share batch x height x width
  * (zero padding keeps the size); ksize is 1 or 3; cin and cout are
- * multiples of 16.  tile and stages tune the TMA pipeline for this call
- * (0: the process-wide setting, see shy_sg_set_conv_tile and
- * shy_sg_set_wgrad_tile): pixels per tile (forward 128 or 256, weight
- * gradient 64 or 128) and stages (2..8). */
+ * multiples of 16.  tile, stages and tap_rows tune the TMA pipeline for
+ * this call (0: the process-wide setting, see shy_sg_set_conv_tile,
+ * shy_sg_set_wgrad_tile and shy_sg_set_conv_tap_rows): pixels per tile
+ * (forward 128 or 256, weight gradient 64 or 128), stages (2..8), and taps
+ * per stage of a 3x3 forward or input gradient (1 or 3). */
 typedef struct shy_sg_conv_desc {
   int32_t batch, height, width;
   int32_t cin, cout, ksize;
-  int32_t tile, stages;
+  int32_t tile, stages, tap_rows;
 } shy_sg_conv_desc;
 
 #define SHY_SG_ACT_NONE 0

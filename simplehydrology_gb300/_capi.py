@@ -90,7 +90,7 @@ class ShyError(RuntimeError):
 class SgConvDesc(C.Structure):
     _fields_ = [("batch", C.c_int32), ("height", C.c_int32), ("width", C.c_int32),
                 ("cin", C.c_int32), ("cout", C.c_int32), ("ksize", C.c_int32),
-                ("tile", C.c_int32), ("stages", C.c_int32)]
+                ("tile", C.c_int32), ("stages", C.c_int32), ("tap_rows", C.c_int32)]
 
 
 class SgAdamw(C.Structure):

@@ -1383,7 +1383,12 @@ int conv_launch(const char* fn, const shy_sg_conv_desc* d, const void* x, int32_
   const int mt = pix ? pix / kTileM : 1;
   const bool tma_path = g_conv_path == SHY_SG_CONV_TMA || g_conv_path == SHY_SG_CONV_PERSISTENT;
   // 3x3 on the one-CTA-per-tile TMA path: one input box per kernel column
-  const int tap_rows = (g_conv_path == SHY_SG_CONV_TMA && d->ksize == 3 && g_conv_tap_rows == 3) ? 3 : 1;
+  if (d->tap_rows != 0 && d->tap_rows != 1 && d->tap_rows != 3) {
+    set_error("%s: tap_rows %d (0, 1 or 3)", fn, d->tap_rows);
+    return SHY_ERR_INVALID_ARG;
+  }
+  const int rows_want = d->tap_rows ? d->tap_rows : g_conv_tap_rows;
+  const int tap_rows = (g_conv_path == SHY_SG_CONV_TMA && d->ksize == 3 && rows_want == 3) ? 3 : 1;
   if (tma_path && encode_conv_maps(d, x, x_stride, w, kc, ntile, mt, tap_rows, &mx, &mw)) {
     ConvTma p{};
     p.bias = bias;

@@ -54,8 +54,11 @@ CHANNELS = (32, 64, 128, 256)
 ACT_NONE, ACT_GELU = 0, 1
 LEVEL = {"enc0a": 0, "enc0b": 0, "enc1a": 1, "enc1b": 1, "enc2a": 2, "enc2b": 2, "mid": 3,
          "dec2a": 2, "dec2b": 2, "dec1a": 1, "dec1b": 1, "dec0a": 0, "dec0b": 0, "head": 0}
-# TMA pipeline candidates (pixels per tile, stages) the autotuner times
-CONV_TILES = ((128, 2), (128, 3), (256, 2), (256, 3))
+# TMA pipeline candidates the autotuner times: (pixels per tile, stages,
+# taps per stage) for forward and input-gradient convolutions (taps per
+# stage 3 applies to 3x3 kernels), (pixels per stage, stages) for weight
+# gradients
+CONV_TILES = tuple((px, st, rows) for rows in (1, 3) for px in (128, 256) for st in (2, 3))
 WGRAD_TILES = ((64, 2), (64, 3), (128, 2), (128, 3))
 
 
@@ -196,7 +199,7 @@ class Surrogate:
         self._ws = {}
         self._prepped = False
         self.launches = 0
-        self.tune = {}  # (layer, "fwd" | "dgrad" | "wgrad") -> (pixels per tile, stages)
+        self.tune = {}  # (layer, "fwd" | "dgrad" | "wgrad") -> a CONV_TILES or WGRAD_TILES entry
 
     # -- plumbing ---------------------------------------------------------
     def _stream(self):
@@ -234,8 +237,8 @@ class Surrogate:
         B, H, W = ws.shape
         lv = LEVEL[name]
         ci, co = (L["cout"], L["cin"]) if kind == "dgrad" else (L["cin"], L["cout"])
-        tile, stages = self.tune.get((name, kind), (0, 0))
-        return SgConvDesc(B, H >> lv, W >> lv, ci, co, L["k"], tile, stages)
+        tile, stages, rows = (tuple(self.tune.get((name, kind), ())) + (0, 0, 0))[:3]
+        return SgConvDesc(B, H >> lv, W >> lv, ci, co, L["k"], tile, stages, rows)
 
     def _conv(self, ws, name, x, xs, z, zs, zo, a, as_, ao, act):
         L = self.layers[name]
@@ -372,7 +375,7 @@ class Surrogate:
         """Time every TMA tile candidate for each layer's forward, input- and
         weight-gradient convolution at this batch shape (CUDA events, scratch
         outputs) and keep the fastest for later calls.  Returns
-        {(layer, kind): (pixels, stages, ms)}."""
+        {(layer, kind): (candidate, ms)}."""
         torch = self.torch
         if not self._prepped:
             self.prep_weights()
@@ -391,8 +394,9 @@ class Surrogate:
             kinds = ("fwd", "wgrad") if name == "enc0a" else ("fwd", "dgrad", "wgrad")
             for kind in kinds:
                 best = None
-                for tile, stages in (WGRAD_TILES if kind == "wgrad" else CONV_TILES):
-                    self.tune[(name, kind)] = (tile, stages)
+                cands = WGRAD_TILES if kind == "wgrad" else [c for c in CONV_TILES if k == 3 or c[2] == 1]
+                for cand in cands:
+                    self.tune[(name, kind)] = cand
                     d = self._desc(ws, name, kind)
                     if kind == "fwd":
                         fn = lambda: self._call("shy_sg_conv_forward", C.byref(d), self._p(x), xs,  # noqa: E731
@@ -410,9 +414,9 @@ class Surrogate:
                     ev[1].record(stream)
                     ev[1].synchronize()
                     ms = ev[0].elapsed_time(ev[1]) / reps
-                    if best is None or ms < best[2]:
-                        best = (tile, stages, ms)
-                self.tune[(name, kind)] = best[:2]
+                    if best is None or ms < best[1]:
+                        best = (cand, ms)
+                self.tune[(name, kind)] = best[0]
                 out[(name, kind)] = best
         self.status()
         return out
