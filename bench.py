@@ -388,6 +388,29 @@ def run_ours(args):
         e2e_value = e2e_units / e2e_s
         nbytes = wl.cells * 4 * len(FIELDS)
 
+    # the whole workload beside the headline window: cycles 0 .. whole-1
+    # from the initial terrain, device time (later cycles carry fewer
+    # drop-steps as the terrain wears down)
+    whole = None
+    if args.workload == "plain" and args.whole_cycles > 0:
+        wl.reset()
+        w.reset_stats()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+        for _ in range(args.whole_cycles):
+            wl.erode()
+        with torch.cuda.stream(stream):
+            ev[1].record(stream)
+        torch.cuda.synchronize()
+        whole_s = ev[0].elapsed_time(ev[1]) / 1e3
+        ws_ = w.stats()
+        whole = {"cycles": args.whole_cycles, "value": ws_.drop_steps / whole_s, "unit": METRIC,
+                 "ms_per_cycle": whole_s * 1e3 / args.whole_cycles,
+                 "drop_steps_per_cycle": ws_.drop_steps / args.whole_cycles,
+                 "timing": "device time of all cycles back to back (CUDA events), no L2 flush"}
+
     config = dict(wl.config)
     config.update({"step": "one erosion cycle",
                    "cycles_timed": f"0-{args.steps - 1} of the workload, from the initial terrain",
@@ -420,6 +443,8 @@ def run_ours(args):
                                           [b - a for a, b in zip(ph0, ph1)]))},
         "drop_steps": steps_total, "wall_s": wall,
     }
+    if whole:
+        out["whole_workload"] = whole
     out["clocks"] = clk.summary()
     if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
@@ -800,8 +825,10 @@ def main():
     ap.add_argument("--drops", type=int, default=DROPS)
     ap.add_argument("--no-e2e", action="store_true")
     # the batched-terrain configuration (not the default bench line)
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "converge", "large", "surrogate",
-                                                              "surrogate-step"])
+    # default: the single-terrain workload on one GPU; with N > 1 the
+    # batched-terrain workload, sharded by whole terrain across the ranks
+    ap.add_argument("--workload", default=None, choices=["plain", "batch", "converge", "large", "surrogate",
+                                                           "surrogate-step"])
     ap.add_argument("--ref-cycles", type=int, default=2000)
     ap.add_argument("--check-every", type=int, default=10)
     ap.add_argument("--terrains", type=int, default=64)
@@ -811,7 +838,11 @@ def main():
     ap.add_argument("--epochs", type=int, default=24)
     ap.add_argument("--eval-terrains", type=int, default=2)
     ap.add_argument("--train-side", type=int, default=256)
+    ap.add_argument("--whole-cycles", type=int, default=500,
+                    help="cycles of the whole-workload average reported beside the headline (0: skip)")
     args = ap.parse_args()
+    if args.workload is None:
+        args.workload = "batch" if args.gpus > 1 else "plain"
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     if args.impl == "reference":

@@ -173,6 +173,18 @@ int shy_world_lockstep_profile(shy_world* w, double* phase_ms, uint64_t* iterati
  * Results do not depend on either setting. */
 int shy_world_set_launch(shy_world* w, int grid, int order);
 
+/* Test hook for the library's bounded device waits (no counterpart in the
+ * reference, which has no device code).  While `ns` is non-zero, the first
+ * bounded wait of every batched-erosion launch (its first grid barrier) and
+ * of every surrogate TMA convolution (conv_tma path) waits for an event that
+ * never happens, gives up after `ns` nanoseconds and takes the kernel's
+ * give-up path: the batched call returns SHY_ERR_TIMEOUT (its world stays
+ * usable: the failed cycle's pending sums and counts are cleared, its
+ * heights are what the cycle had reached), the convolution's error shows in
+ * shy_sg_status().  Nothing faults or hangs.  0 (the default) turns the hook
+ * off; at most 1e10 ns.  Process-wide. */
+int shy_debug_stall_waits(uint64_t ns);
+
 /* Source of erf(0.4 * discharge) (source/cellpool.h:242-244) for the exact
  * mode.  SHY_ERF_DEVICE (default) is the library's own erf, evaluated on the
  * GPU and correctly rounded to float.  SHY_ERF_HOST_LIBM evaluates the host C
@@ -299,9 +311,13 @@ int shy_terrain_init(shy_world* w, int terrain, int32_t seed);
  * 0.  Every GPU that loads the library holds that array until the process
  * exits.  All calls on a device share it: calls that overlap on the GPU (from
  * other threads or other streams) race and corrupt each other's results, so
- * serialise them.  The first call on each device looks up the array's device
- * address (cudaGetSymbolAddress); make that first call before capturing any
- * stream into a CUDA graph. */
+ * serialise them.  The call copies its status to the host and synchronizes
+ * `stream` before it returns, so it must not be issued on a stream that is
+ * being captured into a CUDA graph.  The first call on each device also looks
+ * up the array's device address (cudaGetSymbolAddress); while another stream
+ * of the process is being captured, make sure that first call has already
+ * happened.  Each map must be device (or managed) memory of the current
+ * device; anything else fails with SHY_ERR_INVALID_ARG before any launch. */
 #define SHY_NOALLOC_MAX_CELLS (256 * 256)
 #define SHY_NOALLOC_MAX_DROPS 16384
 #define SHY_NOALLOC_MAX_AGE 4096

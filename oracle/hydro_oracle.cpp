@@ -766,6 +766,33 @@ void vegetation_step(Grid<float>& g, float* plant, const shy_params& P, uint64_t
 // octaves, lacunarity 2, gain 0.5, weighted strength 0, fractal bounding
 // 1 / 1.75, and the OpenSimplex2 3D rotation of the coordinates.  Integer
 // arithmetic is done on uint32_t, which wraps as the library's int does.
+//
+// FnlNoise follows FastNoiseLite's OpenSimplex2 3D evaluation closely, as
+// bit parity requires, so it is a derivative of that library and carries its
+// licence:
+//
+//   MIT License
+//   Copyright(c) 2020 Jordan Peck (jordan.me2@gmail.com)
+//   Copyright(c) 2020 Contributors
+//
+//   Permission is hereby granted, free of charge, to any person obtaining a
+//   copy of this software and associated documentation files(the
+//   "Software"), to deal in the Software without restriction, including
+//   without limitation the rights to use, copy, modify, merge, publish,
+//   distribute, sublicense, and / or sell copies of the Software, and to
+//   permit persons to whom the Software is furnished to do so, subject to
+//   the following conditions :
+//
+//   The above copyright notice and this permission notice shall be included
+//   in all copies or substantial portions of the Software.
+//
+//   THE SOFTWARE IS PROVIDED "AS IS", WITHOUT WARRANTY OF ANY KIND, EXPRESS
+//   OR IMPLIED, INCLUDING BUT NOT LIMITED TO THE WARRANTIES OF
+//   MERCHANTABILITY, FITNESS FOR A PARTICULAR PURPOSE AND NONINFRINGEMENT.
+//   IN NO EVENT SHALL THE AUTHORS OR COPYRIGHT HOLDERS BE LIABLE FOR ANY
+//   CLAIM, DAMAGES OR OTHER LIABILITY, WHETHER IN AN ACTION OF CONTRACT,
+//   TORT OR OTHERWISE, ARISING FROM, OUT OF OR IN CONNECTION WITH THE
+//   SOFTWARE OR THE USE OR OTHER DEALINGS IN THE SOFTWARE.
 struct FnlNoise {
   float frequency = 0.01f;
   static constexpr uint32_t kPx = 501125321u, kPy = 1136930381u, kPz = 1720413743u;

@@ -69,9 +69,17 @@ class GridF64(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("f", C.POINTER(C.c_double) * 8)]
 
 
+# The reference checkout the harness compiles from: SHY_REFERENCE, else the
+# place this build's container mounts it (absent on machines without it).
+REFERENCE_DIR = os.environ.get("SHY_REFERENCE", "/root/reference")
+
+
 def build(quiet: bool = True) -> None:
     """Build liboracle.so (and the reference harness where the checkout exists)."""
-    out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    cmd = ["make", "-C", HERE]
+    if os.path.isfile(os.path.join(REFERENCE_DIR, "source", "world.h")):
+        cmd.append("REF=" + REFERENCE_DIR)
+    out = subprocess.run(cmd, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:

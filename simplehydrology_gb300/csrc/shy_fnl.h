@@ -16,6 +16,34 @@
 // -ffp-contract=off) the device gives the reference's bits.  Integer hashes
 // use unsigned 32-bit arithmetic, which wraps exactly as the library's
 // signed arithmetic does on every target.
+//
+// shy_fnl_os2 follows FastNoiseLite's SingleOpenSimplex2 (3D) closely, as
+// bit parity with the reference's terrain requires, so this file is a
+// derivative of that library and carries its licence:
+//
+//   MIT License
+//
+//   Copyright(c) 2020 Jordan Peck (jordan.me2@gmail.com)
+//   Copyright(c) 2020 Contributors
+//
+//   Permission is hereby granted, free of charge, to any person obtaining a
+//   copy of this software and associated documentation files(the
+//   "Software"), to deal in the Software without restriction, including
+//   without limitation the rights to use, copy, modify, merge, publish,
+//   distribute, sublicense, and / or sell copies of the Software, and to
+//   permit persons to whom the Software is furnished to do so, subject to
+//   the following conditions :
+//
+//   The above copyright notice and this permission notice shall be included
+//   in all copies or substantial portions of the Software.
+//
+//   THE SOFTWARE IS PROVIDED "AS IS", WITHOUT WARRANTY OF ANY KIND, EXPRESS
+//   OR IMPLIED, INCLUDING BUT NOT LIMITED TO THE WARRANTIES OF
+//   MERCHANTABILITY, FITNESS FOR A PARTICULAR PURPOSE AND NONINFRINGEMENT.
+//   IN NO EVENT SHALL THE AUTHORS OR COPYRIGHT HOLDERS BE LIABLE FOR ANY
+//   CLAIM, DAMAGES OR OTHER LIABILITY, WHETHER IN AN ACTION OF CONTRACT,
+//   TORT OR OTHERWISE, ARISING FROM, OUT OF OR IN CONNECTION WITH THE
+//   SOFTWARE OR THE USE OR OTHER DEALINGS IN THE SOFTWARE.
 #pragma once
 
 #include <stdint.h>

@@ -240,6 +240,12 @@ cudaError_t launch_cascade(shy_world* w, int terrain, float x, float y);
 cudaError_t launch_normals(shy_world* w, int terrain, float* out3);
 cudaError_t launch_batched_cycle(shy_world* w);
 cudaError_t launch_heights_to_fixed(shy_world* w);
+// clears what a batched cycle that gave up left behind (pending sums, drop
+// counts, barrier state)
+cudaError_t launch_batched_recover(shy_world* w);
+// the bounded-wait test hook (shy_debug_stall_waits): 0, or how long the
+// first bounded wait of each kernel waits for an event that never comes
+unsigned long long debug_stall_ns();
 cudaError_t launch_vegetation_step(shy_world* w);
 // the reference's init terrain (source/cellpool.h:349-409) into terrain t's
 // heights; `minmax` is two device words of scratch
@@ -255,6 +261,9 @@ cudaError_t launch_unpack_state(shy_world* w, int t, float* d, float* mx, float*
 // timing: open a launch interval of `kind` (returns the pair index or -1)
 cudaError_t timing_begin(shy_world* w, int kind, int* slot);
 cudaError_t timing_end(shy_world* w, int slot);
+
+// the parameter checks every entry point that takes a shy_params applies
+bool params_valid(const shy_params* p);
 
 void set_error(const char* fmt, ...);
 int cuda_fail(cudaError_t e, const char* what);

@@ -136,14 +136,17 @@ __device__ __forceinline__ unsigned long long arr_bit(int x, int y) {
 // bar->abort and every later barrier returns false at once, so the kernel
 // always ends.  Warps 1 and up run `work` while thread 0 waits: work that
 // neither reads what other CTAs write before the barrier nor writes what they
-// read.
+// read.  `extra` arrivals beyond the grid's are awaited and `limit_ns`
+// bounds the wait: the bounded-wait test hook (shy_debug_stall_waits) asks
+// for one arrival that never comes, so the wait runs out.
 template <class Work>
-__device__ bool grid_barrier(GridBar* bar, unsigned& passed, unsigned long long* live, Work&& work) {
+__device__ bool grid_barrier(GridBar* bar, unsigned& passed, unsigned long long* live, Work&& work,
+                             unsigned extra = 0, unsigned long long limit_ns = kBarrierLimitNs) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x >= 32) work();
   if (threadIdx.x == 0) {
-    const unsigned long long target = (unsigned long long)(passed + 1) * gridDim.x;
+    const unsigned long long target = (unsigned long long)(passed + 1) * gridDim.x + extra;
     red_release_add_u64(&bar->arrive, 1ull);
     int ok = 1;
     unsigned long long t0 = 0;
@@ -155,7 +158,7 @@ __device__ bool grid_barrier(GridBar* bar, unsigned& passed, unsigned long long*
         ok = 0;
         break;
       }
-      if (global_ns() - t0 > kBarrierLimitNs) {
+      if (global_ns() - t0 > limit_ns) {
         atomicExch(&bar->abort, 1);
         atomicCAS(&bar->error, 0, SHY_ERR_TIMEOUT);
         ok = 0;
@@ -239,6 +242,7 @@ struct LockArgs {
   DevStats* st;
   GridBar* bar;
   int max_steps;
+  unsigned long long stall_ns;  // test hook: the first barrier waits this long for a missing arrival
 };
 
 // The drop slots [lo, lo + n) of one CTA.
@@ -549,7 +553,8 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     const unsigned long long s = block_sum_u64(born);
     if (threadIdx.x == 0 && s) atomicAdd(&a.bar->live, s);
   }
-  bool ok = grid_barrier(a.bar, passed, &s_live);
+  bool ok = grid_barrier(a.bar, passed, &s_live, [] {}, a.stall_ns ? 1u : 0u,
+                         a.stall_ns ? a.stall_ns : kBarrierLimitNs);
 
   int step = 0;
   for (; ok && step < a.max_steps; ++step) {
@@ -1097,6 +1102,7 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.st = w->stats;
   a.bar = w->bar;
   a.max_steps = (int)w->P.max_age + 3;
+  a.stall_ns = debug_stall_ns();
 
   int slot = -1;
   cudaError_t e;
@@ -1162,10 +1168,38 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.st = b.st;
   a.bar = b.bar;
   a.max_steps = (int)b.P.max_age + 3;
+  a.stall_ns = debug_stall_ns();
   cudaError_t e = launch_lockstep(a, b.sm_count, 0, stream);
   if (e != cudaSuccess) return e;
   cycle_end_kernel<<<cells_grid(b.cells), 256, 0, stream>>>(b.trk, b.rec, b.track_f, b.cq, b.h, b.cells, b.P,
                                                             b.bar, b.st);
+  return cudaGetLastError();
+}
+
+namespace {
+
+// After a cycle that gave up (a timed-out barrier): the pending sums and
+// drop counts it left behind are cleared and the barrier state reset, so the
+// world's next batched call starts clean.
+__global__ void batched_recover_kernel(CellQ* __restrict__ cq, long long cells, GridBar* bar) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells;
+       i += (long long)gridDim.x * blockDim.x) {
+    cq[i].e = 0;
+    cq[i].cnt[0] = 0;
+    cq[i].cnt[1] = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    bar->arrive = 0;
+    bar->live = 0;
+    bar->abort = 0;
+    bar->error = 0;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_batched_recover(shy_world* w) {
+  batched_recover_kernel<<<cells_grid(w->cells), 256, 0, w->stream>>>(w->cq, w->cells, w->bar);
   return cudaGetLastError();
 }
 

@@ -144,9 +144,10 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
               SHY_NOALLOC_MAX_DROPS);
     return SHY_ERR_INVALID_ARG;
   }
-  if (!(params->max_age >= 0.0f) || params->max_age > (float)SHY_NOALLOC_MAX_AGE || params->evap_rate < 0.0f ||
-      params->evap_rate >= 1.0f) {
-    set_error("shy_erode_noalloc: max_age must lie in [0, %d] and evap_rate in [0, 1)", SHY_NOALLOC_MAX_AGE);
+  // the allocating path's checks (NaN fails them), plus the table's limit
+  if (!params_valid(params) || params->max_age > (float)SHY_NOALLOC_MAX_AGE) {
+    set_error("shy_erode_noalloc: invalid parameters (max_age must lie in [0, %d], evap_rate in [0, 1), "
+              "map_scale finite)", SHY_NOALLOC_MAX_AGE);
     return SHY_ERR_INVALID_ARG;
   }
   if (params->cascade_passes != 0) {
@@ -161,6 +162,25 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return cuda_fail(e, "shy_erode_noalloc: device");
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
     return cuda_fail(e, "shy_erode_noalloc: device attributes");
+  // Every map must be device (or managed) memory of the current device: a
+  // host pointer would otherwise become a fault inside the first kernel.
+  // cudaPointerGetAttributes allocates nothing.
+  const void* maps[5] = {height, discharge, momentum_x, momentum_y, root_density};
+  static const char* const names[5] = {"height", "discharge", "momentum_x", "momentum_y", "root_density"};
+  for (int i = 0; i < 5; ++i) {
+    cudaPointerAttributes at;
+    e = cudaPointerGetAttributes(&at, maps[i]);
+    if (e != cudaSuccess) {
+      cudaGetLastError();  // an unknown pointer leaves no sticky error
+      set_error("shy_erode_noalloc: %s is not a CUDA pointer", names[i]);
+      return SHY_ERR_INVALID_ARG;
+    }
+    const bool dev_mem = at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+    if (!dev_mem || (at.type == cudaMemoryTypeDevice && at.device != dev)) {
+      set_error("shy_erode_noalloc: %s is not device memory of the current device", names[i]);
+      return SHY_ERR_INVALID_ARG;
+    }
+  }
 
   const int n = nx * ny;
   Terrain T;

@@ -33,6 +33,7 @@
 // SHY_ERR_TIMEOUT, skips its epilogue and still frees its tensor memory.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <mutex>
 #include <cuda_bf16.h>
 
 #include "../../include/shy_surrogate.h"
@@ -79,12 +80,12 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
 }
 
 // Waits until the phase of `bar` with parity `parity` has completed; gives up
-// after kWaitLimitNs.
-__device__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// after `limit_ns`.
+__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns = kWaitLimitNs) {
   if (mbar_try(bar, parity)) return true;
   const unsigned long long t0 = now_ns();
   while (!mbar_try(bar, parity))
-    if (now_ns() - t0 > kWaitLimitNs) return false;
+    if (now_ns() - t0 > limit_ns) return false;
   return true;
 }
 
@@ -373,6 +374,7 @@ struct ConvTma {
   int tap_rows;  // taps per stage: 3 (one column of a 3x3 kernel, one taller input box) or 1
   uint32_t a_bytes, b_bytes, stage_bytes, layout;
   uint32_t a_box, b_box;  // bytes of the input box and of one weight box (b_bytes: all weight boxes)
+  unsigned long long stall_ns;  // test hook: first wait on a barrier nothing arrives at, this long
 };
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
@@ -416,7 +418,7 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
                                                            const __grid_constant__ CUtensorMap map_w,
                                                            const ConvTma p) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], done;
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], done, never;
   __shared__ uint32_t tmem_slot;
   __shared__ int s_fail;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -435,6 +437,7 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
       mbar_init(&empty[s], 1);
     }
     mbar_init(&done, 1);
+    mbar_init(&never, 1);  // nothing arrives here: the bounded-wait test hook waits on it
     s_fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -470,9 +473,10 @@ __global__ void __launch_bounds__(kThreads) conv_tma_kernel(const __grid_constan
       }
     };
     int issued = 0, consumed = 0;
-    bool fail = false;
-    for (; issued < S - 1 && issued < iters; ++issued) issue(issued);
-    for (int it = 0; it < iters; ++it) {
+    // the test hook: a wait that runs out before anything is issued
+    bool fail = p.stall_ns != 0 && !mbar_wait(&never, 0, p.stall_ns);
+    for (; !fail && issued < S - 1 && issued < iters; ++issued) issue(issued);
+    for (int it = 0; !fail && it < iters; ++it) {
       const int s = it % S;
       if (!mbar_wait(&full[s], (uint32_t)(it / S) & 1u)) {
         fail = true;
@@ -1265,21 +1269,20 @@ int g_conv_pixels = 0;  // pixels per tile, 128 or 256; 0: chosen per convolutio
 int g_conv_tap_rows = 3;  // 3x3 taps per stage on the TMA path: 3 (a kernel column) or 1
 int g_wgrad_pixels = 0, g_wgrad_stages = 0;  // 0: chosen per convolution
 
-// cuTensorMapEncodeTiled from the driver, looked up once through the runtime.
+// cuTensorMapEncodeTiled from the driver, looked up once per process through
+// the runtime (a function-local static: initialised once, thread-safe).
+PFN_cuTensorMapEncodeTiled_v12000 lookup_encode_tiled() {
+  void* f = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+          cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  cudaGetLastError();
+  return nullptr;
+}
 PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-    else
-      cudaGetLastError();
-  }
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = lookup_encode_tiled();
   return fn;
 }
 
@@ -1348,6 +1351,44 @@ bool check_conv_desc(const shy_sg_conv_desc* d, const char* fn) {
 using namespace shy;
 
 namespace {
+
+// Launch set-up of the current device, done once per device under a lock:
+// the dynamic shared-memory limits of the convolution kernels (an attribute
+// of a kernel on one device) and the SM count that sizes persistent and
+// split grids.
+struct DeviceSetup {
+  bool done;
+  int sms;
+};
+const int kMaxDevices = 64;
+std::mutex g_setup_mu;
+DeviceSetup g_setup[kMaxDevices] = {};
+
+const int kConvSmem = 200 * 1024;      // conv_tma, conv_fwd, wgrad kernels
+const int kWsSmem = 227 * 1024 - 1024;  // the persistent convolution
+
+int device_sms() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return 152;
+  }
+  std::lock_guard<std::mutex> lock(g_setup_mu);
+  DeviceSetup& d = g_setup[dev];
+  if (!d.done) {
+    cudaFuncSetAttribute(conv_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmem);
+    cudaFuncSetAttribute(conv_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kWsSmem);
+    cudaFuncSetAttribute(conv_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmem);
+    cudaFuncSetAttribute(wgrad_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmem);
+    cudaFuncSetAttribute(conv_wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmem);
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 152;
+    d.sms = sms;
+    d.done = true;
+  }
+  return d.sms;
+}
+
 // Both convolution entry points: a forward (gz NULL) or an input gradient
 // through a GELU (gz the previous layer's pre-activation, output bf16 to a).
 int conv_launch(const char* fn, const shy_sg_conv_desc* d, const void* x, int32_t x_stride, const void* w,
@@ -1415,6 +1456,7 @@ int conv_launch(const char* fn, const shy_sg_conv_desc* d, const void* x, int32_
     p.tiles_w = (d->width + kTileW - 1) / kTileW;
     p.tiles_h = (d->height + kTileH * mt - 1) / (kTileH * mt);
     p.tap_rows = tap_rows;
+    p.stall_ns = debug_stall_ns();
     p.a_box = (uint32_t)kTileW * (kTileH * mt + tap_rows - 1) * kc * 2;
     p.a_bytes = (p.a_box + 1023u) & ~1023u;
     p.b_box = ((uint32_t)ntile * kc * 2 + 1023u) & ~1023u;
@@ -1429,28 +1471,15 @@ int conv_launch(const char* fn, const shy_sg_conv_desc* d, const void* x, int32_
     const int want = st ? st : (kc == 64 && iters >= 16 && mt == 1 ? 3 : 2);
     p.stages = std::max(2, std::min(want, (200 * 1024 - 1024) / (int)p.stage_bytes));
     const int smem = smem_for((p.stages * (int)p.stage_bytes + 1024) / 2, p.tmem_cols);
-    static bool attr_tma = false;
-    if (!attr_tma) {
-      cudaFuncSetAttribute(conv_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      attr_tma = true;
-    }
+    const int sms = device_sms();
     const long long tiles = (long long)d->batch * p.tiles_h * p.tiles_w;
     if (g_conv_path == SHY_SG_CONV_PERSISTENT) {
       // one CTA per SM, two accumulators, the deepest ring that fits
       p.tmem_cols = pow2_cols(2 * ntile * mt);
-      const int max_smem = 227 * 1024 - 1024;
+      const int max_smem = kWsSmem;
       p.stages = d->stages ? d->stages : std::min(6, (max_smem - 1024) / (int)p.stage_bytes);
       p.stages = std::max(2, std::min(p.stages, (max_smem - 1024) / (int)p.stage_bytes));
       const int ws_smem = std::max(p.stages * (int)p.stage_bytes + 1024, 120 * 1024);
-      static bool attr_ws = false;
-      static int sms = 0;
-      if (!attr_ws) {
-        cudaFuncSetAttribute(conv_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        attr_ws = true;
-      }
       const long long work = tiles * (d->cout / ntile);
       const unsigned grid = (unsigned)std::max(1ll, std::min(work, (long long)std::max(sms, 1)));
       conv_ws_kernel<<<grid, kWsThreads, ws_smem, static_cast<cudaStream_t>(stream)>>>(mx, mw, p);
@@ -1494,11 +1523,7 @@ int conv_launch(const char* fn, const shy_sg_conv_desc* d, const void* x, int32_
   p.tmem_cols = pow2_cols(p.ntile);
   const int stage = (kTileM + p.ntile) * p.kc * 2;
   const int smem = smem_for(stage, p.tmem_cols);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(conv_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  device_sms();
   const long long npix = (long long)d->batch * d->height * d->width;
   dim3 grid((unsigned)((npix + kTileM - 1) / kTileM), (unsigned)(d->cout / p.ntile));
   conv_fwd_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(p);
@@ -1582,14 +1607,10 @@ extern "C" int shy_sg_conv_wgrad(const shy_sg_conv_desc* d, const void* x, int32
     // allocation for either order of the descriptor's two strides
     const int smem = smem_for((q.stages * (int)q.stage_bytes + 1024 + 16384) / 2, q.tmem_cols);
     const long long tiles = (long long)d->batch * q.tiles_h * q.tiles_w;
-    long long splits = std::max(1ll, std::min(tiles, (2ll * 152 + ctas_mn - 1) / ctas_mn));
+    const long long sms = device_sms();
+    long long splits = std::max(1ll, std::min(tiles, (2ll * sms + ctas_mn - 1) / ctas_mn));
     q.tiles_per_split = (tiles + splits - 1) / splits;
     splits = (tiles + q.tiles_per_split - 1) / q.tiles_per_split;
-    static bool attr_w = false;
-    if (!attr_w) {
-      cudaFuncSetAttribute(wgrad_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      attr_w = true;
-    }
     dim3 grid((unsigned)((rows + kTileM - 1) / kTileM), (unsigned)(d->cout / ntile), (unsigned)splits);
     wgrad_tma_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(mx, mdz, q);
     return launch_status(fn);
@@ -1611,16 +1632,12 @@ extern "C" int shy_sg_conv_wgrad(const shy_sg_conv_desc* d, const void* x, int32
   const long long npix = (long long)d->batch * d->height * d->width;
   const long long nchunks = (npix + kWgradK - 1) / kWgradK;
   const int tiles = ((rows + kTileM - 1) / kTileM) * (d->cout / p.ntile);
-  long long splits = std::max(1ll, std::min(nchunks, (4ll * 152 + tiles - 1) / tiles));
+  const long long sms = device_sms();
+  long long splits = std::max(1ll, std::min(nchunks, (4ll * sms + tiles - 1) / tiles));
   p.chunks_per_split = (nchunks + splits - 1) / splits;
   splits = (nchunks + p.chunks_per_split - 1) / p.chunks_per_split;
   const int stage = (kTileM + p.ntile) * kWgradK * 2;
   const int smem = smem_for(stage, p.tmem_cols);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(conv_wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
   dim3 grid((unsigned)((rows + kTileM - 1) / kTileM), (unsigned)(d->cout / p.ntile), (unsigned)splits);
   conv_wgrad_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(p);
   return launch_status(fn);
@@ -1637,7 +1654,8 @@ extern "C" int shy_sg_bias_grad(int64_t pixels, int32_t channels, const void* dz
   if (channels <= 256 && 256 % channels == 0) {
     bias_grad_kernel<<<grid_for(pixels * channels), 256, 0, st>>>(g, dz_stride, pixels, channels, db);
   } else {
-    const long long per = std::max(64ll, (long long)(pixels + 4 * 152 - 1) / (4 * 152));
+    const long long sms4 = 4ll * device_sms();
+    const long long per = std::max(64ll, (long long)(pixels + sms4 - 1) / sms4);
     bias_grad_any_kernel<<<(int)((pixels + per - 1) / per), 128, 0, st>>>(g, dz_stride, pixels, channels, per, db);
   }
   return launch_status("shy_sg_bias_grad");

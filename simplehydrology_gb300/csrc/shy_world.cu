@@ -1,6 +1,7 @@
 // shy_world.cu -- the C ABI (include/shy.h): world lifecycle, field I/O,
 // erosion entry points, counters and timing.  Host code only; the kernels
 // live in shy_exact.cu and shy_lockstep.cu.
+#include <atomic>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -71,17 +72,21 @@ static cudaError_t timing_collect(shy_world* w) {
   return cudaSuccess;
 }
 
-}  // namespace shy
+std::atomic<unsigned long long> g_debug_stall_ns{0};
+unsigned long long debug_stall_ns() { return g_debug_stall_ns.load(std::memory_order_relaxed); }
 
-using namespace shy;
-
-namespace {
-
+// Written so that a NaN in any tested field fails the test.
 bool params_valid(const shy_params* p) {
   return p && p->max_age >= 0.0f && p->max_age < 1.0e6f && p->evap_rate >= 0.0f &&
          p->evap_rate < 1.0f && p->cascade_passes >= 0 && p->cascade_passes <= 64 &&
          isfinite(p->map_scale);
 }
+
+}  // namespace shy
+
+using namespace shy;
+
+namespace {
 
 template <class T> cudaError_t dalloc(T** p, size_t n) {
   return cudaMalloc((void**)p, sizeof(T) * (n ? n : 1));
@@ -174,11 +179,16 @@ int upload_volume_table(shy_world* w) {
   return SHY_OK;
 }
 
+// A batched call's device status.  On an error the cycle's leftovers are
+// cleared (launch_batched_recover) so that the world stays usable; its
+// heights are those the failed cycle had reached.
 int check_device_error(shy_world* w) {
   GridBar b;
   SHY_CHECK_CUDA(cudaMemcpyAsync(&b, w->bar, sizeof(b), cudaMemcpyDeviceToHost, w->stream), "read status");
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
   if (b.error != 0) {
+    SHY_CHECK_CUDA(launch_batched_recover(w), "clear after a failed cycle");
+    SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
     set_error(b.error == SHY_ERR_TIMEOUT ? "a grid barrier of the lock-step kernel timed out"
                                          : "lock-step kernel ended with drops still descending");
     return b.error;
@@ -398,6 +408,15 @@ int world_check(shy_world* w) { return check_world(w); }
 extern "C" {
 
 int shy_version(void) { return SHY_ABI_VERSION; }
+
+int shy_debug_stall_waits(uint64_t ns) {
+  if (ns > 10000000000ull) {
+    set_error("shy_debug_stall_waits: %llu ns is beyond the 10 s a test may wait", (unsigned long long)ns);
+    return SHY_ERR_INVALID_ARG;
+  }
+  g_debug_stall_ns.store(ns, std::memory_order_relaxed);
+  return SHY_OK;
+}
 
 const char* shy_last_error(void) { return g_err; }
 

@@ -104,3 +104,16 @@ def test_cpp_facade_compiles(shy, tmp_path):
                         "-Wl,-rpath," + os.path.dirname(shy._capi.LIB_PATH), "-o", str(exe)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("field,value", [("evap_rate", float("nan")), ("map_scale", float("inf")),
+                                         ("max_age", float("nan")), ("evap_rate", 1.0)])
+def test_noalloc_rejects_invalid_parameters_on_the_host(shy, field, value):
+    """The no-allocation entry point applies the allocating path's parameter
+    checks (a NaN fails them) before it touches a device or a map."""
+    L = shy.lib()
+    p = shy.default_params()
+    setattr(p, field, value)
+    x = C.c_void_p(1)  # never dereferenced: the parameter checks come first
+    rc = L.shy_erode_noalloc(64, 64, C.byref(p), 1, 0, 100, 1, x, x, x, x, x, None, None)
+    assert rc == -1 and b"invalid parameters" in L.shy_last_error()

@@ -61,3 +61,19 @@ def test_noalloc_rejects_requests_beyond_its_scratch(shy):
     assert rc == -1 and b"scratch" in L.shy_last_error()
     rc = L.shy_erode_noalloc(64, 64, C.byref(p), 1, 0, 1 << 20, 1, x, x, x, x, x, None, None)
     assert rc == -1 and b"drops" in L.shy_last_error()
+
+
+def test_noalloc_rejects_host_maps(shy):
+    """A host array passed as a map is refused with an error code before any
+    kernel runs (it would otherwise be read by the device)."""
+    torch = pytest.importorskip("torch")
+    L = shy.lib()
+    p = shy.default_params()
+    nx, ny = 64, 64
+    dev = [torch.zeros((nx, ny), dtype=torch.float32, device="cuda") for _ in range(4)]
+    host = np.zeros((nx, ny), np.float32)
+    ptrs = [t.data_ptr() for t in dev]
+    for i in range(5):
+        args = ptrs[:i] + [host.ctypes.data] + ptrs[i:]
+        rc = L.shy_erode_noalloc(nx, ny, C.byref(p), 1, 0, 100, 1, *args[:5], None, None)
+        assert rc == -1 and b"device memory" in L.shy_last_error(), (i, L.shy_last_error())
