@@ -315,6 +315,17 @@ def run_ours(args):
         wl = PlainWorkload(shy, args.map, args.drops)
     w = wl.w
 
+    # optional: the launch-shape autotuner on the initial state (each
+    # candidate timed over 3 cycles on a checkpoint copy); the bench then
+    # runs with the fastest shape
+    tune = None
+    if args.autotune:
+        from simplehydrology_gb300 import autotune
+        best, times = autotune.autotune(w, None if args.workload == "batch" else wl.drops, cycles=3)
+        tune = {"best": list(best), "ms_per_cycle": {"x".join(str(v) for v in k): round(t * 1e3, 4)
+                                                      for k, t in sorted(times.items(), key=lambda kv: kv[1])},
+                "shape": "grid x order x block x smem_slots (grid 0: every resident CTA)"}
+
     # warm-up on the same workload, then restart from the initial terrain
     for _ in range(args.warmup):
         wl.erode()
@@ -445,6 +456,8 @@ def run_ours(args):
     }
     if whole:
         out["whole_workload"] = whole
+    if tune:
+        out["autotune"] = tune
     out["clocks"] = clk.summary()
     if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
@@ -838,6 +851,8 @@ def main():
     ap.add_argument("--epochs", type=int, default=24)
     ap.add_argument("--eval-terrains", type=int, default=2)
     ap.add_argument("--train-side", type=int, default=256)
+    ap.add_argument("--autotune", action="store_true",
+                    help="run the launch-shape autotuner first and bench the fastest shape")
     ap.add_argument("--whole-cycles", type=int, default=500,
                     help="cycles of the whole-workload average reported beside the headline (0: skip)")
     args = ap.parse_args()

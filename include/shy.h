@@ -172,6 +172,13 @@ int shy_world_lockstep_profile(shy_world* w, double* phase_ms, uint64_t* iterati
  * default) when the cell state is larger than L2, 0 never, 1 always.
  * Results do not depend on either setting. */
 int shy_world_set_launch(shy_world* w, int grid, int order);
+/* CTA size of the batched kernel: `threads` 64, 128 or 256 (the default)
+ * threads per CTA, so that at full residency each CTA owns about that many
+ * drops or fewer (the SM count times the resident CTAs of that size set the
+ * grid); `smem_slots` 1 (default) keeps a CTA's drop slots in shared memory
+ * where they fit without lowering occupancy, 0 always in global memory.
+ * Results do not depend on either setting. */
+int shy_world_set_block(shy_world* w, int threads, int smem_slots);
 
 /* Test hook for the library's bounded device waits (no counterpart in the
  * reference, which has no device code).  While `ns` is non-zero, the first

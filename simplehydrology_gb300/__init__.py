@@ -106,6 +106,11 @@ class _Handle:
         in spawn-cell order (-1: when the state outgrows L2, 0 never, 1 always)."""
         check(lib().shy_world_set_launch(self._w, grid, order))
 
+    def set_block(self, threads: int = 256, smem_slots: int = 1):
+        """Threads per CTA of the batched kernel (64, 128 or 256) and whether
+        drop slots may live in shared memory (1) or always in global (0)."""
+        check(lib().shy_world_set_block(self._w, threads, smem_slots))
+
     def set_cycle(self, cycle: int):
         check(lib().shy_world_set_cycle(self._w, cycle))
 

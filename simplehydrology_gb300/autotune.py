@@ -1,63 +1,105 @@
 """Launch-shape autotuner for the batched mode.
 
-The batched kernel's launch shape -- how many CTAs (so how many drops each
-CTA owns, and whether their slots fit in shared memory) and whether a
-cycle's drops are ordered by spawn cell -- changes its speed, never its
-results.  `autotune` tries candidate shapes on copies of a world's current
-state (through a checkpoint file) and applies the fastest to the world.
+The batched kernel's launch shape changes its speed, never its results:
+
+* the CTA size (64, 128 or 256 threads), hence how many drops each CTA owns
+  at full residency;
+* the grid (every resident CTA, or one CTA per SM), hence also the drops per
+  CTA;
+* whether a cycle's drops are dealt to the CTAs in spawn-cell order;
+* whether a CTA's drop slots may live in shared memory (when they fit) or
+  always in global memory.
+
+`autotune` tries candidate shapes on copies of a world's current state
+(through a checkpoint file), times each over `cycles` cycles with CUDA
+events on the copy's stream, and applies the fastest to the world.
 """
 from __future__ import annotations
 
 import os
 import tempfile
-import time
 
 from . import Batch, World, load
 
+BLOCKS = (64, 128, 256)
+ORDERS = (-1, 0, 1)
 
-def candidates(sm_count: int = 152):
-    """(grid, order) pairs: every resident CTA or one per SM, and the three
-    order settings (-1 automatic, 0 drop order, 1 spawn-cell order)."""
+
+def sm_count(device: int | None = None) -> int:
+    """The SM count of the current (or given) CUDA device."""
+    import torch
+    dev = torch.cuda.current_device() if device is None else device
+    return int(torch.cuda.get_device_properties(dev).multi_processor_count)
+
+
+def candidates(sms: int | None = None, blocks=BLOCKS, orders=ORDERS, smem=(1, 0)):
+    """(grid, order, block, smem_slots) shapes: CTA sizes x (every resident
+    CTA, or one per SM) x the three order settings (-1 automatic, 0 drop
+    order, 1 spawn-cell order) x drop slots in shared memory where they fit
+    or always in global memory."""
+    sms = sm_count() if sms is None else int(sms)
     out = []
-    for grid in (0, sm_count):
-        for order in (-1, 0, 1):
-            out.append((grid, order))
+    for block in blocks:
+        for grid in (0, sms):
+            for order in orders:
+                for sm in smem:
+                    out.append((grid, order, block, sm))
     return out
 
 
-def autotune(world, drops: int | None = None, cycles: int = 1, shapes=None, sm_count: int = 152):
-    """Time `cycles` batched cycles for each launch shape on a copy of
-    `world`'s state and apply the fastest shape to `world`.  `drops` is the
-    drops per cycle for a single-terrain World (a Batch keeps its own).
-    Returns (best_shape, {shape: seconds})."""
+def _full(shape):
+    """(grid, order[, block[, smem_slots]]) with the defaults (256, 1) filled in."""
+    s = tuple(shape)
+    return s + (256, 1)[len(s) - 2:]
+
+
+def apply(world, shape):
+    """Set a (grid, order, block, smem_slots) shape on a World or Batch."""
+    grid, order, block, smem = _full(shape)
+    world.set_launch(grid, order)
+    world.set_block(block, smem)
+
+
+def autotune(world, drops: int | None = None, cycles: int = 3, shapes=None, sms: int | None = None):
+    """Time `cycles` batched cycles (at least 3) for each launch shape on a
+    copy of `world`'s state and apply the fastest shape to `world`.  `drops`
+    is the drops per cycle for a single-terrain World (a Batch keeps its
+    own).  Returns (best_shape, {shape: seconds per cycle})."""
+    import torch
     if isinstance(world, World) and drops is None:
         raise ValueError("drops per cycle is needed for a World")
-    shapes = list(shapes) if shapes is not None else candidates(sm_count)
+    cycles = max(3, int(cycles))
+    shapes = list(shapes) if shapes is not None else candidates(sms)
+    shapes = [_full(s) for s in shapes]
     fd, path = tempfile.mkstemp(suffix=".ckpt")
     os.close(fd)
     times = {}
+
+    def erode(w, n):
+        if isinstance(w, Batch):
+            w.erode(n)
+        else:
+            w.erode(drops, n)
+
     try:
         world.save(path)
         for shape in shapes:
             w = load(path)
             try:
-                w.set_launch(*shape)
-                if isinstance(w, Batch):
-                    w.erode(1)  # first launch of this shape (attribute set-up)
-                else:
-                    w.erode(drops, 1)
+                apply(w, shape)
+                erode(w, 1)  # first launch of this shape (attribute set-up)
                 w.sync()
-                t0 = time.perf_counter()
-                if isinstance(w, Batch):
-                    w.erode(cycles)
-                else:
-                    w.erode(drops, cycles)
+                stream = torch.cuda.ExternalStream(w.stream())
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                ev[0].record(stream)
+                erode(w, cycles)
+                ev[1].record(stream)
                 w.sync()
-                times[shape] = time.perf_counter() - t0
+                times[shape] = ev[0].elapsed_time(ev[1]) / 1e3 / cycles
             finally:
                 w.close()
     finally:
         os.remove(path)
     best = min(times, key=times.get)
-    world.set_launch(*best)
+    apply(world, best)
     return best, times

@@ -186,6 +186,8 @@ struct shy_world {
   int track_mode = 0;         // 0: track_f holds the last call's tracks
   int batch_grid = 0;         // CTAs of the lock-step kernel at most (0: all resident)
   int batch_order = -1;       // slots in spawn-cell order: -1 when the cell state outgrows L2, 0 never, 1 always
+  int batch_block = 256;      // threads per CTA of the lock-step kernel: 64, 128 or 256
+  int batch_smem = 1;         // 0: drop slots in global memory even where shared memory would hold them
 
   shy::Timing timing;
   float* normals = nullptr;   // 3 x cells, lazily allocated

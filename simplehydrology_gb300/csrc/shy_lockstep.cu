@@ -54,6 +54,8 @@ namespace shy {
 
 namespace {
 
+// CTA sizes of the lock-step kernel (threads, one drop slot each while a
+// CTA's slots fit in one pass); 256 unless the world asks otherwise
 const int kLockBlock = 256;
 const int kSmemTerrains = 128;
 // shared-memory bytes per drop slot: its state plus one steep-queue entry
@@ -238,6 +240,7 @@ struct LockArgs {
   long long arr_words;
   const int* order;  // drops sorted by spawn cell (dealt to the CTAs in runs), or null: slot = drop
   int smem_slots;   // 1: drop slots and queue live in dynamic shared memory
+  int smem_allowed;  // 0: keep the slots in global memory even when they would fit
   shy_params P;
   DevStats* st;
   GridBar* bar;
@@ -298,8 +301,9 @@ __device__ __forceinline__ int find_terrain(const Terrain* T, int n, int d) {
   return lo;
 }
 
+template <int kBlock>
 __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v) {
-  __shared__ unsigned long long red[kLockBlock / 32];
+  __shared__ unsigned long long red[kBlock / 32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
@@ -473,6 +477,7 @@ __device__ __forceinline__ void steep_apply(const SteepCell& q, const Terrain& T
 }
 
 // 128 registers: two 256-thread CTAs per SM
+template <int kBlock>
 __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ Terrain sT[kSmemTerrains];
@@ -550,7 +555,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     atomicAdd(&a.cq[c].cnt[0], 1);
   }
   {
-    const unsigned long long s = block_sum_u64(born);
+    const unsigned long long s = block_sum_u64<kBlock>(born);
     if (threadIdx.x == 0 && s) atomicAdd(&a.bar->live, s);
   }
   bool ok = grid_barrier(a.bar, passed, &s_live, [] {}, a.stall_ns ? 1u : 0u,
@@ -817,7 +822,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       }
     }
     {
-      const unsigned long long s = block_sum_u64(retired);
+      const unsigned long long s = block_sum_u64<kBlock>(retired);
       if (threadIdx.x == 0 && s) atomicAdd(&a.bar->live, (unsigned long long)(-(long long)s));
     }
     lap(4);
@@ -828,13 +833,13 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   // counters
   {
     unsigned long long v;
-    v = block_sum_u64(n_steps);   if (threadIdx.x == 0 && v) atomicAdd(&a.st->steps, v);
-    v = block_sum_u64(n_oob);     if (threadIdx.x == 0 && v) atomicAdd(&a.st->oob, v);
-    v = block_sum_u64(n_drops);   if (threadIdx.x == 0 && v) atomicAdd(&a.st->drops, v);
-    v = block_sum_u64(n_skipped); if (threadIdx.x == 0 && v) atomicAdd(&a.st->skipped, v);
-    v = block_sum_u64((unsigned long long)gain_q);
+    v = block_sum_u64<kBlock>(n_steps);   if (threadIdx.x == 0 && v) atomicAdd(&a.st->steps, v);
+    v = block_sum_u64<kBlock>(n_oob);     if (threadIdx.x == 0 && v) atomicAdd(&a.st->oob, v);
+    v = block_sum_u64<kBlock>(n_drops);   if (threadIdx.x == 0 && v) atomicAdd(&a.st->drops, v);
+    v = block_sum_u64<kBlock>(n_skipped); if (threadIdx.x == 0 && v) atomicAdd(&a.st->skipped, v);
+    v = block_sum_u64<kBlock>((unsigned long long)gain_q);
     if (threadIdx.x == 0 && v) atomicAdd((unsigned long long*)&a.st->gain_q, v);
-    v = block_sum_u64((unsigned long long)loss_q);
+    v = block_sum_u64<kBlock>((unsigned long long)loss_q);
     if (threadIdx.x == 0 && v) atomicAdd((unsigned long long*)&a.st->loss_q, v);
   }
   if (timer) {
@@ -1019,18 +1024,20 @@ cudaError_t launch_spawn_order(shy_world* w, int total) {
 
 namespace {
 
-// Launches one lock-step cycle.  The grid is the resident CTAs per SM times
-// the SMs (fewer for small cycles: at least 32 drops per CTA); each CTA's
-// drop slots go to shared memory when they fit without lowering that
-// occupancy, else to the global arrays in `a`.
-cudaError_t launch_lockstep(LockArgs& a, int sm_count, int grid_hint, cudaStream_t stream) {
+// Launches one lock-step cycle with CTAs of kBlock threads.  The grid is
+// the resident CTAs per SM times the SMs (fewer for small cycles: at least 32
+// drops per CTA); each CTA's drop slots go to shared memory when they fit
+// without lowering that occupancy (and the world allows it), else to the
+// global arrays in `a`.
+template <int kBlock>
+cudaError_t launch_lockstep_n(LockArgs& a, int sm_count, int grid_hint, cudaStream_t stream) {
   int dev = 0, optin = 0, per0 = 0;
   cudaError_t e;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
   cudaFuncAttributes fa;
-  if ((e = cudaFuncGetAttributes(&fa, lockstep_kernel)) != cudaSuccess) return e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, lockstep_kernel, kLockBlock, 0)) != cudaSuccess)
+  if ((e = cudaFuncGetAttributes(&fa, lockstep_kernel<kBlock>)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, lockstep_kernel<kBlock>, kBlock, 0)) != cudaSuccess)
     return e;
   if (per0 < 1) return cudaErrorLaunchOutOfResources;
   const long long max_dyn = (long long)optin - (long long)fa.sharedSizeBytes;
@@ -1043,13 +1050,13 @@ cudaError_t launch_lockstep(LockArgs& a, int sm_count, int grid_hint, cudaStream
   const long long b = (long long)slot_range(a.total_drops, g, 0, a.order != nullptr).cap * kSlotBytes;
   size_t bytes = 0;
   a.smem_slots = 0;
-  if (b <= max_dyn) {
+  if (b <= max_dyn && a.smem_allowed) {
     if (b > 48 * 1024 &&
-        (e = cudaFuncSetAttribute(lockstep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b)) !=
+        (e = cudaFuncSetAttribute(lockstep_kernel<kBlock>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b)) !=
             cudaSuccess)
       return e;
     int per = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lockstep_kernel, kLockBlock, (size_t)b)) !=
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lockstep_kernel<kBlock>, kBlock, (size_t)b)) !=
         cudaSuccess)
       return e;
     if ((long long)per * sm_count >= g) {  // the slots fit without costing occupancy
@@ -1058,8 +1065,16 @@ cudaError_t launch_lockstep(LockArgs& a, int sm_count, int grid_hint, cudaStream
     }
   }
   void* args[] = {&a};
-  return cudaLaunchCooperativeKernel((const void*)lockstep_kernel, dim3(grid), dim3(kLockBlock), args, bytes,
+  return cudaLaunchCooperativeKernel((const void*)lockstep_kernel<kBlock>, dim3(grid), dim3(kBlock), args, bytes,
                                      stream);
+}
+
+cudaError_t launch_lockstep(LockArgs& a, int sm_count, int grid_hint, int block, cudaStream_t stream) {
+  switch (block) {
+    case 64: return launch_lockstep_n<64>(a, sm_count, grid_hint, stream);
+    case 128: return launch_lockstep_n<128>(a, sm_count, grid_hint, stream);
+    default: return launch_lockstep_n<kLockBlock>(a, sm_count, grid_hint, stream);
+  }
 }
 
 }  // namespace
@@ -1112,7 +1127,8 @@ cudaError_t launch_batched_cycle(shy_world* w) {
     if ((e = timing_end(w, slot)) != cudaSuccess) return e;
   }
   if ((e = timing_begin(w, SHY_KERNEL_DROPS, &slot)) != cudaSuccess) return e;
-  if ((e = launch_lockstep(a, w->sm_count, w->batch_grid, w->stream)) != cudaSuccess) return e;
+  a.smem_allowed = w->batch_smem;
+  if ((e = launch_lockstep(a, w->sm_count, w->batch_grid, w->batch_block, w->stream)) != cudaSuccess) return e;
   if ((e = timing_end(w, slot)) != cudaSuccess) return e;
 
   if ((e = timing_begin(w, SHY_KERNEL_APPLY, &slot)) != cudaSuccess) return e;
@@ -1169,7 +1185,8 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.bar = b.bar;
   a.max_steps = (int)b.P.max_age + 3;
   a.stall_ns = debug_stall_ns();
-  cudaError_t e = launch_lockstep(a, b.sm_count, 0, stream);
+  a.smem_allowed = 1;
+  cudaError_t e = launch_lockstep(a, b.sm_count, 0, kLockBlock, stream);
   if (e != cudaSuccess) return e;
   cycle_end_kernel<<<cells_grid(b.cells), 256, 0, stream>>>(b.trk, b.rec, b.track_f, b.cq, b.h, b.cells, b.P,
                                                             b.bar, b.st);

@@ -637,6 +637,18 @@ int shy_world_set_launch(shy_world* w, int grid, int order) {
   return SHY_OK;
 }
 
+int shy_world_set_block(shy_world* w, int threads, int smem_slots) {
+  int rc = check_world(w);
+  if (rc) return rc;
+  if ((threads != 64 && threads != 128 && threads != 256) || smem_slots < 0 || smem_slots > 1) {
+    set_error("shy_world_set_block: threads must be 64, 128 or 256 and smem_slots 0 or 1");
+    return SHY_ERR_INVALID_ARG;
+  }
+  w->batch_block = threads;
+  w->batch_smem = smem_slots;
+  return SHY_OK;
+}
+
 int shy_world_sync(shy_world* w) {
   int rc = check_world(w);
   if (rc) return rc;

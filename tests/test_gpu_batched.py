@@ -246,16 +246,44 @@ def test_batch_beyond_shared_terrain_table(shy, po):
     b.close()
 
 
+def test_every_launch_shape_gives_the_oracle_bits(shy, po):
+    """Every candidate of the autotuner's search space -- CTA size 64, 128 or
+    256, every resident CTA or one per SM (and a small grid, so that CTAs
+    hold several slots per thread), drop or spawn-cell order, drop slots in
+    shared or global memory -- runs the same schedule: the oracle's bits."""
+    from simplehydrology_gb300 import autotune
+    nx, ny, drops = 96, 80, 3000
+    H = po.value_noise(nx, ny, 21)
+    m = po.Maps(nx, ny, height=H)
+    acc = po.erode_batched(m, 3, 0, drops, 2)
+    shapes = autotune.candidates() + [(7, 1, 64, 1), (5, 0, 128, 0), (3, -1, 256, 1)]
+    for shape in shapes:
+        w = shy.World(nx, ny, seed=3)
+        w.set_field("height", H)
+        autotune.apply(w, shape)
+        w.erode(drops, 2)
+        compare_all(w.get_field, m, po, f"shape {shape}")
+        assert w.stats().drop_steps == acc.steps, shape
+        w.close()
+
+
 def test_autotune_applies_a_shape_and_keeps_results(shy, po):
     from simplehydrology_gb300 import autotune
     nx, ny, drops = 96, 80, 2000
     H = po.value_noise(nx, ny, 21)
     w = shy.World(nx, ny, seed=3)
     w.set_field("height", H)
-    best, times = autotune.autotune(w, drops, cycles=1, shapes=[(0, -1), (7, 0), (0, 1)])
-    assert best in times and len(times) == 3
+    best, times = autotune.autotune(w, drops, cycles=3)
+    assert best in times and len(times) == len(autotune.candidates()) == 36
+    assert all(t > 0 for t in times.values())
     w.erode(drops, 2)  # with the chosen shape
     m = po.Maps(nx, ny, height=H)
     po.erode_batched(m, 3, 0, drops, 2)
     compare_all(w.get_field, m, po, "after autotune")
     w.close()
+
+
+def test_autotune_counts_the_sms():
+    torch = pytest.importorskip("torch")
+    from simplehydrology_gb300 import autotune
+    assert autotune.sm_count() == torch.cuda.get_device_properties(0).multi_processor_count
