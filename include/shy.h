@@ -149,6 +149,17 @@ int shy_terrain_set_state(shy_world* w, int terrain, const float* height, const 
                           const float* momentum_x, const float* momentum_y, size_t count);
 int shy_terrain_get_state(shy_world* w, int terrain, float* height, float* discharge, float* momentum_x,
                           float* momentum_y, size_t count);
+/* The same state calls on DEVICE memory (no reference counterpart: the
+ * reference has no device): each non-NULL pointer is nx * ny floats of device
+ * (or managed) memory of the world's device.  The copies run on the world's
+ * stream; the data must be ready when the call is made (work that writes it
+ * on another stream must have finished), and the call returns after the
+ * world's stream finished the copies.  Used by the surrogate's warm start,
+ * whose predictions never leave the device. */
+int shy_terrain_set_state_device(shy_world* w, int terrain, const float* height, const float* discharge,
+                                 const float* momentum_x, const float* momentum_y, size_t count);
+int shy_terrain_get_state_device(shy_world* w, int terrain, float* height, float* discharge,
+                                 float* momentum_x, float* momentum_y, size_t count);
 /* The world's cudaStream_t, for callers that order their own work with it. */
 int shy_world_stream(shy_world* w, void** stream);
 int shy_world_stats(shy_world* w, shy_stats* out);
@@ -156,6 +167,7 @@ int shy_world_reset_stats(shy_world* w);
 /* Batched-mode random stream position: the next shy_erode cycle uses this
  * cycle index for its spawn positions. */
 int shy_world_set_cycle(shy_world* w, uint64_t cycle);
+int shy_world_get_cycle(shy_world* w, uint64_t* cycle);
 int shy_world_enable_timing(shy_world* w, int on);
 int shy_world_timing(shy_world* w, shy_timing* out);
 /* Where the batched kernel's time goes, as seen by its first CTA, summed

@@ -114,6 +114,12 @@ class _Handle:
     def set_cycle(self, cycle: int):
         check(lib().shy_world_set_cycle(self._w, cycle))
 
+    def cycle(self) -> int:
+        """The cycle index the next batched cycle uses for its spawns."""
+        c = C.c_uint64()
+        check(lib().shy_world_get_cycle(self._w, C.byref(c)))
+        return c.value
+
     def sync(self):
         check(lib().shy_world_sync(self._w))
 
@@ -160,6 +166,42 @@ class _Handle:
             out = {name: np.empty((nx, ny), np.float32) for name in self._STATE}
         ptrs, n = self._state_args(terrain, out, True)
         check(lib().shy_terrain_get_state(self._w, terrain, *ptrs, n))
+        return out
+
+    def _device_args(self, terrain, tensors):
+        nx, ny = self._terrain_shape(terrain)
+        ptrs = []
+        for name in self._STATE:
+            t = tensors.get(name)
+            if t is None:
+                ptrs.append(None)
+                continue
+            import torch
+            if (not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float32
+                    or not t.is_contiguous() or t.numel() != nx * ny):
+                raise ValueError(f"{name}: want a contiguous float32 CUDA tensor of {nx * ny} elements")
+            ptrs.append(t.data_ptr())
+        return ptrs, nx * ny
+
+    def set_state_device(self, terrain: int = 0, **tensors):
+        """set_state from torch CUDA tensors, device to device
+        (shy_terrain_set_state_device); the tensors' producing work must have
+        finished (synchronize its stream first)."""
+        unknown = set(tensors) - set(self._STATE)
+        if unknown:
+            raise ValueError(f"unknown fields {sorted(unknown)}")
+        ptrs, n = self._device_args(terrain, tensors)
+        check(lib().shy_terrain_set_state_device(self._w, terrain, *ptrs, n))
+
+    def get_state_device(self, terrain: int = 0, out=None):
+        """The four state fields of one terrain as torch CUDA tensors (nx, ny),
+        device to device (shy_terrain_get_state_device), into `out` when given."""
+        import torch
+        nx, ny = self._terrain_shape(terrain)
+        if out is None:
+            out = {name: torch.empty((nx, ny), dtype=torch.float32, device="cuda") for name in self._STATE}
+        ptrs, n = self._device_args(terrain, out)
+        check(lib().shy_terrain_get_state_device(self._w, terrain, *ptrs, n))
         return out
 
     def save(self, path):

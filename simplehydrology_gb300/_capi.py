@@ -122,10 +122,15 @@ SIGNATURES = {
     "shy_world_sync": (C.c_int, [W]),
     "shy_terrain_set_state": (C.c_int, [W, C.c_int, FP, FP, FP, FP, C.c_size_t]),
     "shy_terrain_get_state": (C.c_int, [W, C.c_int, FP, FP, FP, FP, C.c_size_t]),
+    "shy_terrain_set_state_device": (C.c_int, [W, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_size_t]),
+    "shy_terrain_get_state_device": (C.c_int, [W, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_size_t]),
     "shy_world_stream": (C.c_int, [W, P(C.c_void_p)]),
     "shy_world_stats": (C.c_int, [W, P(Stats)]),
     "shy_world_reset_stats": (C.c_int, [W]),
     "shy_world_set_cycle": (C.c_int, [W, C.c_uint64]),
+    "shy_world_get_cycle": (C.c_int, [W, C.POINTER(C.c_uint64)]),
     "shy_world_enable_timing": (C.c_int, [W, C.c_int]),
     "shy_world_timing": (C.c_int, [W, P(Timing)]),
     "shy_world_set_erf_source": (C.c_int, [W, C.c_int]),

@@ -617,6 +617,72 @@ int shy_terrain_get_state(shy_world* w, int t, float* height, float* discharge, 
   return SHY_OK;
 }
 
+// device pointers of the state calls: device (or managed) memory of the
+// world's device, or null
+static int check_device_ptrs(shy_world* w, const char* fn, const void* const* p, int n) {
+  for (int i = 0; i < n; ++i) {
+    if (!p[i]) continue;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p[i]) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("%s: argument %d is not a CUDA pointer", fn, i);
+      return SHY_ERR_INVALID_ARG;
+    }
+    if (!(at.type == cudaMemoryTypeManaged || (at.type == cudaMemoryTypeDevice && at.device == w->device))) {
+      set_error("%s: argument %d is not device memory of the world's device", fn, i);
+      return SHY_ERR_INVALID_ARG;
+    }
+  }
+  return SHY_OK;
+}
+
+int shy_terrain_set_state_device(shy_world* w, int t, const float* height, const float* discharge,
+                                 const float* momentum_x, const float* momentum_y, size_t count) {
+  int rc = check_terrain(w, t);
+  if (rc) return rc;
+  const long long n = (long long)w->terrains[t].nx * w->terrains[t].ny;
+  if (count != (size_t)n) {
+    set_error("set_state_device: count %zu, want %lld", count, n);
+    return SHY_ERR_INVALID_ARG;
+  }
+  const void* ptrs[4] = {height, discharge, momentum_x, momentum_y};
+  if ((rc = check_device_ptrs(w, "set_state_device", ptrs, 4)) != SHY_OK) return rc;
+  cudaStream_t s = w->stream;
+  if (height) {
+    SHY_CHECK_CUDA(cudaMemcpyAsync(w->h + w->terrains[t].cell_base, height, sizeof(float) * (size_t)n,
+                                   cudaMemcpyDeviceToDevice, s),
+                   "copy heights");
+    w->hq_stale = true;
+  }
+  if (discharge || momentum_x || momentum_y)
+    SHY_CHECK_CUDA(launch_pack_state(w, t, discharge, momentum_x, momentum_y), "pack state");
+  if (discharge) w->ceq_source = ERF_DEVICE;
+  SHY_CHECK_CUDA(cudaStreamSynchronize(s), "synchronize");
+  return SHY_OK;
+}
+
+int shy_terrain_get_state_device(shy_world* w, int t, float* height, float* discharge, float* momentum_x,
+                                 float* momentum_y, size_t count) {
+  int rc = check_terrain(w, t);
+  if (rc) return rc;
+  const long long n = (long long)w->terrains[t].nx * w->terrains[t].ny;
+  if (count != (size_t)n) {
+    set_error("get_state_device: count %zu, want %lld", count, n);
+    return SHY_ERR_INVALID_ARG;
+  }
+  const void* ptrs[4] = {height, discharge, momentum_x, momentum_y};
+  if ((rc = check_device_ptrs(w, "get_state_device", ptrs, 4)) != SHY_OK) return rc;
+  cudaStream_t s = w->stream;
+  if (discharge || momentum_x || momentum_y)
+    SHY_CHECK_CUDA(launch_unpack_state(w, t, discharge, momentum_x, momentum_y), "unpack state");
+  if (height)
+    SHY_CHECK_CUDA(cudaMemcpyAsync(height, w->h + w->terrains[t].cell_base, sizeof(float) * (size_t)n,
+                                   cudaMemcpyDeviceToDevice, s),
+                   "copy heights");
+  SHY_CHECK_CUDA(cudaStreamSynchronize(s), "synchronize");
+  return SHY_OK;
+}
+
 int shy_world_set_field(shy_world* w, int field, const float* host, size_t count) {
   return shy_terrain_set_field(w, 0, field, host, count);
 }
@@ -701,6 +767,20 @@ int shy_world_set_cycle(shy_world* w, uint64_t cycle) {
   unsigned long long c = cycle;
   SHY_CHECK_CUDA(cudaMemcpyAsync(&w->bar->cycle, &c, sizeof(c), cudaMemcpyHostToDevice, w->stream), "set cycle");
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
+  return SHY_OK;
+}
+
+int shy_world_get_cycle(shy_world* w, uint64_t* cycle) {
+  int rc = check_world(w);
+  if (rc) return rc;
+  if (!cycle) {
+    set_error("null output");
+    return SHY_ERR_INVALID_ARG;
+  }
+  unsigned long long c = 0;
+  SHY_CHECK_CUDA(cudaMemcpyAsync(&c, &w->bar->cycle, sizeof(c), cudaMemcpyDeviceToHost, w->stream), "get cycle");
+  SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
+  *cycle = c;
   return SHY_OK;
 }
 

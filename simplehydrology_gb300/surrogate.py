@@ -468,16 +468,55 @@ class Surrogate:
 
     def warm_start(self, world, terrain: int = 0):
         """Write the predicted discharge and momentum maps of a terrain into a
-        World or Batch (its current heightmap is the input)."""
+        World or Batch (its current heightmap is the input).  Device to
+        device: the heights come out and the maps go in through
+        shy_terrain_get/set_state_device, never through host memory."""
         torch = self.torch
-        get = (lambda f: world.get_field(terrain, f)) if hasattr(world, "__len__") else world.get_field
-        put = (lambda f, v: world.set_field(terrain, f, v)) if hasattr(world, "__len__") else world.set_field
-        h = get("height")
-        d, mx, my = self.predict(torch.from_numpy(h[None]).to(self.dev))
-        torch.cuda.synchronize(self.dev)
-        put("discharge", d[0].cpu().numpy())
-        put("momentum_x", mx[0].cpu().numpy())
-        put("momentum_y", my[0].cpu().numpy())
+        h = world.get_state_device(terrain)["height"]
+        d, mx, my = self.predict(h[None])
+        torch.cuda.current_stream(self.dev).synchronize()
+        world.set_state_device(terrain, discharge=d[0], momentum_x=mx[0], momentum_y=my[0])
+
+    def warm_start_judged(self, world, drops: int, probe_cycles: int = 5, threshold: float = 0.05,
+                          terrain: int = 0):
+        """Warm start with the plain particle method as judge and fallback.
+
+        The world's state (heights, maps, spawn-stream cycle) is kept on the
+        device; the prediction is written into the world and `probe_cycles`
+        plain cycles of `drops` drops run from it.  The judge is the log-L2
+        distance between the mean discharge of those cycles and the
+        prediction: the particle method, started from a right prediction,
+        keeps it.  At or below `threshold` the warm start is kept and the
+        world continues from the probe's end.  Above it the warm start is
+        discarded: the kept state is restored and the same cycles run plain,
+        so the world ends where it would have without the surrogate (bit for
+        bit when its fixed-point heights were last derived from its float
+        heights, as after set_field or generate: the restore goes through
+        the float heights).  Returns {"accepted", "log_l2", "probe_cycles"}.
+        A single-terrain World only (the probe runs shy_erode)."""
+        torch = self.torch
+        saved = world.get_state_device(terrain)
+        cycle = world.cycle()
+        d, mx, my = self.predict(saved["height"][None])
+        torch.cuda.current_stream(self.dev).synchronize()
+        pred = d[0].clone()
+        world.set_state_device(terrain, discharge=d[0], momentum_x=mx[0], momentum_y=my[0])
+        acc = torch.zeros_like(pred)
+        probe = {"discharge": torch.empty_like(pred)}
+        for _ in range(probe_cycles):
+            world.erode(drops, 1)
+            world.get_state_device(terrain, out=probe)
+            acc += probe["discharge"]
+        acc /= max(1, probe_cycles)
+        a, b = torch.log1p(acc.double()), torch.log1p(pred.double())
+        nb = float(torch.linalg.vector_norm(b))
+        dist = float(torch.linalg.vector_norm(a - b)) / nb if nb > 0 else float("inf")
+        accepted = dist <= threshold
+        if not accepted:  # the fallback: the plain method from the kept state
+            world.set_state_device(terrain, **saved)
+            world.set_cycle(cycle)
+            world.erode(drops, probe_cycles)
+        return {"accepted": accepted, "log_l2": dist, "probe_cycles": probe_cycles}
 
     def status(self):
         check(lib().shy_sg_status())

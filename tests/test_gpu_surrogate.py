@@ -431,3 +431,85 @@ def test_autotune_picks_a_tile_per_call(sg):
     loss = float(net.train_step(h, t, 1e-3).item())
     net.status()
     assert np.isfinite(loss)
+
+
+def test_device_state_calls_match_host_ones(sg, shy):
+    """shy_terrain_get/set_state_device move the same bits as the host state
+    calls, with no host copy of the data."""
+    w = shy.World(96, 80, seed=3)
+    w.generate(3, 8)
+    w.erode(500, 2)
+    host = w.get_state()
+    dev_ = w.get_state_device()
+    for k, v in host.items():
+        assert np.array_equal(dev_[k].cpu().numpy().view(np.uint32), v.view(np.uint32)), k
+    w2 = shy.World(96, 80, seed=3)
+    w2.set_state_device(**dev_)
+    back = w2.get_state()
+    for k, v in host.items():
+        assert np.array_equal(back[k].view(np.uint32), v.view(np.uint32)), k
+    with pytest.raises(ValueError):  # host tensors are refused before the call
+        w2.set_state_device(discharge=torch.zeros(96 * 80))
+    w.close()
+    w2.close()
+
+
+def _small_net(sg):
+    n_tr = 32
+    H, D, MX, MY = sg.make_pairs(n_tr, size=128, cycles=20, seed0=700)
+    norm = sg.Norm.fit(H, D, MX, MY)
+    net = sg.Surrogate(seed=2, norm=norm)
+    sg.train(net, H, D, MX, MY, epochs=4, batch=8, lr=2e-3)
+    net.status()
+    return net
+
+
+def test_warm_start_is_device_to_device_and_writes_the_prediction(sg, shy):
+    net = _small_net(sg)
+    w = shy.World(128, 128, seed=9)
+    w.generate(9, 8)
+    net.warm_start(w)
+    h = torch.from_numpy(w.get_field("height")[None]).cuda()
+    d, mx, my = net.predict(h)
+    torch.cuda.synchronize()
+    for name, t in (("discharge", d), ("momentum_x", mx), ("momentum_y", my)):
+        assert np.array_equal(w.get_field(name).view(np.uint32), t[0].cpu().numpy().view(np.uint32)), name
+    w.close()
+
+
+def test_judged_warm_start_falls_back_to_the_plain_method(sg, shy):
+    """A prediction the particle method moves by more than the threshold is
+    discarded: the world ends bit for bit where the plain method alone ends."""
+    net = _small_net(sg)
+    drops, k = 1024, 3
+    w = shy.World(128, 128, seed=21)
+    w.generate(21, 8)
+    res = net.warm_start_judged(w, drops, probe_cycles=k, threshold=1e-6)
+    assert not res["accepted"] and res["log_l2"] > 1e-6
+    plain = shy.World(128, 128, seed=21)
+    plain.generate(21, 8)
+    plain.erode(drops, k)
+    for f in ("height", "discharge", "momentum_x", "momentum_y"):
+        assert np.array_equal(w.get_field(f).view(np.uint32), plain.get_field(f).view(np.uint32)), f
+    assert w.cycle() == plain.cycle() == k
+    w.close()
+    plain.close()
+
+
+def test_judged_warm_start_keeps_an_accepted_prediction(sg, shy):
+    """Within the threshold the warm start stands: the world continues from
+    the probe cycles run after the prediction."""
+    net = _small_net(sg)
+    drops, k = 1024, 3
+    w = shy.World(128, 128, seed=22)
+    w.generate(22, 8)
+    res = net.warm_start_judged(w, drops, probe_cycles=k, threshold=10.0)
+    assert res["accepted"]
+    ref = shy.World(128, 128, seed=22)
+    ref.generate(22, 8)
+    net.warm_start(ref)
+    ref.erode(drops, k)
+    for f in ("height", "discharge", "momentum_x", "momentum_y"):
+        assert np.array_equal(w.get_field(f).view(np.uint32), ref.get_field(f).view(np.uint32)), f
+    w.close()
+    ref.close()
