@@ -588,7 +588,7 @@ def _discharge_run(shy, seed, n, drops, cycles, warm=None, spawn_seed=None):
     from zero maps, or from the surrogate's maps when `warm` is given; the
     spawns follow `spawn_seed` (default `seed`).
     Returns (discharge after each cycle, device ms of each cycle, warm-start
-    seconds: the surrogate's prediction and the map upload, wall clock)."""
+    seconds: the prediction and the device-to-device map write, wall clock)."""
     import torch
     w = shy.World(n, n, seed=seed if spawn_seed is None else spawn_seed)
     w.generate(seed, 8)
@@ -618,19 +618,24 @@ def run_surrogate(args):
 
     The plain method's discharge is a blend with lrate 0.1 of each cycle's
     tracks (source/world.h:83-85), so from zero maps it takes tens of cycles
-    to settle; after that the terrain's erosion keeps moving it slowly, and
-    single-cycle snapshots differ by about 10 % log-L2 at 65,536 drops on
-    1024^2.  So the reference D* is the mean discharge of cycles
-    horizon+1 .. horizon+10 of the plain run, and a run has converged at
-    the first cycle k where the mean discharge of its last min(k, 10)
-    cycles is within 5 % log-L2 of D*.  The warm run starts from the
-    surrogate's maps and its time includes the prediction.
+    to settle, and it carries the spawn order's noise: two plain runs of one
+    terrain with different spawns stay about 0.4 log-L2 apart.  So D* of a
+    terrain is the mean discharge of cycles horizon+1 .. horizon+10 averaged
+    over `spawn_runs` plain runs with different spawns, and each run is
+    compared with the D* of the other runs (leave one out), never with one
+    that contains itself.  A run's distance at cycle k is the log-L2 between
+    the mean discharge of its last min(k, 10) cycles and that D*.  The floor
+    is the distance the plain runs reach at the horizon; a run has converged
+    at the first k where its distance is within 5 % of that floor
+    (distance <= 1.05 x floor).  The strict reading, distance <= 0.05, is
+    reported too.  The warm run starts from the surrogate's maps (written
+    device to device) and its time includes the prediction.
 
     The surrogate is trained first, on pairs the batched GPU particle method
     generates: 256^2 value-noise terrains (seeds 10000+i), input the initial
     heightmap, targets the maps after `horizon` cycles at the same drop
-    density (4,096 drops per cycle).  Evaluation terrains are 1024^2, seeds
-    20000+i."""
+    density (4,096 drops per cycle), averaged over `spawn_runs` spawn
+    orders.  Evaluation terrains are 1024^2, seeds 20000+i."""
     import numpy as np
     import torch
 
@@ -642,12 +647,13 @@ def run_surrogate(args):
     clock = ClockSampler(torch.cuda.current_device())
     clock.__enter__()
     horizon, theta, n_tr, n_val = args.horizon, 0.05, args.train_terrains, 64
+    runs = args.spawn_runs
     side = args.train_side
     if side != 256:  # fewer, larger terrains, trained on random 256^2 crops
         n_tr, n_val = max(1, n_tr * 256 * 256 // (side * side)), max(1, 64 * 256 * 256 // (side * side))
     t0 = time.perf_counter()
     H, D, MX, MY = sg.make_pairs(n_tr + n_val, size=side, cycles=horizon, seed0=10000,
-                                 per_launch=max(16, 64 * 256 * 256 // (side * side)))
+                                 per_launch=max(16, 64 * 256 * 256 // (side * side)), spawn_runs=runs)
     gen_s = time.perf_counter() - t0
     norm = sg.Norm.fit(H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr])
     net = sg.Surrogate(seed=0, norm=norm)
@@ -696,55 +702,65 @@ def run_surrogate(args):
 
     # warm start against plain on 1024^2 terrains
     n, drops, total = 1024, 65536, horizon + 10
+
+    def window(ds, k):
+        return np.mean(ds[max(0, k - 10):k], axis=0)
+
+    def first(dist, bound):
+        return next((k + 1 for k, d in enumerate(dist) if d <= bound), None)
+
     per = []
     for i in range(args.eval_terrains):
         seed = 20000 + i
-        dp, mp, _ = _discharge_run(shy, seed, n, drops, total)
-        ref = np.mean(dp[horizon:], axis=0)
-        dw_, mw, t_warm = _discharge_run(shy, seed, n, drops, total, warm=net)
-        # the same terrain with other spawns: how far apart two plain runs end
-        do, _, _ = _discharge_run(shy, seed, n, drops, total, spawn_seed=seed + 7919)
+        plain = [_discharge_run(shy, seed, n, drops, total, spawn_seed=seed + sg.SPAWN_STRIDE * r)
+                 for r in range(runs)]
+        finals = [np.mean(ds[horizon:], axis=0) for ds, _, _ in plain]
+        # D* of run r: the other runs' mean (leave one out)
+        dstar = [np.mean([f for q, f in enumerate(finals) if q != r], axis=0) for r in range(runs)]
+        floor = float(np.mean([sg.log_l2(window(plain[r][0], horizon), dstar[r]) for r in range(runs)]))
+        dp, mp, _ = plain[0]
+        dw_, mw, t_warm = _discharge_run(shy, seed, n, drops, total, warm=net)  # spawn order of run 0
         pred = net.predict(torch.from_numpy(_initial_height(shy, seed, n)[None]).cuda())[0][0].cpu().numpy()
-
-        def window(ds, k):
-            return np.mean(ds[max(0, k - 10):k], axis=0)
-
-        dist_p = [sg.log_l2(window(dp, k), ref) for k in range(1, total + 1)]
-        dist_w = [sg.log_l2(window(dw_, k), ref) for k in range(1, total + 1)]
-        snap_p = [sg.log_l2(d, ref) for d in dp]
-        dist_o = [sg.log_l2(window(do, k), ref) for k in range(1, total + 1)]
-        d_pred = sg.log_l2(pred, ref)
-        worth = next((k + 1 for k, d in enumerate(dist_p) if d <= d_pred), None)
-        kp = next((k + 1 for k, d in enumerate(dist_p) if d <= theta), None)
-        kw = next((k + 1 for k, d in enumerate(dist_w) if d <= theta), None)
+        dist_p = [sg.log_l2(window(dp, k), dstar[0]) for k in range(1, total + 1)]
+        dist_w = [sg.log_l2(window(dw_, k), dstar[0]) for k in range(1, total + 1)]
+        d_pred = sg.log_l2(pred, dstar[0])
+        bound = (1.0 + theta) * floor
+        kp, kw = first(dist_p, bound), first(dist_w, bound)
         tp = sum(mp[:kp]) / 1e3 if kp else None
         tw = t_warm + sum(mw[:kw]) / 1e3 if kw else None
-        per.append({"seed": seed, "cycles_plain": kp, "cycles_warm": kw, "plain_s": tp, "warm_s": tw,
+        per.append({"seed": seed, "floor": floor, "bound": bound, "cycles_plain": kp, "cycles_warm": kw,
+                    "plain_s": tp, "warm_s": tw, "speedup": (tp / tw) if tp and tw else None,
                     "warm_start_s": t_warm, "log_l2_prediction": d_pred,
-                    "prediction_worth_plain_cycles": worth,
-                    "log_l2_other_spawns_window": [round(d, 4) for d in dist_o[::5]],
+                    "prediction_worth_plain_cycles": first(dist_p, d_pred),
+                    "strict_5pct_plain": first(dist_p, theta), "strict_5pct_warm": first(dist_w, theta),
                     "log_l2_plain_window": [round(d, 4) for d in dist_p[::5]],
                     "log_l2_warm_window": [round(d, 4) for d in dist_w[::5]],
-                    "log_l2_plain_snapshot": [round(d, 4) for d in snap_p[::5]],
                     "ms_per_cycle": sum(mp) / len(mp)})
     clock.__exit__()
     tps = [r["plain_s"] for r in per if r["plain_s"]]
     tws = [r["warm_s"] for r in per if r["warm_s"]]
-    out = {"metric": "time to converged discharge (<=5% log-L2), plain vs surrogate warm start", "unit": "s",
+    out = {"metric": "time to converged discharge (within 5% of the plain runs' floor, log-L2), plain vs "
+                     "surrogate warm start", "unit": "s",
            "value": statistics.mean(tws) if tws else None,
            "plain_s": statistics.mean(tps) if tps else None,
+           "warm_s": statistics.mean(tws) if tws else None,
            "speedup": (statistics.mean(tps) / statistics.mean(tws)) if tps and tws else None,
+           "target_speedup": 3.0,
            "higher_is_better": False, "n_gpus": 1, "dtype": "bf16 (f32 accumulate)",
            "data": "synthetic (seeded value-noise terrains; training pairs from the GPU particle method)",
            "config": {"workload": "learned warm-start: U-Net (1.36 M parameters, 4 levels, channels 32-256) "
                                   "trained on 256x256 terrains, evaluated on 1024x1024 at 65536 drops/cycle",
-                      "horizon_cycles": horizon, "threshold": theta, "window_cycles": 10,
+                      "horizon_cycles": horizon, "threshold": theta, "window_cycles": 10, "spawn_runs": runs,
+                      "dstar": "mean over the other spawn runs of the mean discharge of cycles "
+                               "horizon+1..horizon+10",
+                      "converged": "log-L2 to D* <= (1 + threshold) x the plain runs' floor",
+                      "eval_terrains": args.eval_terrains,
                       "train_terrains": n_tr, "train_side": side, "epochs": args.epochs, "batch": batch},
            "training": {"pairs_s": gen_s, "train_s": train_ms / 1e3, "steps": steps,
                         "tflops": train_flops / (train_ms / 1e3) / 1e12,
                         "loss_by_epoch": [round(v, 5) for v in losses],
                         "launches": net.launches - launches0, "validation": val},
-           "roofline": {"bound": "tensor", "kernel": "conv_fwd_kernel (384->128, 3x3, 16x64x64 pixels)",
+           "roofline": {"bound": "tensor", "kernel": "conv_tma_kernel (384->128, 3x3, 16x64x64 pixels)",
                         "achieved": conv_flops / (conv_ms / 1e3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
                         "frac": conv_flops / (conv_ms / 1e3) / 1e12 / bf16_peak, "peak_source": peak_src,
                         "avg_launch_ms": conv_ms, "traffic": None,
@@ -847,9 +863,10 @@ def main():
     ap.add_argument("--terrains", type=int, default=64)
     # --workload surrogate
     ap.add_argument("--horizon", type=int, default=50)
-    ap.add_argument("--train-terrains", type=int, default=2048)
+    ap.add_argument("--train-terrains", type=int, default=4096)
     ap.add_argument("--epochs", type=int, default=24)
-    ap.add_argument("--eval-terrains", type=int, default=2)
+    ap.add_argument("--eval-terrains", type=int, default=4)
+    ap.add_argument("--spawn-runs", type=int, default=4)
     ap.add_argument("--train-side", type=int, default=256)
     ap.add_argument("--autotune", action="store_true",
                     help="run the launch-shape autotuner first and bench the fastest shape")

@@ -718,12 +718,39 @@ void vegetation_step(Grid<float>& g, float* plant, const shy_params& P, uint64_t
       for (int dy = -1; dy <= 1; ++dy)
         if (!g.oob(x + dx, y + dy)) dq[g.at(x + dx, y + dy)] += q32(f * veg_weight(dx, dy));
   };
-  auto place = [&](int x, int y) {
+  // a new plant, at most one per cell (the first claim wins; every claim
+  // places the same plant)
+  auto claim = [&](int x, int y) {
     const size_t t = g.at(x, y);
-    if (taken[t]) return;
+    if (taken[t]) return false;
     taken[t] = 1;
     plant[t] = P.plant_grow_rate * (P.plant_max_size - 0.0f);
     root(x, y, 1.0f);
+    return true;
+  };
+  // The spread rule of source/vegetation.h:160-183 from cell (x, y) with the
+  // draws of `c` (what = w0 .. w0 + 3), on the step's starting maps.
+  auto spread_target = [&](int x, int y, size_t c, unsigned w0, int& tx, int& ty) {
+    if (!(R.u(c, w0) < P.plant_spread_prob)) return false;
+    tx = x + (int)(R.u(c, w0 + 1) * 9.0f) - 4;
+    ty = y + (int)(R.u(c, w0 + 2) * 9.0f) - 4;
+    if (g.oob(tx, ty)) return false;
+    const size_t t = g.at(tx, ty);
+    if (erfd(t) >= P.plant_max_discharge) return false;
+    if ((float)(int)(R.u(c, w0 + 3) * 1000.0f) / 1000.0f <= g.root[t]) return false;
+    if (!(normal(g, tx, ty, P.map_scale).y > P.plant_max_steep)) return false;
+    if (p0[t] > 0.0f) return false;
+    return true;
+  };
+  // The reference visits a plant appended during Vegetation::grow in the
+  // same call (source/vegetation.h:138, plants.size() is re-read), so a new
+  // plant may spread at once: the plant a claim places takes one spread
+  // attempt in the same step, with draws keyed by its own cell (chains of
+  // three or more new plants in one step are cut at two).
+  auto place = [&](int x, int y) {
+    if (!claim(x, y)) return;
+    int tx, ty;
+    if (spread_target(x, y, g.at(x, y), 6, tx, ty)) claim(tx, ty);
   };
   for (int x = 0; x < g.nx; ++x)
     for (int y = 0; y < g.ny; ++y) {
@@ -737,15 +764,8 @@ void vegetation_step(Grid<float>& g, float* plant, const shy_params& P, uint64_t
           continue;
         }
         plant[c] = s;
-        if (!(R.u(c, 1) < P.plant_spread_prob)) continue;
-        const int tx = x + (int)(R.u(c, 2) * 9.0f) - 4, ty = y + (int)(R.u(c, 3) * 9.0f) - 4;
-        if (g.oob(tx, ty)) continue;
-        const size_t t = g.at(tx, ty);
-        if (erfd(t) >= P.plant_max_discharge) continue;
-        if ((float)(int)(R.u(c, 4) * 1000.0f) / 1000.0f <= g.root[t]) continue;
-        if (!(normal(g, tx, ty, P.map_scale).y > P.plant_max_steep)) continue;
-        if (p0[t] > 0.0f) continue;
-        place(tx, ty);
+        int tx, ty;
+        if (spread_target(x, y, c, 1, tx, ty)) place(tx, ty);
       } else {
         if (!(R.u(c, 5) < P.plant_spawn_prob)) continue;
         if (erfd(c) >= P.plant_max_discharge) continue;

@@ -6,7 +6,8 @@
 // grow (:63-65), die on discharge, height or a 1/1000 draw (:67-74) with
 // root(-1), spread with 1/20 to a cell offset by up to 4 (:160-183), and
 // spawn on empty cells with plant_spawn_prob where Plant::spawn allows
-// (:76-85).  root(f) adds f * {1, 0.6, 0.4} over the 3 x 3 block (:87-118)
+// (:76-85).  A new plant may spread in the step it appears, as the
+// reference's loop visits appended plants in the same call.  root(f) adds f * {1, 0.6, 0.4} over the 3 x 3 block (:87-118)
 // as 32.32 fixed-point sums.  A cell that several new plants reach gets one
 // (claimed atomically; the outcome does not depend on who wins), and the
 // plant map is double-buffered, so the step is deterministic.  After the
@@ -56,11 +57,38 @@ __global__ void veg_step_kernel(const Terrain* __restrict__ terrains, int n_terr
           if (!oob(cx + dx, cy + dy, T.nx, T.ny))
             add_i64(&rootq[T.cell_base + (long long)(cx + dx) * T.ny + (cy + dy)], shy_q32(f * veg_weight(dx, dy)));
     };
-    auto place = [&](int tx, int ty) {
+    // a new plant, at most one per cell (the first claim wins; every claim
+    // places the same plant)
+    auto claim_cell = [&](int tx, int ty) {
       const long long t = T.cell_base + (long long)tx * T.ny + ty;
-      if (atomicExch(&claim[t], tag) == tag) return;
+      if (atomicExch(&claim[t], tag) == tag) return false;
       plant1[t] = P.plant_grow_rate * (P.plant_max_size - 0.0f);
       root_add(tx, ty, 1.0f);
+      return true;
+    };
+    // the spread rule (:160-183) from (sx, sy) with the draws of local cell
+    // `c` (what = w0 .. w0 + 3), on the step's starting maps
+    auto spread_target = [&](int sx, int sy, long long c, unsigned w0, int& tx, int& ty) {
+      if (!(u(c, w0) < P.plant_spread_prob)) return false;
+      tx = sx + (int)(u(c, w0 + 1) * 9.0f) - 4;
+      ty = sy + (int)(u(c, w0 + 2) * 9.0f) - 4;
+      if (oob(tx, ty, T.nx, T.ny)) return false;
+      const long long t = T.cell_base + (long long)tx * T.ny + ty;
+      if (erfd(t) >= P.plant_max_discharge) return false;
+      if ((float)(int)(u(c, w0 + 3) * 1000.0f) / 1000.0f <= root[t]) return false;
+      if (!(normal_from(PlainHeights{hT, T.nx, T.ny}, tx, ty, T.nx, T.ny, P.map_scale).y > P.plant_max_steep))
+        return false;
+      return !(plant0[t] > 0.0f);
+    };
+    // The reference visits a plant appended during Vegetation::grow in the
+    // same call (:138 re-reads plants.size()), so a new plant may spread at
+    // once: the plant a claim places takes one spread attempt in the same
+    // step, with draws keyed by its own cell (chains of three or more new
+    // plants in one step are cut at two).
+    auto place = [&](int tx, int ty) {
+      if (!claim_cell(tx, ty)) return;
+      int ux, uy;
+      if (spread_target(tx, ty, (long long)tx * T.ny + ty, 6, ux, uy)) claim_cell(ux, uy);
     };
     const float s0 = plant0[i];
     if (s0 > 0.0f) {
@@ -71,16 +99,8 @@ __global__ void veg_step_kernel(const Terrain* __restrict__ terrains, int n_terr
         continue;
       }
       plant1[i] = s;
-      if (!(u(lc, 1) < P.plant_spread_prob)) continue;
-      const int tx = x + (int)(u(lc, 2) * 9.0f) - 4, ty = y + (int)(u(lc, 3) * 9.0f) - 4;
-      if (oob(tx, ty, T.nx, T.ny)) continue;
-      const long long t = T.cell_base + (long long)tx * T.ny + ty;
-      if (erfd(t) >= P.plant_max_discharge) continue;
-      if ((float)(int)(u(lc, 4) * 1000.0f) / 1000.0f <= root[t]) continue;
-      if (!(normal_from(PlainHeights{hT, T.nx, T.ny}, tx, ty, T.nx, T.ny, P.map_scale).y > P.plant_max_steep))
-        continue;
-      if (plant0[t] > 0.0f) continue;
-      place(tx, ty);
+      int tx, ty;
+      if (spread_target(x, y, lc, 1, tx, ty)) place(tx, ty);
     } else {
       if (!(u(lc, 5) < P.plant_spawn_prob)) continue;
       if (erfd(i) >= P.plant_max_discharge) continue;

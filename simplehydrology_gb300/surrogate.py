@@ -545,28 +545,42 @@ class Surrogate:
                 g[L["b"]:L["b"] + L["cout"]])
 
 
-def make_pairs(n, size=256, drops=None, cycles=50, seed0=10000, per_launch=64, params=None):
+SPAWN_STRIDE = 7919  # spawn seed of run r of a terrain: its seed + SPAWN_STRIDE * r
+
+
+def make_pairs(n, size=256, drops=None, cycles=50, seed0=10000, per_launch=64, params=None, spawn_runs=1):
     """Training pairs from the batched GPU particle method.  Terrain i is
     the value-noise heightmap of seed seed0 + i.  Its input is the heightmap
     before erosion.  Its targets are the discharge and momentum maps after
     `cycles` plain cycles from zero maps, at `drops` drops per cycle (by
-    default size^2 / 16, the density of 65,536 drops on 1024 x 1024).
-    Terrains run `per_launch` at a time in one Batch.  Returns float32
-    arrays (heights, discharge, momentum x, momentum y), each (n, size, size)."""
+    default size^2 / 16, the density of 65,536 drops on 1024 x 1024),
+    averaged over `spawn_runs` runs whose spawns differ (spawn seeds
+    seed0 + i + SPAWN_STRIDE * r): a target that depends on the terrain, not
+    on one run's spawn order.  Terrains run `per_launch` at a time (times
+    the runs) in one Batch.  Returns float32 arrays (heights, discharge,
+    momentum x, momentum y), each (n, size, size)."""
     from . import Batch
     drops = drops or max(1, size * size // 16)
+    runs = max(1, int(spawn_runs))
     out = [np.empty((n, size, size), np.float32) for _ in range(4)]
+    tmp = np.empty((size, size), np.float32)
     for s in range(0, n, per_launch):
         k = min(per_launch, n - s)
-        b = Batch([(size, size)] * k, [drops] * k, [seed0 + s + i for i in range(k)], params)
+        seeds = [seed0 + s + i + SPAWN_STRIDE * r for r in range(runs) for i in range(k)]
+        b = Batch([(size, size)] * (k * runs), [drops] * (k * runs), seeds, params)
         try:
+            for r in range(runs):
+                for i in range(k):
+                    b.generate(r * k + i, seed0 + s + i, 8)
             for i in range(k):
-                b.generate(i, seed0 + s + i, 8)
                 b.get_field(i, "height", out=out[0][s + i])
             b.erode(cycles)
-            for i in range(k):
-                for j, f in enumerate(("discharge", "momentum_x", "momentum_y")):
-                    b.get_field(i, f, out=out[j + 1][s + i])
+            for j, f in enumerate(("discharge", "momentum_x", "momentum_y")):
+                for i in range(k):
+                    acc = np.zeros((size, size), np.float64)
+                    for r in range(runs):
+                        acc += b.get_field(r * k + i, f, out=tmp)
+                    out[j + 1][s + i] = (acc / runs).astype(np.float32)
         finally:
             b.close()
     return tuple(out)
@@ -628,4 +642,5 @@ def log_l2(d, ref):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-__all__ = ["Surrogate", "Norm", "LAYERS", "param_count", "flops_per_pixel", "make_pairs", "train", "log_l2"]
+__all__ = ["Surrogate", "Norm", "LAYERS", "param_count", "flops_per_pixel", "make_pairs", "train", "log_l2",
+           "SPAWN_STRIDE"]
