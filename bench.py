@@ -739,6 +739,10 @@ def run_surrogate(args):
     clock.__exit__()
     tps = [r["plain_s"] for r in per if r["plain_s"]]
     tws = [r["warm_s"] for r in per if r["warm_s"]]
+    # what the prediction is worth: the plain cycles' device time to the
+    # prediction's distance from D*, against the warm start's cost
+    lv = [(r["prediction_worth_plain_cycles"] * r["ms_per_cycle"] / 1e3, r["warm_start_s"]) for r in per
+          if r["prediction_worth_plain_cycles"]]
     out = {"metric": "time to converged discharge (within 5% of the plain runs' floor, log-L2), plain vs "
                      "surrogate warm start", "unit": "s",
            "value": statistics.mean(tws) if tws else None,
@@ -746,6 +750,10 @@ def run_surrogate(args):
            "warm_s": statistics.mean(tws) if tws else None,
            "speedup": (statistics.mean(tps) / statistics.mean(tws)) if tps and tws else None,
            "target_speedup": 3.0,
+           "prediction_level": {"plain_s": statistics.mean(a for a, _ in lv) if lv else None,
+                                "warm_start_s": statistics.mean(b for _, b in lv) if lv else None,
+                                "speedup": (statistics.mean(a for a, _ in lv) / statistics.mean(b for _, b in lv))
+                                if lv else None},
            "higher_is_better": False, "n_gpus": 1, "dtype": "bf16 (f32 accumulate)",
            "data": "synthetic (seeded value-noise terrains; training pairs from the GPU particle method)",
            "config": {"workload": "learned warm-start: U-Net (1.36 M parameters, 4 levels, channels 32-256) "
