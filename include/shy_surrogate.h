@@ -36,7 +36,8 @@ extern "C" {
  * multiples of 16.  tile, stages and tap_rows tune the TMA pipeline for
  * this call (0: the process-wide setting, see shy_sg_set_conv_tile,
  * shy_sg_set_wgrad_tile and shy_sg_set_conv_tap_rows): pixels per tile
- * (forward 128 or 256, weight gradient 64 or 128), stages (2..8), and taps
+ * (forward 128, 256 or 512 -- 512 on the SHY_SG_CONV_TMA path only --,
+ * weight gradient 64 or 128), stages (2..8), and taps
  * per stage of a 3x3 forward or input gradient (1 or 3). */
 typedef struct shy_sg_conv_desc {
   int32_t batch, height, width;
@@ -61,7 +62,8 @@ typedef struct shy_sg_conv_desc {
 #define SHY_SG_CONV_PERSISTENT 2
 int shy_sg_set_conv_path(int32_t path);
 /* Tile and depth of the TMA pipeline (process-wide): pixels per tile (128,
- * or 256 with two accumulators sharing each weight chunk) and stages
+ * or 256 / 512 with two / four accumulators sharing each weight chunk; 512
+ * uses 32-channel chunks and all of the SM's tensor memory) and stages
  * (2..8, one channel chunk each); 0 for either (the default) chooses per
  * convolution.  Deeper pipelines keep more loads in flight; shallower ones
  * fit more CTAs on an SM. */

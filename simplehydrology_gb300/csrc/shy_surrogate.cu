@@ -1413,16 +1413,24 @@ int conv_launch(const char* fn, const shy_sg_conv_desc* d, const void* x, int32_
     return SHY_ERR_INVALID_ARG;
   }
   const int ntile = pick_ntile(d->cout);
-  const int kc = d->cin % 64 == 0 ? 64 : d->cin % 32 == 0 ? 32 : 16;
   CUtensorMap mx, mw;
   // tile: the call's own choice, else the process-wide one, else 128 pixels
-  if (d->tile != 0 && d->tile != 128 && d->tile != 256) {
-    set_error("%s: tile %d (0, 128 or 256 pixels)", fn, d->tile);
+  if (d->tile != 0 && d->tile != 128 && d->tile != 256 && d->tile != 512) {
+    set_error("%s: tile %d (0, 128, 256 or 512 pixels)", fn, d->tile);
     return SHY_ERR_INVALID_ARG;
   }
   const int pix = d->tile ? d->tile : g_conv_pixels;
   const int mt = pix ? pix / kTileM : 1;
   const bool tma_path = g_conv_path == SHY_SG_CONV_TMA || g_conv_path == SHY_SG_CONV_PERSISTENT;
+  // 512-pixel tiles: four accumulators of up to 128 columns (all of TMEM at
+  // N = 128, one CTA per SM) and 32-channel chunks, so that two or three
+  // stages fit in shared memory; each weight chunk then feeds 512 pixels.
+  // The persistent path double-buffers its accumulators and cannot hold them.
+  if (mt == 4 && (!tma_path || g_conv_path == SHY_SG_CONV_PERSISTENT)) {
+    set_error("%s: 512-pixel tiles are for the TMA path (one CTA per tile)", fn);
+    return SHY_ERR_INVALID_ARG;
+  }
+  const int kc = (d->cin % 64 == 0 && mt < 4) ? 64 : d->cin % 32 == 0 ? 32 : 16;
   // 3x3 on the one-CTA-per-tile TMA path: one input box per kernel column
   if (d->tap_rows != 0 && d->tap_rows != 1 && d->tap_rows != 3) {
     set_error("%s: tap_rows %d (0, 1 or 3)", fn, d->tap_rows);
@@ -1825,8 +1833,9 @@ extern "C" int shy_sg_set_conv_path(int32_t path) {
 }
 
 extern "C" int shy_sg_set_conv_tile(int32_t pixels, int32_t stages) {
-  if ((pixels != 0 && pixels != 128 && pixels != 256) || (stages != 0 && (stages < 2 || stages > kMaxStages))) {
-    set_error("shy_sg_set_conv_tile: %d pixels (0, 128 or 256), %d stages (0 or 2..%d)", pixels, stages,
+  if ((pixels != 0 && pixels != 128 && pixels != 256 && pixels != 512) ||
+      (stages != 0 && (stages < 2 || stages > kMaxStages))) {
+    set_error("shy_sg_set_conv_tile: %d pixels (0, 128, 256 or 512), %d stages (0 or 2..%d)", pixels, stages,
               kMaxStages);
     return SHY_ERR_INVALID_ARG;
   }

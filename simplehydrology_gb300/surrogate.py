@@ -58,7 +58,7 @@ LEVEL = {"enc0a": 0, "enc0b": 0, "enc1a": 1, "enc1b": 1, "enc2a": 2, "enc2b": 2,
 # taps per stage) for forward and input-gradient convolutions (taps per
 # stage 3 applies to 3x3 kernels), (pixels per stage, stages) for weight
 # gradients
-CONV_TILES = tuple((px, st, rows) for rows in (1, 3) for px in (128, 256) for st in (2, 3))
+CONV_TILES = tuple((px, st, rows) for rows in (1, 3) for px in (128, 256, 512) for st in (2, 3))
 WGRAD_TILES = ((64, 2), (64, 3), (128, 2), (128, 3))
 
 

@@ -92,7 +92,8 @@ def conv_path(request, sg):
     ok(lib().shy_sg_set_conv_tap_rows(3))
 
 
-@pytest.fixture(params=[(0, 0), (256, 2), (256, 3), (128, 4)], ids=["auto", "256px2", "256px3", "128px4"])
+@pytest.fixture(params=[(0, 0), (256, 2), (256, 3), (128, 4), (512, 2), (512, 3)],
+                ids=["auto", "256px2", "256px3", "128px4", "512px2", "512px3"])
 def conv_tile(request, sg):
     """The TMA convolution's pixel tiles and depths; the automatic choice is restored after."""
     ok(lib().shy_sg_set_conv_tile(*request.param))
@@ -116,6 +117,12 @@ def test_conv_forward_matches_oracle(sg, conv_path, conv_tile, case):
     a = torch.zeros((P, as_), dtype=torch.bfloat16, device="cuda")
     from simplehydrology_gb300._capi import SgConvDesc
     d = SgConvDesc(B, H, W, ci, co, k)
+    if conv_path == 2 and conv_tile[0] == 512:
+        # the persistent path double-buffers its accumulators: four of them
+        # would not fit in tensor memory, so the call is refused up front
+        rc = lib().shy_sg_conv_forward(C.byref(d), p(xd), xs, p(wd), p(bd), p(z), zs, zo, p(a), as_, ao, 1, None)
+        assert rc == -1 and b"512" in lib().shy_last_error()
+        return
     ok(lib().shy_sg_conv_forward(C.byref(d), p(xd), xs, p(wd), p(bd), p(z), zs, zo, p(a), as_, ao, 1, None))
     status()
     want = so.conv(x[..., :ci], w, b).reshape(P, co)
