@@ -1423,21 +1423,23 @@ int conv_launch(const char* fn, const shy_sg_conv_desc* d, const void* x, int32_
   const int mt = pix ? pix / kTileM : 1;
   const bool tma_path = g_conv_path == SHY_SG_CONV_TMA || g_conv_path == SHY_SG_CONV_PERSISTENT;
   // 512-pixel tiles: four accumulators of up to 128 columns (all of TMEM at
-  // N = 128, one CTA per SM) and 32-channel chunks, so that two or three
-  // stages fit in shared memory; each weight chunk then feeds 512 pixels.
-  // The persistent path double-buffers its accumulators and cannot hold them.
+  // N = 128, one CTA per SM); each weight chunk then feeds 512 pixels.  With
+  // three taps per stage they take 32-channel chunks, so that two or three
+  // stages fit in shared memory; with one tap per stage 64-channel chunks
+  // (128-byte box rows) fit two stages.  The persistent path double-buffers
+  // its accumulators and cannot hold four.
   if (mt == 4 && (!tma_path || g_conv_path == SHY_SG_CONV_PERSISTENT)) {
     set_error("%s: 512-pixel tiles are for the TMA path (one CTA per tile)", fn);
     return SHY_ERR_INVALID_ARG;
   }
-  const int kc = (d->cin % 64 == 0 && mt < 4) ? 64 : d->cin % 32 == 0 ? 32 : 16;
-  // 3x3 on the one-CTA-per-tile TMA path: one input box per kernel column
   if (d->tap_rows != 0 && d->tap_rows != 1 && d->tap_rows != 3) {
     set_error("%s: tap_rows %d (0, 1 or 3)", fn, d->tap_rows);
     return SHY_ERR_INVALID_ARG;
   }
   const int rows_want = d->tap_rows ? d->tap_rows : g_conv_tap_rows;
   const int tap_rows = (g_conv_path == SHY_SG_CONV_TMA && d->ksize == 3 && rows_want == 3) ? 3 : 1;
+  const int kc = (d->cin % 64 == 0 && (mt < 4 || tap_rows == 1)) ? 64 : d->cin % 32 == 0 ? 32 : 16;
+  // (3x3 on the one-CTA-per-tile TMA path: one input box per kernel column)
   if (tma_path && encode_conv_maps(d, x, x_stride, w, kc, ntile, mt, tap_rows, &mx, &mw)) {
     ConvTma p{};
     p.bias = bias;
