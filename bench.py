@@ -841,6 +841,61 @@ def run_surrogate_step(args):
         "clocks": clock.summary()}))
 
 
+def run_surrogate_conv(args):
+    """The surrogate's largest convolution alone -- dec2a forward, 384 -> 128
+    channels, 3x3, at the training batch (16 x 64 x 64 pixels, 58.0 GFLOP)
+    with GELU -- for each TMA tile setting (pixels, stages, taps per stage),
+    or only the one given by --tile/--stages/--tap-rows.  CUDA events over
+    --steps launches after --warmup."""
+    import torch
+
+    import simplehydrology_gb300 as shy
+    from simplehydrology_gb300 import build as shybuild
+    from simplehydrology_gb300 import surrogate as sg
+    shybuild.build()
+    net = sg.Surrogate(seed=SEED)
+    net.prep_weights()
+    batch = 16
+    ws = net.workspace(batch, 256, 256, True)
+    flops = 2.0 * batch * 64 * 64 * 9 * 384 * 128
+    if args.tile:
+        cands = [(args.tile, args.stages_conv, args.tap_rows)]
+    else:
+        cands = [c for c in sg.CONV_TILES]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    res = {}
+    for px, st, rows in cands:
+        shy._capi.check(shy.lib().shy_sg_set_conv_tile(px, st))
+        shy._capi.check(shy.lib().shy_sg_set_conv_tap_rows(rows))
+        for _ in range(args.warmup):
+            net._conv(ws, "dec2a", ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
+        ev[0].record()
+        for _ in range(args.steps):
+            net._conv(ws, "dec2a", ws.cat[2], 384, ws.z["dec2a"], 128, 0, ws.a["dec2a"], 128, 0, sg.ACT_GELU)
+        ev[1].record()
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1]) / args.steps
+        res[f"{px}x{st}x{rows}"] = {"ms": ms, "tflops": flops / (ms / 1e3) / 1e12}
+    net.status()
+    shy._capi.check(shy.lib().shy_sg_set_conv_tile(0, 0))
+    shy._capi.check(shy.lib().shy_sg_set_conv_tap_rows(3))
+    best = max(res, key=lambda k: res[k]["tflops"])
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, src = float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        peak, src = 1900.0, "fallback"
+    print(json.dumps({"metric": "largest surrogate convolution throughput", "value": res[best]["tflops"],
+                      "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "higher_is_better": True, "dtype": "bf16 (f32 accumulate)", "data": "synthetic",
+                      "config": {"workload": "dec2a forward, 16 x 64 x 64 pixels, 384 -> 128, 3x3, GELU",
+                                 "best": best},
+                      "roofline": {"bound": "tensor", "achieved": res[best]["tflops"], "peak": peak,
+                                   "unit": "TFLOP/s", "frac": res[best]["tflops"] / peak, "peak_source": src,
+                                   "kernel": "conv_tma_kernel", "traffic": None},
+                      "by_tile": res}))
+
+
 def _initial_height(shy, seed, n):
     w = shy.World(n, n, seed=seed)
     w.generate(seed, 8)
@@ -865,7 +920,11 @@ def main():
     # default: the single-terrain workload on one GPU; with N > 1 the
     # batched-terrain workload, sharded by whole terrain across the ranks
     ap.add_argument("--workload", default=None, choices=["plain", "batch", "converge", "large", "surrogate",
-                                                           "surrogate-step"])
+                                                           "surrogate-step", "surrogate-conv"])
+    # --workload surrogate-conv: one tile setting (default: every candidate)
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--stages-conv", type=int, default=0)
+    ap.add_argument("--tap-rows", type=int, default=3)
     ap.add_argument("--ref-cycles", type=int, default=2000)
     ap.add_argument("--check-every", type=int, default=10)
     ap.add_argument("--terrains", type=int, default=64)
@@ -893,6 +952,8 @@ def main():
         run_surrogate(args)
     elif args.workload == "surrogate-step":
         run_surrogate_step(args)
+    elif args.workload == "surrogate-conv":
+        run_surrogate_conv(args)
     else:
         run_ours(args)
 
