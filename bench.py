@@ -322,9 +322,11 @@ def run_ours(args):
     if args.autotune:
         from simplehydrology_gb300 import autotune
         best, times = autotune.autotune(w, None if args.workload == "batch" else wl.drops, cycles=3)
+        graph, gtimes = autotune.autotune.last_graphs
         tune = {"best": list(best), "ms_per_cycle": {"x".join(str(v) for v in k): round(t * 1e3, 4)
                                                       for k, t in sorted(times.items(), key=lambda kv: kv[1])},
-                "shape": "grid x order x block x smem_slots (grid 0: every resident CTA)"}
+                "shape": "grid x order x block x smem_slots (grid 0: every resident CTA)",
+                "cycles_per_graph": graph, "ms_per_cycle_by_graph": {g: round(t * 1e3, 4) for g, t in gtimes.items()}}
 
     # warm-up on the same workload, then restart from the initial terrain
     for _ in range(args.warmup):

@@ -191,6 +191,13 @@ int shy_world_set_launch(shy_world* w, int grid, int order);
  * where they fit without lowering occupancy, 0 always in global memory.
  * Results do not depend on either setting. */
 int shy_world_set_block(shy_world* w, int threads, int smem_slots);
+/* Batched cycles per CUDA graph: with k > 0, shy_erode / shy_batch_erode run
+ * each k cycles as one graph (the lock-step and end-of-cycle launches of k
+ * cycles), captured on the world's stream on first use and again whenever
+ * the parameters, drops, launch shape or buffers change; leftover cycles and
+ * calls with per-kernel timing on launch one by one.  0 (the default): no
+ * graphs.  Results do not depend on it. */
+int shy_world_set_graph(shy_world* w, int cycles_per_graph);
 
 /* Test hook for the library's bounded device waits (no counterpart in the
  * reference, which has no device code).  While `ns` is non-zero, the first

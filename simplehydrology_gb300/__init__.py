@@ -111,6 +111,10 @@ class _Handle:
         drop slots may live in shared memory (1) or always in global (0)."""
         check(lib().shy_world_set_block(self._w, threads, smem_slots))
 
+    def set_graph(self, cycles_per_graph: int = 0):
+        """Run batched cycles as CUDA graphs of this many cycles (0: none)."""
+        check(lib().shy_world_set_graph(self._w, cycles_per_graph))
+
     def set_cycle(self, cycle: int):
         check(lib().shy_world_set_cycle(self._w, cycle))
 

@@ -8,11 +8,13 @@ The batched kernel's launch shape changes its speed, never its results:
   CTA;
 * whether a cycle's drops are dealt to the CTAs in spawn-cell order;
 * whether a CTA's drop slots may live in shared memory (when they fit) or
-  always in global memory.
+  always in global memory;
+* how many cycles run as one CUDA graph.
 
 `autotune` tries candidate shapes on copies of a world's current state
 (through a checkpoint file), times each over `cycles` cycles with CUDA
-events on the copy's stream, and applies the fastest to the world.
+events on the copy's stream, and applies the fastest to the world; then,
+with that shape, it times each cycles-per-graph setting the same way.
 """
 from __future__ import annotations
 
@@ -23,6 +25,7 @@ from . import Batch, World, load
 
 BLOCKS = (64, 128, 256)
 ORDERS = (-1, 0, 1)
+GRAPHS = (0, 1, 4, 16)  # cycles per CUDA graph (0: launched one by one)
 
 
 def sm_count(device: int | None = None) -> int:
@@ -60,12 +63,43 @@ def apply(world, shape):
     world.set_block(block, smem)
 
 
-def autotune(world, drops: int | None = None, cycles: int = 3, shapes=None, sms: int | None = None):
-    """Time `cycles` batched cycles (at least 3) for each launch shape on a
-    copy of `world`'s state and apply the fastest shape to `world`.  `drops`
-    is the drops per cycle for a single-terrain World (a Batch keeps its
-    own).  Returns (best_shape, {shape: seconds per cycle})."""
+def _time(path, shape, graph, drops, cycles, warm):
+    """Seconds per cycle of `cycles` cycles on a copy of the checkpoint, after
+    `warm` untimed cycles (which also capture any graph)."""
     import torch
+    w = load(path)
+    try:
+        apply(w, shape)
+        w.set_graph(graph)
+
+        def erode(n):
+            if isinstance(w, Batch):
+                w.erode(n)
+            else:
+                w.erode(drops, n)
+
+        erode(warm)
+        w.sync()
+        stream = torch.cuda.ExternalStream(w.stream())
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record(stream)
+        erode(cycles)
+        ev[1].record(stream)
+        w.sync()
+        return ev[0].elapsed_time(ev[1]) / 1e3 / cycles
+    finally:
+        w.close()
+
+
+def autotune(world, drops: int | None = None, cycles: int = 3, shapes=None, sms: int | None = None,
+             graphs=GRAPHS):
+    """Time `cycles` batched cycles (at least 3) for each launch shape on a
+    copy of `world`'s state and apply the fastest shape to `world`; then time
+    each cycles-per-graph setting in `graphs` with that shape (over at least
+    the largest setting's cycles) and apply the fastest.  `drops` is the drops
+    per cycle for a single-terrain World (a Batch keeps its own).  Returns
+    (best_shape, {shape: seconds per cycle}); the graph choice and its
+    timings are in the attribute `autotune.last_graphs`."""
     if isinstance(world, World) and drops is None:
         raise ValueError("drops per cycle is needed for a World")
     cycles = max(3, int(cycles))
@@ -73,33 +107,22 @@ def autotune(world, drops: int | None = None, cycles: int = 3, shapes=None, sms:
     shapes = [_full(s) for s in shapes]
     fd, path = tempfile.mkstemp(suffix=".ckpt")
     os.close(fd)
-    times = {}
-
-    def erode(w, n):
-        if isinstance(w, Batch):
-            w.erode(n)
-        else:
-            w.erode(drops, n)
-
+    times, gtimes = {}, {}
     try:
         world.save(path)
         for shape in shapes:
-            w = load(path)
-            try:
-                apply(w, shape)
-                erode(w, 1)  # first launch of this shape (attribute set-up)
-                w.sync()
-                stream = torch.cuda.ExternalStream(w.stream())
-                ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-                ev[0].record(stream)
-                erode(w, cycles)
-                ev[1].record(stream)
-                w.sync()
-                times[shape] = ev[0].elapsed_time(ev[1]) / 1e3 / cycles
-            finally:
-                w.close()
+            times[shape] = _time(path, shape, 0, drops, cycles, 1)
+        best = min(times, key=times.get)
+        gc = max([cycles] + [int(g) for g in graphs])
+        for g in graphs:
+            gtimes[int(g)] = _time(path, best, int(g), drops, gc, max(1, int(g)))
     finally:
         os.remove(path)
-    best = min(times, key=times.get)
     apply(world, best)
+    graph = min(gtimes, key=gtimes.get) if gtimes else 0
+    world.set_graph(graph)
+    autotune.last_graphs = (graph, gtimes)
     return best, times
+
+
+autotune.last_graphs = (0, {})

@@ -188,6 +188,9 @@ struct shy_world {
   int batch_order = -1;       // slots in spawn-cell order: -1 when the cell state outgrows L2, 0 never, 1 always
   int batch_block = 256;      // threads per CTA of the lock-step kernel: 64, 128 or 256
   int batch_smem = 1;         // 0: drop slots in global memory even where shared memory would hold them
+  int graph_cycles = 0;       // batched cycles per CUDA graph (0: launched one by one)
+  cudaGraphExec_t gexec = nullptr;  // the captured cycles
+  unsigned long long graph_key = 0; // what they were captured with (launch_key)
 
   shy::Timing timing;
   float* normals = nullptr;   // 3 x cells, lazily allocated

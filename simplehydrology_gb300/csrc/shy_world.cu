@@ -95,6 +95,7 @@ template <class T> cudaError_t dalloc(T** p, size_t n) {
 void free_world(shy_world* w) {
   if (!w) return;
   if (w->stream) cudaStreamSynchronize(w->stream);
+  if (w->gexec) cudaGraphExecDestroy(w->gexec);
   void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage, w->dgain,
                   w->dterr, w->dcell, w->dctr, w->dterrains, w->stats, w->bar, w->ddrop,
                   w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down,
@@ -715,6 +716,17 @@ int shy_world_set_block(shy_world* w, int threads, int smem_slots) {
   return SHY_OK;
 }
 
+int shy_world_set_graph(shy_world* w, int cycles_per_graph) {
+  int rc = check_world(w);
+  if (rc) return rc;
+  if (cycles_per_graph < 0 || cycles_per_graph > 4096) {
+    set_error("shy_world_set_graph: cycles per graph must lie in [0, 4096]");
+    return SHY_ERR_INVALID_ARG;
+  }
+  w->graph_cycles = cycles_per_graph;
+  return SHY_OK;
+}
+
 int shy_world_sync(shy_world* w) {
   int rc = check_world(w);
   if (rc) return rc;
@@ -835,6 +847,68 @@ int shy_world_set_erf_source(shy_world* w, int source) {
   return SHY_OK;
 }
 
+namespace {
+
+// FNV-1a over what a captured batched cycle bakes in on the host: the
+// parameters, the terrain table, the launch shape and every buffer pointer
+// the launches take.  A graph is captured again when any of it changed.
+unsigned long long launch_key(const shy_world* w) {
+  unsigned long long h = 1469598103934665603ull;
+  auto mix = [&](const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) {
+      h ^= b[i];
+      h *= 1099511628211ull;
+    }
+  };
+  mix(&w->P, sizeof(w->P));
+  for (const auto& T : w->terrains) mix(&T, sizeof(T));
+  const int shape[6] = {w->batch_grid, w->batch_order, w->batch_block, w->batch_smem, w->graph_cycles, w->sm_count};
+  mix(shape, sizeof(shape));
+  const void* ptrs[] = {w->h, w->cq, w->rec, w->voltab, w->trk, w->track_f, w->dpos, w->dspd, w->dvs, w->dage,
+                        w->dgain, w->down, w->dterr, w->dcell, w->dctr, w->dsteep, w->arr, w->dorder, w->dkey,
+                        w->drank, w->dhist, w->dterrains, w->stats, w->bar, w->relax, w->hq_relax};
+  mix(ptrs, sizeof(ptrs));
+  return h;
+}
+
+// `cycles` batched cycles: with graph_cycles = K > 0 (and per-kernel timing
+// off), runs of K cycles go as one CUDA graph, captured on first use and
+// again whenever the launch key changes; the rest launch one by one.  The
+// cycle index and the counters live on the device, so every replay takes
+// the next spawns.
+int run_batched_cycles(shy_world* w, int cycles) {
+  const int K = w->graph_cycles;
+  int c = 0;
+  if (K > 0 && !w->timing.on && cycles >= K) {
+    const unsigned long long key = launch_key(w);
+    if (w->gexec && w->graph_key != key) {
+      cudaGraphExecDestroy(w->gexec);
+      w->gexec = nullptr;
+    }
+    if (!w->gexec) {
+      cudaGraph_t g = nullptr;
+      SHY_CHECK_CUDA(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeRelaxed), "begin graph capture");
+      cudaError_t e = cudaSuccess;
+      for (int i = 0; i < K && e == cudaSuccess; ++i) e = launch_batched_cycle(w);
+      const cudaError_t e2 = cudaStreamEndCapture(w->stream, &g);
+      if (e == cudaSuccess) e = e2;
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&w->gexec, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        w->gexec = nullptr;
+        return cuda_fail(e, "capture batched cycles into a CUDA graph");
+      }
+      w->graph_key = key;
+    }
+    for (; cycles - c >= K; c += K) SHY_CHECK_CUDA(cudaGraphLaunch(w->gexec, w->stream), "launch graph");
+  }
+  for (; c < cycles; ++c) SHY_CHECK_CUDA(launch_batched_cycle(w), "batched cycle");
+  return SHY_OK;
+}
+
+}  // namespace
+
 int shy_batch_erode(shy_world* w, int cycles) {
   int rc = check_world(w);
   if (rc) return rc;
@@ -849,7 +923,7 @@ int shy_batch_erode(shy_world* w, int cycles) {
   }
   if (w->P.cascade_passes > 0 && !w->hq_relax)
     SHY_CHECK_CUDA(dalloc(&w->hq_relax, (size_t)w->cells), "allocate relax buffer");
-  for (int c = 0; c < cycles; ++c) SHY_CHECK_CUDA(launch_batched_cycle(w), "batched cycle");
+  if ((rc = run_batched_cycles(w, cycles)) != SHY_OK) return rc;
   return check_device_error(w);
 }
 

@@ -276,6 +276,8 @@ def test_autotune_applies_a_shape_and_keeps_results(shy, po):
     best, times = autotune.autotune(w, drops, cycles=3)
     assert best in times and len(times) == len(autotune.candidates()) == 36
     assert all(t > 0 for t in times.values())
+    graph, gtimes = autotune.autotune.last_graphs
+    assert graph in gtimes and sorted(gtimes) == sorted(autotune.GRAPHS)
     w.erode(drops, 2)  # with the chosen shape
     m = po.Maps(nx, ny, height=H)
     po.erode_batched(m, 3, 0, drops, 2)
@@ -287,3 +289,27 @@ def test_autotune_counts_the_sms():
     torch = pytest.importorskip("torch")
     from simplehydrology_gb300 import autotune
     assert autotune.sm_count() == torch.cuda.get_device_properties(0).multi_processor_count
+
+
+def test_cycles_as_cuda_graphs_give_the_oracle_bits(shy, po):
+    """Cycles replayed from CUDA graphs (7 cycles in graphs of 3: two
+    replays and one cycle launched alone), a new capture after the drops per
+    cycle change, and per-kernel timing (no graphs) all give the oracle's
+    bits."""
+    nx, ny = 96, 80
+    H = po.value_noise(nx, ny, 21)
+    w = shy.World(nx, ny, seed=3)
+    w.set_field("height", H)
+    w.set_graph(3)
+    w.erode(2000, 7)
+    w.erode(1500, 4)  # another drop count: captured again
+    w.enable_timing(True)
+    w.erode(1500, 2)  # timed kernels: launched one by one
+    w.enable_timing(False)
+    m = po.Maps(nx, ny, height=H)
+    hq = np.zeros((nx, ny), np.int64)
+    po.erode_batched(m, 3, 0, 2000, 7, hq=hq)
+    po.erode_batched(m, 3, 7, 1500, 6, hq=hq)
+    compare_all(w.get_field, m, po, "graphs")
+    assert w.cycle() == 13
+    w.close()
