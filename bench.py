@@ -406,23 +406,29 @@ def run_ours(args):
     # drop-steps as the terrain wears down)
     whole = None
     if args.workload == "plain" and args.whole_cycles > 0:
+        # one World::erode call of every cycle, run as CUDA graphs of 16
+        # cycles (the graph is captured by an untimed call first)
+        w.set_graph(16)
+        wl.reset()
+        w.erode(wl.drops, 16)
         wl.reset()
         w.reset_stats()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
         torch.cuda.synchronize()
         with torch.cuda.stream(stream):
             ev[0].record(stream)
-        for _ in range(args.whole_cycles):
-            wl.erode()
+        w.erode(wl.drops, args.whole_cycles)
         with torch.cuda.stream(stream):
             ev[1].record(stream)
         torch.cuda.synchronize()
+        w.set_graph(0)
         whole_s = ev[0].elapsed_time(ev[1]) / 1e3
         ws_ = w.stats()
         whole = {"cycles": args.whole_cycles, "value": ws_.drop_steps / whole_s, "unit": METRIC,
                  "ms_per_cycle": whole_s * 1e3 / args.whole_cycles,
                  "drop_steps_per_cycle": ws_.drop_steps / args.whole_cycles,
-                 "timing": "device time of all cycles back to back (CUDA events), no L2 flush"}
+                 "timing": "one shy_erode call of all cycles from the initial terrain, CUDA graphs of 16 cycles, "
+                           "device time (CUDA events), no L2 flush"}
 
     config = dict(wl.config)
     config.update({"step": "one erosion cycle",
