@@ -86,10 +86,10 @@ struct alignas(16) SteepCell {
 
 // Grid barrier state of the persistent lock-step kernel.
 struct GridBar {
-  unsigned long long arrive;  // monotonically increasing arrival count
+  unsigned long long arrive;  // arrivals * 2^32 + drops still descending (the lock-step kernel's barrier)
   int abort;                  // set when a bounded wait gives up
   int error;                  // first error code seen on the device
-  unsigned long long live;    // drops still descending in the current cycle
+  unsigned long long live;    // unused (the live count rides on `arrive`)
   unsigned long long tick;    // unused
   unsigned long long cycle;   // batched cycle index (spawn RNG)
   // CTA 0's view of the lock-step phases: descend, wait, scan, wait,

@@ -48,6 +48,8 @@
 //
 // The end-of-cycle kernel converts the tracks to float, applies the lrate
 // blend (source/world.h:81-86) and rebuilds the per-cell records.
+#include <mutex>
+
 #include "shy_device.cuh"
 
 namespace shy {
@@ -132,28 +134,37 @@ __device__ __forceinline__ unsigned long long arr_bit(int x, int y) {
 
 // Grid-wide barrier over a monotonically increasing arrival counter (reset to
 // zero between launches).  `passed` counts the barriers this CTA has passed.
-// Thread 0 reads the live-drop count once the barrier is passed (every CTA
-// added its retirements before arriving) and leaves it in `*live` for the
-// whole CTA.  Every wait is bounded: past kBarrierLimitNs the waiter sets
-// bar->abort and every later barrier returns false at once, so the kernel
-// always ends.  Warps 1 and up run `work` while thread 0 waits: work that
-// neither reads what other CTAs write before the barrier nor writes what they
-// read.  `extra` arrivals beyond the grid's are awaited and `limit_ns`
-// bounds the wait: the bounded-wait test hook (shy_debug_stall_waits) asks
-// for one arrival that never comes, so the wait runs out.
+// The counter also carries the grid's live-drop count: each arrival adds
+// 2^32 plus the CTA's change to that count (`delta`, from thread 0), so after
+// n arrivals the counter is n * 2^32 + live, with 0 <= live < 2^32 once all
+// of a barrier's arrivals are in (every change is added by then).  The wait
+// ends when the counter reaches target * 2^32 -- exact, since before the last
+// arrival the partial sum is below that -- and the low 32 bits of the value
+// read then are the live count, left in `*live` for the whole CTA: arrivals
+// at the next barrier (possible before this CTA reads) add 2^32 with no
+// change, because the count changes only at spawn and at the end of a step.
+// Every wait is bounded: past limit_ns the waiter sets bar->abort and every
+// later barrier returns false at once, so the kernel always ends.  Warps 1
+// and up run `work` while thread 0 waits: work that neither reads what other
+// CTAs write before the barrier nor writes what they read.  `extra` arrivals
+// beyond the grid's are awaited: the bounded-wait test hook
+// (shy_debug_stall_waits) asks for one arrival that never comes, so the wait
+// runs out.
 template <class Work>
 __device__ bool grid_barrier(GridBar* bar, unsigned& passed, unsigned long long* live, Work&& work,
-                             unsigned extra = 0, unsigned long long limit_ns = kBarrierLimitNs) {
+                             unsigned extra = 0, unsigned long long limit_ns = kBarrierLimitNs,
+                             long long delta = 0) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x >= 32) work();
   if (threadIdx.x == 0) {
-    const unsigned long long target = (unsigned long long)(passed + 1) * gridDim.x + extra;
-    red_release_add_u64(&bar->arrive, 1ull);
+    const unsigned long long target = ((unsigned long long)(passed + 1) * gridDim.x + extra) << 32;
+    red_release_add_u64(&bar->arrive, (1ull << 32) + (unsigned long long)delta);
     int ok = 1;
     unsigned long long t0 = 0;
     unsigned spins = 0;
-    while (ld_acquire_u64(&bar->arrive) < target) {
+    unsigned long long v;
+    while ((v = ld_acquire_u64(&bar->arrive)) < target) {
       if (++spins < 64) continue;
       if (t0 == 0) t0 = global_ns();
       if (ld_relaxed_i32(&bar->abort)) {
@@ -168,7 +179,7 @@ __device__ bool grid_barrier(GridBar* bar, unsigned& passed, unsigned long long*
       }
       __nanosleep(64);
     }
-    if (live) *live = ld_relaxed_u64(&bar->live);
+    if (live) *live = (v - target) & 0xffffffffull;
     s_ok = ok;
   }
   __syncthreads();
@@ -554,12 +565,9 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     S.gain[j] = 0;
     atomicAdd(&a.cq[c].cnt[0], 1);
   }
-  {
-    const unsigned long long s = block_sum_u64<kBlock>(born);
-    if (threadIdx.x == 0 && s) atomicAdd(&a.bar->live, s);
-  }
+  const unsigned long long born_all = block_sum_u64<kBlock>(born);  // valid in thread 0
   bool ok = grid_barrier(a.bar, passed, &s_live, [] {}, a.stall_ns ? 1u : 0u,
-                         a.stall_ns ? a.stall_ns : kBarrierLimitNs);
+                         a.stall_ns ? a.stall_ns : kBarrierLimitNs, (long long)born_all);
 
   int step = 0;
   for (; ok && step < a.max_steps; ++step) {
@@ -821,12 +829,12 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         ++retired;
       }
     }
-    {
-      const unsigned long long s = block_sum_u64<kBlock>(retired);
-      if (threadIdx.x == 0 && s) atomicAdd(&a.bar->live, (unsigned long long)(-(long long)s));
-    }
+    const unsigned long long retired_all = block_sum_u64<kBlock>(retired);  // valid in thread 0
     lap(4);
-    if (!grid_barrier(a.bar, passed, &s_live)) { ok = false; break; }
+    if (!grid_barrier(a.bar, passed, &s_live, [] {}, 0u, kBarrierLimitNs, -(long long)retired_all)) {
+      ok = false;
+      break;
+    }
   }
   lap(5);
 
@@ -845,7 +853,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   if (timer) {
     for (int i = 0; i < 6; ++i) a.bar->phase_ns[i] += s_ph[i];
     a.bar->iterations += (unsigned long long)step;
-    if (ok && a.bar->live != 0) atomicCAS(&a.bar->error, 0, SHY_ERR_STATE);
+    if (ok && s_live != 0) atomicCAS(&a.bar->error, 0, SHY_ERR_STATE);
   }
 }
 
@@ -1029,37 +1037,81 @@ namespace {
 // drops per CTA); each CTA's drop slots go to shared memory when they fit
 // without lowering that occupancy (and the world allows it), else to the
 // global arrays in `a`.
+// What a launch of lockstep_kernel<kBlock> needs to know about the device,
+// queried once per device and CTA size (and per dynamic shared-memory size
+// for the occupancy with slots in shared memory) rather than every cycle.
+struct LaunchFacts {
+  bool valid = false;
+  int optin = 0;               // opt-in shared memory per CTA
+  long long static_smem = 0;   // the kernel's static shared memory
+  int per0 = 0;                // resident CTAs per SM without dynamic shared memory
+  long long smem_set = 0;      // dynamic shared memory the attribute allows
+  long long last_b = -1;       // last dynamic size asked about, and its
+  int last_per = 0;            //   resident CTAs per SM
+};
+const int kMaxDevices = 64;
+std::mutex g_facts_mu;
+
 template <int kBlock>
-cudaError_t launch_lockstep_n(LockArgs& a, int sm_count, int grid_hint, cudaStream_t stream) {
-  int dev = 0, optin = 0, per0 = 0;
+cudaError_t launch_facts(LaunchFacts** out) {
+  static LaunchFacts facts[kMaxDevices];
+  int dev = 0;
   cudaError_t e;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-  if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
-  cudaFuncAttributes fa;
-  if ((e = cudaFuncGetAttributes(&fa, lockstep_kernel<kBlock>)) != cudaSuccess) return e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, lockstep_kernel<kBlock>, kBlock, 0)) != cudaSuccess)
-    return e;
-  if (per0 < 1) return cudaErrorLaunchOutOfResources;
-  const long long max_dyn = (long long)optin - (long long)fa.sharedSizeBytes;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  LaunchFacts& f = facts[dev];
+  if (!f.valid) {
+    if ((e = cudaDeviceGetAttribute(&f.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, lockstep_kernel<kBlock>)) != cudaSuccess) return e;
+    f.static_smem = (long long)fa.sharedSizeBytes;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f.per0, lockstep_kernel<kBlock>, kBlock, 0)) !=
+        cudaSuccess)
+      return e;
+    f.valid = true;
+  }
+  *out = &f;
+  return cudaSuccess;
+}
+
+// Launches one lock-step cycle with CTAs of kBlock threads.  The grid is
+// the resident CTAs per SM times the SMs (fewer for small cycles: at least 32
+// drops per CTA); each CTA's drop slots go to shared memory when they fit
+// without lowering that occupancy (and the world allows it), else to the
+// global arrays in `a`.
+template <int kBlock>
+cudaError_t launch_lockstep_n(LockArgs& a, int sm_count, int grid_hint, cudaStream_t stream) {
+  std::lock_guard<std::mutex> lock(g_facts_mu);
+  LaunchFacts* f = nullptr;
+  cudaError_t e;
+  if ((e = launch_facts<kBlock>(&f)) != cudaSuccess) return e;
+  if (f->per0 < 1) return cudaErrorLaunchOutOfResources;
+  const long long max_dyn = (long long)f->optin - f->static_smem;
   long long want = ((long long)a.total_drops + 31) / 32;
   if (want < 1) want = 1;
   if (grid_hint > 0 && want > grid_hint) want = grid_hint;
 
-  const long long g = (long long)per0 * sm_count < want ? (long long)per0 * sm_count : want;
+  const long long g = (long long)f->per0 * sm_count < want ? (long long)f->per0 * sm_count : want;
   const int grid = (int)g;
   const long long b = (long long)slot_range(a.total_drops, g, 0, a.order != nullptr).cap * kSlotBytes;
   size_t bytes = 0;
   a.smem_slots = 0;
   if (b <= max_dyn && a.smem_allowed) {
-    if (b > 48 * 1024 &&
-        (e = cudaFuncSetAttribute(lockstep_kernel<kBlock>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b)) !=
-            cudaSuccess)
-      return e;
-    int per = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lockstep_kernel<kBlock>, kBlock, (size_t)b)) !=
-        cudaSuccess)
-      return e;
-    if ((long long)per * sm_count >= g) {  // the slots fit without costing occupancy
+    if (b > 48 * 1024 && b > f->smem_set) {
+      if ((e = cudaFuncSetAttribute(lockstep_kernel<kBlock>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b)) !=
+          cudaSuccess)
+        return e;
+      f->smem_set = b;
+    }
+    if (b != f->last_b) {
+      int per = 0;
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lockstep_kernel<kBlock>, kBlock, (size_t)b)) !=
+          cudaSuccess)
+        return e;
+      f->last_b = b;
+      f->last_per = per;
+    }
+    if ((long long)f->last_per * sm_count >= g) {  // the slots fit without costing occupancy
       a.smem_slots = 1;
       bytes = (size_t)b;
     }
