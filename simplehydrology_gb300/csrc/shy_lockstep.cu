@@ -150,14 +150,21 @@ __device__ __forceinline__ unsigned long long arr_bit(int x, int y) {
 // beyond the grid's are awaited: the bounded-wait test hook
 // (shy_debug_stall_waits) asks for one arrival that never comes, so the wait
 // runs out.
+// `retired`, if given, is a shared counter of drops the CTA's warps retired
+// since the last barrier: thread 0 subtracts it from the live count (on top
+// of `delta`) once every warp has arrived, and clears it.
 template <class Work>
 __device__ bool grid_barrier(GridBar* bar, unsigned& passed, unsigned long long* live, Work&& work,
                              unsigned extra = 0, unsigned long long limit_ns = kBarrierLimitNs,
-                             long long delta = 0) {
+                             long long delta = 0, unsigned* retired = nullptr) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x >= 32) work();
   if (threadIdx.x == 0) {
+    if (retired) {
+      delta -= (long long)*retired;
+      *retired = 0;
+    }
     const unsigned long long target = ((unsigned long long)(passed + 1) * gridDim.x + extra) << 32;
     red_release_add_u64(&bar->arrive, (1ull << 32) + (unsigned long long)delta);
     int ok = 1;
@@ -494,10 +501,14 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   __shared__ Terrain sT[kSmemTerrains];
   __shared__ int s_nq;                  // steep cascades queued this step
   __shared__ unsigned long long s_live;  // drops still descending
+  __shared__ unsigned s_retired;        // drops this CTA retired in the current step
   const bool smem_t = a.n_terrains <= kSmemTerrains;
   if (smem_t)
     for (int i = threadIdx.x; i < a.n_terrains; i += blockDim.x) sT[i] = a.terrains[i];
-  if (threadIdx.x == 0) s_nq = 0;
+  if (threadIdx.x == 0) {
+    s_nq = 0;
+    s_retired = 0;
+  }
   __syncthreads();
   const Terrain* TT = smem_t ? sT : a.terrains;
 
@@ -829,9 +840,12 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         ++retired;
       }
     }
-    const unsigned long long retired_all = block_sum_u64<kBlock>(retired);  // valid in thread 0
+    {  // per warp into the shared counter; the barrier takes it off the live count
+      const unsigned r = __reduce_add_sync(0xffffffffu, (unsigned)retired);
+      if ((threadIdx.x & 31) == 0 && r) atomicAdd(&s_retired, r);
+    }
     lap(4);
-    if (!grid_barrier(a.bar, passed, &s_live, [] {}, 0u, kBarrierLimitNs, -(long long)retired_all)) {
+    if (!grid_barrier(a.bar, passed, &s_live, [] {}, 0u, kBarrierLimitNs, 0, &s_retired)) {
       ok = false;
       break;
     }
