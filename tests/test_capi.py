@@ -117,3 +117,19 @@ def test_noalloc_rejects_invalid_parameters_on_the_host(shy, field, value):
     x = C.c_void_p(1)  # never dereferenced: the parameter checks come first
     rc = L.shy_erode_noalloc(64, 64, C.byref(p), 1, 0, 100, 1, x, x, x, x, x, None, None)
     assert rc == -1 and b"invalid parameters" in L.shy_last_error()
+
+
+def test_new_entry_points_check_their_arguments_on_the_host(shy):
+    """Launch shape, CUDA graphs, device state and cycle calls refuse a null
+    world (and bad values) with SHY_ERR_INVALID_ARG before touching a device."""
+    L = shy.lib()
+    assert L.shy_world_set_block(None, 256, 1) == -1
+    assert L.shy_world_set_graph(None, 4) == -1
+    c = C.c_uint64()
+    assert L.shy_world_get_cycle(None, C.byref(c)) == -1
+    assert L.shy_terrain_set_state_device(None, 0, None, None, None, None, 0) == -1
+    assert L.shy_terrain_get_state_device(None, 0, None, None, None, None, 0) == -1
+    assert L.shy_debug_stall_waits(20_000_000_000) == -1
+    assert L.shy_debug_stall_waits(0) == 0
+    assert L.shy_sg_set_conv_tile(384, 0) == -1 and b"512" in L.shy_last_error()
+    assert L.shy_sg_set_conv_tile(512, 3) == 0 and L.shy_sg_set_conv_tile(0, 0) == 0
