@@ -591,7 +591,7 @@ def run_converge(args):
     print(json.dumps(out))
 
 
-def _discharge_run(shy, seed, n, drops, cycles, warm=None, spawn_seed=None):
+def _discharge_run(shy, seed, n, drops, cycles, warm=None, spawn_seed=None, scale=1.0):
     """A plain run of `cycles` cycles on the value-noise terrain of `seed`
     from zero maps, or from the surrogate's maps when `warm` is given; the
     spawns follow `spawn_seed` (default `seed`).
@@ -604,7 +604,7 @@ def _discharge_run(shy, seed, n, drops, cycles, warm=None, spawn_seed=None):
     if warm is not None:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        warm.warm_start(w)
+        warm.warm_start(w, scale=scale)
         w.sync()
         t_warm = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(w.stream())
@@ -660,24 +660,36 @@ def run_surrogate(args):
     if side != 256:  # fewer, larger terrains, trained on random 256^2 crops
         n_tr, n_val = max(1, n_tr * 256 * 256 // (side * side)), max(1, 64 * 256 * 256 // (side * side))
     t0 = time.perf_counter()
-    H, D, MX, MY = sg.make_pairs(n_tr + n_val, size=side, cycles=horizon, seed0=10000,
+    H, D, MX, MY = sg.make_pairs((0 if args.load_net else n_tr) + n_val, size=side, cycles=horizon,
+                                 seed0=10000 + (n_tr if args.load_net else 0),
                                  per_launch=max(16, 64 * 256 * 256 // (side * side)), spawn_runs=runs)
+    if args.load_net:  # the held-out pairs only; the network comes from the file
+        pad = [np.zeros((n_tr,) + a.shape[1:], np.float32) for a in (H, D, MX, MY)]
+        H, D, MX, MY = (np.concatenate([p_, a]) for p_, a in zip(pad, (H, D, MX, MY)))
     gen_s = time.perf_counter() - t0
-    norm = sg.Norm.fit(H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr])
-    net = sg.Surrogate(seed=0, norm=norm)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     batch = 16
-    net.autotune(batch, 256, 256)
-    launches0 = net.launches
-    ev[0].record()
-    losses = sg.train(net, H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr], epochs=args.epochs, batch=batch, lr=2e-3,
-                      crop=256 if side != 256 else None, steps_per_epoch=args.train_terrains // batch)
-    ev[1].record()
-    torch.cuda.synchronize()
-    net.status()
-    train_ms = ev[0].elapsed_time(ev[1])
+    if args.load_net:
+        net = sg.Surrogate(seed=0)
+        net.load_state_dict(dict(np.load(args.load_net, allow_pickle=True)["state"].item()))
+        losses, train_ms, launches0 = [], 0.0, net.launches
+    else:
+        norm = sg.Norm.fit(H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr])
+        net = sg.Surrogate(seed=0, norm=norm)
+        net.autotune(batch, 256, 256)
+        launches0 = net.launches
+        ev[0].record()
+        losses = sg.train(net, H[:n_tr], D[:n_tr], MX[:n_tr], MY[:n_tr], epochs=args.epochs, batch=batch,
+                          lr=2e-3, crop=256 if side != 256 else None,
+                          steps_per_epoch=args.train_terrains // batch)
+        ev[1].record()
+        torch.cuda.synchronize()
+        net.status()
+        train_ms = ev[0].elapsed_time(ev[1])
+        if args.save_net:
+            np.savez(args.save_net, state=np.array(net.state_dict(), dtype=object))
     steps = args.epochs * (args.train_terrains // batch)
-    train_flops = steps * batch * 256 * 256 * sg.flops_per_pixel(True)
+    train_flops = steps * batch * 256 * 256 * sg.flops_per_pixel(True) if train_ms else 0.0
     # held-out 256^2 pairs: the prediction against the particle method's maps
     val_pred, _, _ = net.predict(torch.from_numpy(H[n_tr:]).cuda())
     vp = val_pred.cpu().numpy()
@@ -717,6 +729,7 @@ def run_surrogate(args):
     def first(dist, bound):
         return next((k + 1 for k, d in enumerate(dist) if d <= bound), None)
 
+    scales = [float(v) for v in args.warm_scales.split(",")]
     per = []
     for i in range(args.eval_terrains):
         seed = 20000 + i
@@ -727,26 +740,41 @@ def run_surrogate(args):
         dstar = [np.mean([f for q, f in enumerate(finals) if q != r], axis=0) for r in range(runs)]
         floor = float(np.mean([sg.log_l2(window(plain[r][0], horizon), dstar[r]) for r in range(runs)]))
         dp, mp, _ = plain[0]
-        dw_, mw, t_warm = _discharge_run(shy, seed, n, drops, total, warm=net)  # spawn order of run 0
         pred = net.predict(torch.from_numpy(_initial_height(shy, seed, n)[None]).cuda())[0][0].cpu().numpy()
         dist_p = [sg.log_l2(window(dp, k), dstar[0]) for k in range(1, total + 1)]
-        dist_w = [sg.log_l2(window(dw_, k), dstar[0]) for k in range(1, total + 1)]
         d_pred = sg.log_l2(pred, dstar[0])
         bound = (1.0 + theta) * floor
-        kp, kw = first(dist_p, bound), first(dist_w, bound)
+        kp = first(dist_p, bound)
         tp = sum(mp[:kp]) / 1e3 if kp else None
-        tw = t_warm + sum(mw[:kw]) / 1e3 if kw else None
-        per.append({"seed": seed, "floor": floor, "bound": bound, "cycles_plain": kp, "cycles_warm": kw,
-                    "plain_s": tp, "warm_s": tw, "speedup": (tp / tw) if tp and tw else None,
-                    "warm_start_s": t_warm, "log_l2_prediction": d_pred,
-                    "prediction_worth_plain_cycles": first(dist_p, d_pred),
-                    "strict_5pct_plain": first(dist_p, theta), "strict_5pct_warm": first(dist_w, theta),
-                    "log_l2_plain_window": [round(d, 4) for d in dist_p[::5]],
-                    "log_l2_warm_window": [round(d, 4) for d in dist_w[::5]],
-                    "ms_per_cycle": sum(mp) / len(mp)})
+        row = {"seed": seed, "floor": floor, "bound": bound, "cycles_plain": kp, "plain_s": tp,
+               "log_l2_prediction": d_pred, "prediction_worth_plain_cycles": first(dist_p, d_pred),
+               "strict_5pct_plain": first(dist_p, theta),
+               "log_l2_plain_window": [round(d, 4) for d in dist_p[::5]],
+               "ms_per_cycle": sum(mp) / len(mp), "warm": {}}
+        for scale in scales:  # the spawn order of run 0
+            dw_, mw, t_warm = _discharge_run(shy, seed, n, drops, total, warm=net, scale=scale)
+            dist_w = [sg.log_l2(window(dw_, k), dstar[0]) for k in range(1, total + 1)]
+            kw = first(dist_w, bound)
+            tw = t_warm + sum(mw[:kw]) / 1e3 if kw else None
+            row["warm"][str(scale)] = {"cycles_warm": kw, "warm_s": tw, "warm_start_s": t_warm,
+                                       "speedup": (tp / tw) if tp and tw else None,
+                                       "strict_5pct_warm": first(dist_w, theta),
+                                       "log_l2_warm_window": [round(d, 4) for d in dist_w[::5]]}
+        first_scale = row["warm"][str(scales[0])]
+        row.update({k: first_scale[k] for k in ("cycles_warm", "warm_s", "warm_start_s", "speedup",
+                                                 "strict_5pct_warm", "log_l2_warm_window")})
+        per.append(row)
     clock.__exit__()
     tps = [r["plain_s"] for r in per if r["plain_s"]]
     tws = [r["warm_s"] for r in per if r["warm_s"]]
+    by_scale = {}
+    for sc in scales:
+        ws_ = [r["warm"][str(sc)]["warm_s"] for r in per]
+        done = [w_ for w_ in ws_ if w_]
+        by_scale[str(sc)] = {"converged_terrains": len(done),
+                             "warm_s": statistics.mean(done) if done else None,
+                             "speedup": (statistics.mean(tps) / statistics.mean(done)) if tps and done and
+                             len(done) == len(per) else None}
     # what the prediction is worth: the plain cycles' device time to the
     # prediction's distance from D*, against the warm start's cost
     lv = [(r["prediction_worth_plain_cycles"] * r["ms_per_cycle"] / 1e3, r["warm_start_s"]) for r in per
@@ -758,6 +786,7 @@ def run_surrogate(args):
            "warm_s": statistics.mean(tws) if tws else None,
            "speedup": (statistics.mean(tps) / statistics.mean(tws)) if tps and tws else None,
            "target_speedup": 3.0,
+           "warm_scales": by_scale,
            "prediction_level": {"plain_s": statistics.mean(a for a, _ in lv) if lv else None,
                                 "warm_start_s": statistics.mean(b for _, b in lv) if lv else None,
                                 "speedup": (statistics.mean(a for a, _ in lv) / statistics.mean(b for _, b in lv))
@@ -773,7 +802,8 @@ def run_surrogate(args):
                       "eval_terrains": args.eval_terrains,
                       "train_terrains": n_tr, "train_side": side, "epochs": args.epochs, "batch": batch},
            "training": {"pairs_s": gen_s, "train_s": train_ms / 1e3, "steps": steps,
-                        "tflops": train_flops / (train_ms / 1e3) / 1e12,
+                        "tflops": train_flops / (train_ms / 1e3) / 1e12 if train_ms else None,
+                        "loaded_from": args.load_net or None,
                         "loss_by_epoch": [round(v, 5) for v in losses],
                         "launches": net.launches - launches0, "validation": val},
            "roofline": {"bound": "tensor", "kernel": "conv_tma_kernel (384->128, 3x3, 16x64x64 pixels)",
@@ -942,6 +972,10 @@ def main():
     ap.add_argument("--epochs", type=int, default=24)
     ap.add_argument("--eval-terrains", type=int, default=4)
     ap.add_argument("--spawn-runs", type=int, default=4)
+    ap.add_argument("--warm-scales", default="1.0",
+                    help="comma-separated scales of the warm start's maps (the first one fills the main keys)")
+    ap.add_argument("--save-net", default="", help="--workload surrogate: save the trained network (.npz)")
+    ap.add_argument("--load-net", default="", help="--workload surrogate: use this network instead of training")
     ap.add_argument("--train-side", type=int, default=256)
     ap.add_argument("--autotune", action="store_true",
                     help="run the launch-shape autotuner first and bench the fastest shape")

@@ -466,16 +466,23 @@ class Surrogate:
                    self._p(out[1]), self._p(out[2]))
         return tuple(out)
 
-    def warm_start(self, world, terrain: int = 0):
+    def warm_start(self, world, terrain: int = 0, scale: float = 1.0):
         """Write the predicted discharge and momentum maps of a terrain into a
-        World or Batch (its current heightmap is the input).  Device to
-        device: the heights come out and the maps go in through
+        World or Batch (its current heightmap is the input), times `scale`.
+        The plain method's maps after k cycles from zero are about
+        (1 - (1 - lrate)^k) of their settled values (the lrate blend,
+        source/world.h:83-85), so a scale below 1 starts the world where a
+        plain run stands after that many cycles.  Device to device: the
+        heights come out and the maps go in through
         shy_terrain_get/set_state_device, never through host memory."""
         torch = self.torch
         h = world.get_state_device(terrain)["height"]
         d, mx, my = self.predict(h[None])
+        if scale != 1.0:
+            d, mx, my = d * scale, mx * scale, my * scale
         torch.cuda.current_stream(self.dev).synchronize()
-        world.set_state_device(terrain, discharge=d[0], momentum_x=mx[0], momentum_y=my[0])
+        world.set_state_device(terrain, discharge=d[0].contiguous(), momentum_x=mx[0].contiguous(),
+                               momentum_y=my[0].contiguous())
 
     def warm_start_judged(self, world, drops: int, probe_cycles: int = 5, threshold: float = 0.05,
                           terrain: int = 0):
