@@ -1427,8 +1427,9 @@ int conv_launch(const char* fn, const shy_sg_conv_desc* d, const void* x, int32_
   // three taps per stage they take 32-channel chunks, so that two or three
   // stages fit in shared memory; with one tap per stage 64-channel chunks
   // (128-byte box rows) fit two stages.  The persistent path double-buffers
-  // its accumulators and cannot hold four.
-  if (mt == 4 && (!tma_path || g_conv_path == SHY_SG_CONV_PERSISTENT)) {
+  // its accumulators and cannot hold four; the staged path has its own tile
+  // and ignores this one.
+  if (mt == 4 && g_conv_path == SHY_SG_CONV_PERSISTENT) {
     set_error("%s: 512-pixel tiles are for the TMA path (one CTA per tile)", fn);
     return SHY_ERR_INVALID_ARG;
   }
