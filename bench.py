@@ -28,7 +28,9 @@ end-of-cycle pass over the whole step time.
 discharge (within 5 % log-L2 of the discharge after 4 x 500 cycles).
 
 `--workload surrogate` trains the learned warm-start on the device and
-compares the time to converged discharge with and without it;
+compares the time to converged discharge with and without it (`--warm-scales`
+tries scaled warm starts; `--save-net` / `--load-net` keep the network);
+`--workload surrogate-conv` times the largest convolution per tile setting;
 `--workload surrogate-step` times its training step alone (TFLOP/s).
 
 `--workload large` runs the large-scale configuration: 8192^2, 4,194,304
