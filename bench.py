@@ -316,6 +316,8 @@ def run_ours(args):
     else:
         wl = PlainWorkload(shy, args.map, args.drops)
     w = wl.w
+    if args.resort is not None:
+        w.set_resort(args.resort)
 
     # optional: the launch-shape autotuner on the initial state (each
     # candidate timed over 3 cycles on a checkpoint copy); the bench then
@@ -328,7 +330,9 @@ def run_ours(args):
         tune = {"best": list(best), "ms_per_cycle": {"x".join(str(v) for v in k): round(t * 1e3, 4)
                                                       for k, t in sorted(times.items(), key=lambda kv: kv[1])},
                 "shape": "grid x order x block x smem_slots (grid 0: every resident CTA)",
-                "cycles_per_graph": graph, "ms_per_cycle_by_graph": {g: round(t * 1e3, 4) for g, t in gtimes.items()}}
+                "cycles_per_graph": graph, "ms_per_cycle_by_graph": {g: round(t * 1e3, 4) for g, t in gtimes.items()},
+                "resort": autotune.autotune.last_resorts[0],
+                "ms_per_cycle_by_resort": {r: round(t * 1e3, 4) for r, t in autotune.autotune.last_resorts[1].items()}}
 
     # warm-up on the same workload, then restart from the initial terrain
     for _ in range(args.warmup):
@@ -436,6 +440,8 @@ def run_ours(args):
     config.update({"step": "one erosion cycle",
                    "cycles_timed": f"0-{args.steps - 1} of the workload, from the initial terrain",
                    "l2": "flushed between steps (256 MiB write, untimed)",
+                   "redeal_steps": (args.resort if args.resort is not None else
+                                    "library default: 16 with spawn-ordered slots in global memory, else none"),
                    "parallelism": (("terrain shards" if args.workload == "batch" else "replicas") +
                                    f" x{world_size}") if world_size > 1 else "single GPU"})
     out = {
@@ -979,6 +985,8 @@ def main():
     ap.add_argument("--save-net", default="", help="--workload surrogate: save the trained network (.npz)")
     ap.add_argument("--load-net", default="", help="--workload surrogate: use this network instead of training")
     ap.add_argument("--train-side", type=int, default=256)
+    ap.add_argument("--resort", type=int, default=None,
+                    help="steps between re-deals of the live drops (-1 automatic, 0 never); default: automatic")
     ap.add_argument("--autotune", action="store_true",
                     help="run the launch-shape autotuner first and bench the fastest shape")
     ap.add_argument("--whole-cycles", type=int, default=500,

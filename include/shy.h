@@ -191,6 +191,15 @@ int shy_world_set_launch(shy_world* w, int grid, int order);
  * where they fit without lowering occupancy, 0 always in global memory.
  * Results do not depend on either setting. */
 int shy_world_set_block(shy_world* w, int threads, int smem_slots);
+/* Re-deal of a batched cycle's drops: every `steps` lock-step steps, the
+ * drops still descending are sorted by the cell they are in and dealt to
+ * the CTAs in runs again, so that drops touching the same cells run
+ * together while the drops drift from their spawn cells, and retired drops
+ * leave the CTAs' slot ranges.  Only with drop slots in global memory.
+ * -1 (the default): every 16 steps when the slots are in spawn-cell order
+ * (see shy_world_set_launch), else never; 0 never; 1-4096 that many steps.
+ * Results do not depend on it. */
+int shy_world_set_resort(shy_world* w, int steps);
 /* Batched cycles per CUDA graph: with k > 0, shy_erode / shy_batch_erode run
  * each k cycles as one graph (the lock-step and end-of-cycle launches of k
  * cycles), captured on the world's stream on first use and again whenever

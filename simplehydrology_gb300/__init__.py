@@ -111,6 +111,12 @@ class _Handle:
         drop slots may live in shared memory (1) or always in global (0)."""
         check(lib().shy_world_set_block(self._w, threads, smem_slots))
 
+    def set_resort(self, steps: int = -1):
+        """Every `steps` lock-step steps, sort the live drops by their cell and
+        deal them to the CTAs again (slots in global memory only; -1: every
+        16 steps with spawn-ordered slots, else never; 0 never)."""
+        check(lib().shy_world_set_resort(self._w, steps))
+
     def set_graph(self, cycles_per_graph: int = 0):
         """Run batched cycles as CUDA graphs of this many cycles (0: none)."""
         check(lib().shy_world_set_graph(self._w, cycles_per_graph))

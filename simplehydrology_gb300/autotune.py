@@ -9,12 +9,15 @@ The batched kernel's launch shape changes its speed, never its results:
 * whether a cycle's drops are dealt to the CTAs in spawn-cell order;
 * whether a CTA's drop slots may live in shared memory (when they fit) or
   always in global memory;
-* how many cycles run as one CUDA graph.
+* how many cycles run as one CUDA graph;
+* how often the live drops are re-dealt to the CTAs, sorted by their cell
+  (slots in global memory only).
 
 `autotune` tries candidate shapes on copies of a world's current state
 (through a checkpoint file), times each over `cycles` cycles with CUDA
 events on the copy's stream, and applies the fastest to the world; then,
-with that shape, it times each cycles-per-graph setting the same way.
+with that shape, it times each cycles-per-graph setting the same way, and
+with both, each re-deal interval.
 """
 from __future__ import annotations
 
@@ -26,6 +29,7 @@ from . import Batch, World, load
 BLOCKS = (64, 128, 256)
 ORDERS = (-1, 0, 1)
 GRAPHS = (0, 1, 4, 16)  # cycles per CUDA graph (0: launched one by one)
+RESORTS = (-1, 0, 4, 64)  # steps between re-deals (-1: the library's default)
 
 
 def sm_count(device: int | None = None) -> int:
@@ -63,7 +67,7 @@ def apply(world, shape):
     world.set_block(block, smem)
 
 
-def _time(path, shape, graph, drops, cycles, warm):
+def _time(path, shape, graph, drops, cycles, warm, resort=-1):
     """Seconds per cycle of `cycles` cycles on a copy of the checkpoint, after
     `warm` untimed cycles (which also capture any graph)."""
     import torch
@@ -71,6 +75,7 @@ def _time(path, shape, graph, drops, cycles, warm):
     try:
         apply(w, shape)
         w.set_graph(graph)
+        w.set_resort(resort)
 
         def erode(n):
             if isinstance(w, Batch):
@@ -92,14 +97,16 @@ def _time(path, shape, graph, drops, cycles, warm):
 
 
 def autotune(world, drops: int | None = None, cycles: int = 3, shapes=None, sms: int | None = None,
-             graphs=GRAPHS):
+             graphs=GRAPHS, resorts=RESORTS):
     """Time `cycles` batched cycles (at least 3) for each launch shape on a
     copy of `world`'s state and apply the fastest shape to `world`; then time
     each cycles-per-graph setting in `graphs` with that shape (over at least
-    the largest setting's cycles) and apply the fastest.  `drops` is the drops
-    per cycle for a single-terrain World (a Batch keeps its own).  Returns
-    (best_shape, {shape: seconds per cycle}); the graph choice and its
-    timings are in the attribute `autotune.last_graphs`."""
+    the largest setting's cycles) and apply the fastest; then each re-deal
+    interval in `resorts` with both, and apply the fastest.  `drops` is the
+    drops per cycle for a single-terrain World (a Batch keeps its own).
+    Returns (best_shape, {shape: seconds per cycle}); the graph choice and
+    its timings are in the attribute `autotune.last_graphs`, the re-deal
+    choice and its timings in `autotune.last_resorts`."""
     if isinstance(world, World) and drops is None:
         raise ValueError("drops per cycle is needed for a World")
     cycles = max(3, int(cycles))
@@ -107,7 +114,7 @@ def autotune(world, drops: int | None = None, cycles: int = 3, shapes=None, sms:
     shapes = [_full(s) for s in shapes]
     fd, path = tempfile.mkstemp(suffix=".ckpt")
     os.close(fd)
-    times, gtimes = {}, {}
+    times, gtimes, rtimes = {}, {}, {}
     try:
         world.save(path)
         for shape in shapes:
@@ -116,13 +123,19 @@ def autotune(world, drops: int | None = None, cycles: int = 3, shapes=None, sms:
         gc = max([cycles] + [int(g) for g in graphs])
         for g in graphs:
             gtimes[int(g)] = _time(path, best, int(g), drops, gc, max(1, int(g)))
+        graph = min(gtimes, key=gtimes.get) if gtimes else 0
+        for r in resorts:
+            rtimes[int(r)] = _time(path, best, graph, drops, gc, max(1, graph), int(r))
     finally:
         os.remove(path)
     apply(world, best)
-    graph = min(gtimes, key=gtimes.get) if gtimes else 0
     world.set_graph(graph)
+    resort = min(rtimes, key=rtimes.get) if rtimes else -1
+    world.set_resort(resort)
     autotune.last_graphs = (graph, gtimes)
+    autotune.last_resorts = (resort, rtimes)
     return best, times
 
 
 autotune.last_graphs = (0, {})
+autotune.last_resorts = (-1, {})

@@ -18,6 +18,11 @@ namespace shy {
 // terrains packed back to back in every per-cell array; cell (x, y) of
 // terrain t is element cell_base + x * ny + y (x-major like the reference's
 // math::flatten, source/include/math.h:11-14).
+// Buckets of cells the batched mode's re-deal sorts live drops into, at
+// most; and its default steps between re-deals.
+const int kResortBuckets = 8192;
+const int kResortSteps = 16;
+
 struct Terrain {
   long long cell_base;
   long long arr_base;  // first word of this terrain's arrivals bitmap
@@ -161,6 +166,15 @@ struct shy_world {
   int* dkey = nullptr;        // spawn-order scratch: run of each drop's spawn cell
   int* drank = nullptr;       //   and its place within the run
   int* dhist = nullptr;       //   runs' counts, then offsets (at most 65,536)
+  // second set of the slots' persistent fields (the re-deal moves the live
+  // drops between the two sets), and its bucket counts (kResortBuckets)
+  float2* dpos2 = nullptr;
+  float2* dspd2 = nullptr;
+  float2* dvs2 = nullptr;
+  int* dage2 = nullptr;
+  long long* dgain2 = nullptr;
+  int* dterr2 = nullptr;
+  int* dresort = nullptr;
   float* stage = nullptr;             // cells floats, third staging buffer of the state calls
   float* feed = nullptr;              // staging buffer of shy_feed for host output
   size_t feed_len = 0;
@@ -188,6 +202,8 @@ struct shy_world {
   int batch_order = -1;       // slots in spawn-cell order: -1 when the cell state outgrows L2, 0 never, 1 always
   int batch_block = 256;      // threads per CTA of the lock-step kernel: 64, 128 or 256
   int batch_smem = 1;         // 0: drop slots in global memory even where shared memory would hold them
+  int batch_resort = -1;      // steps between re-deals of the live drops (-1: kResortSteps with
+                              // spawn-ordered slots in global memory, else never; 0 never)
   int graph_cycles = 0;       // batched cycles per CUDA graph (0: launched one by one)
   cudaGraphExec_t gexec = nullptr;  // the captured cycles
   unsigned long long graph_key = 0; // what they were captured with (launch_key)

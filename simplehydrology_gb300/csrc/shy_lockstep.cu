@@ -35,6 +35,12 @@
 // cell and dealt to the CTAs in runs of consecutive drops, round-robin: each
 // run is a compact stretch of the maps, and every CTA samples stretches from
 // the whole map, so live drops stay balanced across CTAs as drops retire.
+// Drops drift from their spawn cells within tens of steps, so every `resort`
+// steps (slots in global memory only) the live drops are sorted again, by
+// the cell they are in, and dealt to the CTAs in runs once more: the drops
+// that touch the same cells stay in the same runs, which run at about the
+// same time, and the retired drops drop out of the slot ranges.  A drop's
+// slot carries its whole state, so this changes no result.
 // Heights live in 32.32 fixed point for the whole cycle (the float map is
 // rewritten at its end), so every update is an integer addition.
 // Integer sums make every result independent of thread timing: the same
@@ -257,6 +263,17 @@ struct LockArgs {
   unsigned long long* arr;  // arrivals bitmaps, one per step parity, arr_words words each
   long long arr_words;
   const int* order;  // drops sorted by spawn cell (dealt to the CTAs in runs), or null: slot = drop
+  // second set of the slots' persistent fields, for the re-deal (which
+  // moves the live drops from one set to the other)
+  float2* pos2;
+  float2* spd2;
+  float2* vs2;
+  int* age2;
+  long long* gain2;
+  int* terr2;
+  int* rhist;    // re-deal: live drops per bucket of cells, then offsets; zero between re-deals
+  int rshift;    //   bucket = cell >> rshift (at most kResortBuckets buckets)
+  int resort;    //   steps between re-deals (0: never; only with slots in global memory)
   int smem_slots;   // 1: drop slots and queue live in dynamic shared memory
   int smem_allowed;  // 0: keep the slots in global memory even when they would fit
   shy_params P;
@@ -280,6 +297,23 @@ struct Slots {
   SteepCell* steep;
 };
 
+// The slots from `lo` on in global memory, persistent fields from set `buf`
+// (0: the first set, 1: the second).
+__device__ __forceinline__ Slots slots_global(const LockArgs& a, int buf, long long lo) {
+  Slots S;
+  S.steep = a.steep + lo;
+  S.pos = (buf ? a.pos2 : a.pos) + lo;
+  S.spd = (buf ? a.spd2 : a.spd) + lo;
+  S.vs = (buf ? a.vs2 : a.vs) + lo;
+  S.gain = (buf ? a.gain2 : a.gain) + lo;
+  S.own = a.own + lo;
+  S.cell = a.cell + lo;
+  S.ctr = a.ctr + lo;
+  S.age = (buf ? a.age2 : a.age) + lo;
+  S.terr = (buf ? a.terr2 : a.terr) + lo;
+  return S;
+}
+
 __device__ __forceinline__ Slots slots_of(const LockArgs& a, unsigned char* smem, long long lo, int cap) {
   Slots S;
   if (a.smem_slots) {
@@ -296,16 +330,7 @@ __device__ __forceinline__ Slots slots_of(const LockArgs& a, unsigned char* smem
     S.age = reinterpret_cast<int*>(p); p += 4 * cap;
     S.terr = reinterpret_cast<int*>(p);
   } else {
-    S.steep = a.steep + lo;
-    S.pos = a.pos + lo;
-    S.spd = a.spd + lo;
-    S.vs = a.vs + lo;
-    S.gain = a.gain + lo;
-    S.own = a.own + lo;
-    S.cell = a.cell + lo;
-    S.ctr = a.ctr + lo;
-    S.age = a.age + lo;
-    S.terr = a.terr + lo;
+    S = slots_global(a, 0, lo);
   }
   return S;
 }
@@ -494,8 +519,154 @@ __device__ __forceinline__ void steep_apply(const SteepCell& q, const Terrain& T
   if (q.u.out.dc != 0) add_i64(&cq[c2].hq, q.u.out.dc);
 }
 
-// 128 registers: two 256-thread CTAs per SM
+// Exclusive prefix sum of the kResortBuckets counts h[] in place (16-byte
+// aligned), by one CTA of kBlock threads: each thread sums a stretch of
+// 4-int vectors (loaded four at a time, so that a stretch costs few round
+// trips), the CTA scans the stretch sums, each thread writes its stretch's
+// offsets.
 template <int kBlock>
+__device__ void cta_exclusive_scan(int* h) {
+  static_assert(kResortBuckets % (16 * kBlock) == 0, "stretches of whole groups of four vectors");
+  constexpr int kVec = kResortBuckets / 4 / kBlock;  // vectors per thread
+  __shared__ int s_w[kBlock / 32];
+  int4* v = reinterpret_cast<int4*>(h) + threadIdx.x * kVec;
+  int sum = 0;
+  for (int g = 0; g < kVec; g += 4) {
+    int4 q[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) q[u] = v[g + u];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) sum += q[u].x + q[u].y + q[u].z + q[u].w;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = sum;  // inclusive within the warp
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_w[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < kBlock / 32 ? s_w[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kBlock / 32) s_w[lane] = w;
+  }
+  __syncthreads();
+  int run = x - sum + (warp ? s_w[warp - 1] : 0);
+  for (int g = 0; g < kVec; g += 4) {
+    int4 q[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) q[u] = v[g + u];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      int4 o;
+      o.x = run; run += q[u].x;
+      o.y = run; run += q[u].y;
+      o.z = run; run += q[u].z;
+      o.w = run; run += q[u].w;
+      v[g + u] = o;
+    }
+  }
+}
+
+// The cell a live drop (inside its terrain) is in.
+__device__ __forceinline__ long long drop_cell(const Terrain& T, float2 p) {
+  return T.cell_base + (long long)(int)p.x * T.ny + (int)p.y;
+}
+
+// Re-deal between steps: the `live` drops still descending, sorted by the
+// bucket of cells they are in, go to the CTAs in runs (run k of CTA b is run
+// k * grid + b of the sorted drops, as at spawn), from one set of the slots'
+// persistent fields to the other.  Three grid barriers: after the bucket
+// counts, after CTA 0's prefix sum, after the moves.  Then each CTA clears
+// its share of the counts and returns its new range, in the other set.  A
+// drop's rank within its bucket is whatever the atomics give: no result
+// depends on which slot a drop is in.  The CTA's slots pass as scalars
+// (first slot `lo`, `nd` of them, set `buf`), so that the caller's slot
+// pointers stay in registers rather than on the stack.
+struct Redealt {
+  long long lo;
+  int nd;
+  bool ok;
+};
+template <int kBlock>
+__device__ __noinline__ Redealt redeal(const LockArgs& a, const Terrain* TT, long long lo, int nd, int buf,
+                                       unsigned passed, long long live) {
+  Redealt r;
+  r.lo = lo;
+  r.nd = nd;
+  r.ok = false;
+  const Slots S = slots_global(a, buf, lo);
+  // each pass loads the next slot's fields before its own atomic, so that a
+  // thread's slots cost overlapping round trips
+  {
+    int ag_n = -1, ti_n = 0;
+    float2 p_n = make_float2(0.0f, 0.0f);
+    if ((int)threadIdx.x < nd) {
+      ag_n = S.age[threadIdx.x]; ti_n = S.terr[threadIdx.x]; p_n = S.pos[threadIdx.x];
+    }
+    for (int j = threadIdx.x; j < nd; j += kBlock) {
+      const int ag = ag_n, ti = ti_n;
+      const float2 p = p_n;
+      if (j + kBlock < nd) {
+        ag_n = S.age[j + kBlock]; ti_n = S.terr[j + kBlock]; p_n = S.pos[j + kBlock];
+      }
+      if (ag >= 0) atomicAdd(&a.rhist[drop_cell(TT[ti], p) >> a.rshift], 1);
+    }
+  }
+  if (!grid_barrier(a.bar, passed, nullptr)) return r;
+  if (blockIdx.x == 0) cta_exclusive_scan<kBlock>(a.rhist);
+  if (!grid_barrier(a.bar, passed, nullptr)) return r;
+  const long long R = order_run(live, gridDim.x);
+  const Slots D = slots_global(a, buf ^ 1, 0);
+  int ag_n = -1, ti_n = 0;
+  float2 p_n = make_float2(0.0f, 0.0f), s_n = p_n, v_n = p_n;
+  long long g_n = 0;
+  if ((int)threadIdx.x < nd) {
+    const int j = threadIdx.x;
+    ag_n = S.age[j]; ti_n = S.terr[j]; p_n = S.pos[j]; s_n = S.spd[j]; v_n = S.vs[j]; g_n = S.gain[j];
+  }
+  for (int j = threadIdx.x; j < nd; j += kBlock) {
+    const int ag = ag_n, ti = ti_n;
+    const float2 p = p_n, sp = s_n, vs = v_n;
+    const long long gn = g_n;
+    if (j + kBlock < nd) {
+      const int jn = j + kBlock;
+      ag_n = S.age[jn]; ti_n = S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; v_n = S.vs[jn]; g_n = S.gain[jn];
+    }
+    if (ag < 0) continue;
+    const long long k = atomicAdd(&a.rhist[drop_cell(TT[ti], p) >> a.rshift], 1);
+    if (k >= live) {  // more drops than the live count: never expected
+      atomicCAS(&a.bar->error, 0, SHY_ERR_STATE);
+      continue;
+    }
+    const long long kr = k / R;
+    const long long d = slot_range(live, gridDim.x, kr % gridDim.x, true).lo + (kr / gridDim.x) * R + k % R;
+    D.pos[d] = p;
+    D.spd[d] = sp;
+    D.vs[d] = vs;
+    D.age[d] = ag;
+    D.gain[d] = gn;
+    D.terr[d] = ti;
+  }
+  if (!grid_barrier(a.bar, passed, nullptr)) return r;
+  const SlotRange sr = slot_range(live, gridDim.x, blockIdx.x, true);
+  r.lo = sr.lo;
+  r.nd = sr.nd;
+  r.ok = true;
+  const long long w0 = (long long)blockIdx.x * kResortBuckets / gridDim.x;
+  const long long w1 = (long long)(blockIdx.x + 1) * kResortBuckets / gridDim.x;
+  for (long long i = w0 + threadIdx.x; i < w1; i += kBlock) a.rhist[i] = 0;
+  return r;
+}
+
+// 128 registers: two 256-thread CTAs per SM.  kRedeal: the instantiation
+// with the re-deal (slots in global memory, a.resort > 0); the other has no
+// trace of it, so that its slot pointers stay fixed for the whole cycle.
+template <int kBlock, bool kRedeal>
 __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ Terrain sT[kSmemTerrains];
@@ -514,10 +685,13 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
 
   // this CTA's drop slots: [lo, lo + nd), storage for `cap`
   const SlotRange sr = slot_range(a.total_drops, gridDim.x, blockIdx.x, a.order != nullptr);
-  const long long lo = sr.lo;
-  const int nd = sr.nd, cap = sr.cap;
-  const Slots S = slots_of(a, s_dyn, lo, cap);
+  long long lo = sr.lo;
+  int nd = sr.nd;
+  const int cap = sr.cap;
+  Slots S = slots_of(a, s_dyn, lo, cap);
   const long long run = order_run(a.total_drops, gridDim.x);
+  int buf = 0;  // which set of persistent slot fields the CTA's slots are in
+  const bool redeals = kRedeal && a.resort > 0 && !a.smem_slots;
 
   const shy_params& P = a.P;
   const unsigned long long cycle = a.bar->cycle;
@@ -547,6 +721,11 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     const long long w0 = (long long)blockIdx.x * (2 * a.arr_words) / gridDim.x;
     const long long w1 = (long long)(blockIdx.x + 1) * (2 * a.arr_words) / gridDim.x;
     for (long long i = w0 + threadIdx.x; i < w1; i += blockDim.x) a.arr[i] = 0ull;
+  }
+  if (redeals) {  // and the re-deal's bucket counts
+    const long long w0 = (long long)blockIdx.x * kResortBuckets / gridDim.x;
+    const long long w1 = (long long)(blockIdx.x + 1) * kResortBuckets / gridDim.x;
+    for (long long i = w0 + threadIdx.x; i < w1; i += blockDim.x) a.rhist[i] = 0;
   }
 
   // spawn (source/world.h:64-74)
@@ -849,6 +1028,20 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       ok = false;
       break;
     }
+    // every CTA sees the same step and live count, so all take the same
+    // barriers
+    if (redeals && (step + 1) % a.resort == 0 && s_live != 0) {
+      const Redealt r = redeal<kBlock>(a, TT, lo, nd, buf, passed, (long long)s_live);
+      passed += 3;
+      if (!r.ok) {
+        ok = false;
+        break;
+      }
+      lo = r.lo;
+      nd = r.nd;
+      buf ^= 1;
+      S = slots_global(a, buf, lo);
+    }
   }
   lap(5);
 
@@ -1030,6 +1223,13 @@ int order_shift(long long cells) {
   return shift;
 }
 
+// the bucket shift of the re-deal: at most kResortBuckets buckets of cells
+int resort_shift(long long cells) {
+  int shift = 0;
+  while (((cells - 1) >> shift) + 1 > kResortBuckets) ++shift;
+  return shift;
+}
+
 cudaError_t launch_spawn_order(shy_world* w, int total) {
   const int shift = order_shift(w->cells);
   const int nb = (int)((w->cells - 1) >> shift) + 1;
@@ -1051,7 +1251,7 @@ namespace {
 // drops per CTA); each CTA's drop slots go to shared memory when they fit
 // without lowering that occupancy (and the world allows it), else to the
 // global arrays in `a`.
-// What a launch of lockstep_kernel<kBlock> needs to know about the device,
+// What a launch of lockstep_kernel<kBlock, kRedeal> needs to know about the device,
 // queried once per device and CTA size (and per dynamic shared-memory size
 // for the occupancy with slots in shared memory) rather than every cycle.
 struct LaunchFacts {
@@ -1066,7 +1266,7 @@ struct LaunchFacts {
 const int kMaxDevices = 64;
 std::mutex g_facts_mu;
 
-template <int kBlock>
+template <int kBlock, bool kRedeal>
 cudaError_t launch_facts(LaunchFacts** out) {
   static LaunchFacts facts[kMaxDevices];
   int dev = 0;
@@ -1077,9 +1277,9 @@ cudaError_t launch_facts(LaunchFacts** out) {
   if (!f.valid) {
     if ((e = cudaDeviceGetAttribute(&f.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
     cudaFuncAttributes fa;
-    if ((e = cudaFuncGetAttributes(&fa, lockstep_kernel<kBlock>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&fa, lockstep_kernel<kBlock, kRedeal>)) != cudaSuccess) return e;
     f.static_smem = (long long)fa.sharedSizeBytes;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f.per0, lockstep_kernel<kBlock>, kBlock, 0)) !=
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f.per0, lockstep_kernel<kBlock, kRedeal>, kBlock, 0)) !=
         cudaSuccess)
       return e;
     f.valid = true;
@@ -1098,7 +1298,7 @@ cudaError_t launch_lockstep_n(LockArgs& a, int sm_count, int grid_hint, cudaStre
   std::lock_guard<std::mutex> lock(g_facts_mu);
   LaunchFacts* f = nullptr;
   cudaError_t e;
-  if ((e = launch_facts<kBlock>(&f)) != cudaSuccess) return e;
+  if ((e = launch_facts<kBlock, false>(&f)) != cudaSuccess) return e;
   if (f->per0 < 1) return cudaErrorLaunchOutOfResources;
   const long long max_dyn = (long long)f->optin - f->static_smem;
   long long want = ((long long)a.total_drops + 31) / 32;
@@ -1112,14 +1312,16 @@ cudaError_t launch_lockstep_n(LockArgs& a, int sm_count, int grid_hint, cudaStre
   a.smem_slots = 0;
   if (b <= max_dyn && a.smem_allowed) {
     if (b > 48 * 1024 && b > f->smem_set) {
-      if ((e = cudaFuncSetAttribute(lockstep_kernel<kBlock>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b)) !=
+      if ((e = cudaFuncSetAttribute(lockstep_kernel<kBlock, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)b)) !=
           cudaSuccess)
         return e;
       f->smem_set = b;
     }
     if (b != f->last_b) {
       int per = 0;
-      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lockstep_kernel<kBlock>, kBlock, (size_t)b)) !=
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lockstep_kernel<kBlock, false>, kBlock,
+                                                             (size_t)b)) !=
           cudaSuccess)
         return e;
       f->last_b = b;
@@ -1131,7 +1333,18 @@ cudaError_t launch_lockstep_n(LockArgs& a, int sm_count, int grid_hint, cudaStre
     }
   }
   void* args[] = {&a};
-  return cudaLaunchCooperativeKernel((const void*)lockstep_kernel<kBlock>, dim3(grid), dim3(kBlock), args, bytes,
+  if (!a.smem_slots && a.resort > 0) {
+    // slots in global memory with re-deals: the other instantiation, with
+    // its own residency (every CTA of a cooperative launch must fit at once)
+    LaunchFacts* fr = nullptr;
+    if ((e = launch_facts<kBlock, true>(&fr)) != cudaSuccess) return e;
+    if (fr->per0 < 1) return cudaErrorLaunchOutOfResources;
+    const long long gr = (long long)fr->per0 * sm_count < want ? (long long)fr->per0 * sm_count : want;
+    return cudaLaunchCooperativeKernel((const void*)lockstep_kernel<kBlock, true>, dim3((int)gr), dim3(kBlock),
+                                       args, 0, stream);
+  }
+  a.resort = 0;
+  return cudaLaunchCooperativeKernel((const void*)lockstep_kernel<kBlock, false>, dim3(grid), dim3(kBlock), args, bytes,
                                      stream);
 }
 
@@ -1178,6 +1391,15 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   const long long state_bytes = w->cells * (long long)(sizeof(CellQ) + sizeof(Tracks) + sizeof(float4) + 4);
   const bool ordered = w->batch_order < 0 ? state_bytes > w->l2_bytes : w->batch_order != 0;
   a.order = ordered ? w->dorder : nullptr;
+  a.pos2 = w->dpos2;
+  a.spd2 = w->dspd2;
+  a.vs2 = w->dvs2;
+  a.age2 = w->dage2;
+  a.gain2 = w->dgain2;
+  a.terr2 = w->dterr2;
+  a.rhist = w->dresort;
+  a.rshift = resort_shift(w->cells);
+  a.resort = w->batch_resort < 0 ? (ordered ? kResortSteps : 0) : w->batch_resort;
   a.smem_slots = 0;
   a.P = w->P;
   a.st = w->stats;
@@ -1245,6 +1467,11 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.arr = b.arr;
   a.arr_words = b.arr_words;
   a.order = nullptr;
+  a.pos2 = a.spd2 = a.vs2 = nullptr;
+  a.age2 = a.terr2 = a.rhist = nullptr;
+  a.gain2 = nullptr;
+  a.rshift = 0;
+  a.resort = 0;  // no second set of slots in the caller's buffers
   a.smem_slots = 0;
   a.P = b.P;
   a.st = b.st;

@@ -100,7 +100,7 @@ void free_world(shy_world* w) {
                   w->dterr, w->dcell, w->dctr, w->dterrains, w->stats, w->bar, w->ddrop,
                   w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down,
                   w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed, w->crand, w->plants, w->stage, w->dorder, w->dkey, w->drank, w->dhist,
-                  w->dsteep};
+                  w->dsteep, w->dpos2, w->dspd2, w->dvs2, w->dage2, w->dgain2, w->dterr2, w->dresort};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& p : w->timing.pending) {
@@ -115,7 +115,8 @@ void free_world(shy_world* w) {
 int alloc_drop_slots(shy_world* w, int n) {
   if (n <= w->max_drops) return SHY_OK;
   void* ptrs[] = {w->dpos, w->dspd, w->dvs, w->dage, w->dgain, w->dterr, w->dcell, w->dctr, w->down,
-                  w->dsteep, w->dorder, w->dkey, w->drank};
+                  w->dsteep, w->dorder, w->dkey, w->drank, w->dpos2, w->dspd2, w->dvs2, w->dage2, w->dgain2,
+                  w->dterr2};
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -125,6 +126,9 @@ int alloc_drop_slots(shy_world* w, int n) {
   w->dsteep = nullptr;
   w->dorder = w->dkey = w->drank = nullptr;
   w->dcell = w->dctr = nullptr;
+  w->dpos2 = w->dspd2 = w->dvs2 = nullptr;
+  w->dage2 = w->dterr2 = nullptr;
+  w->dgain2 = nullptr;
   w->max_drops = 0;
   SHY_CHECK_CUDA(dalloc(&w->dpos, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dspd, n), "allocate drop slots");
@@ -139,7 +143,14 @@ int alloc_drop_slots(shy_world* w, int n) {
   SHY_CHECK_CUDA(dalloc(&w->dorder, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dkey, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->drank, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->dpos2, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->dspd2, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->dvs2, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->dage2, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->dgain2, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->dterr2, n), "allocate drop slots");
   if (!w->dhist) SHY_CHECK_CUDA(dalloc(&w->dhist, 65536), "allocate drop slots");
+  if (!w->dresort) SHY_CHECK_CUDA(dalloc(&w->dresort, shy::kResortBuckets), "allocate drop slots");
   w->max_drops = n;
   return SHY_OK;
 }
@@ -716,6 +727,17 @@ int shy_world_set_block(shy_world* w, int threads, int smem_slots) {
   return SHY_OK;
 }
 
+int shy_world_set_resort(shy_world* w, int steps) {
+  int rc = check_world(w);
+  if (rc) return rc;
+  if (steps < -1 || steps > 4096) {
+    set_error("shy_world_set_resort: steps must be -1 (automatic), 0 (never) or lie in [1, 4096]");
+    return SHY_ERR_INVALID_ARG;
+  }
+  w->batch_resort = steps;
+  return SHY_OK;
+}
+
 int shy_world_set_graph(shy_world* w, int cycles_per_graph) {
   int rc = check_world(w);
   if (rc) return rc;
@@ -863,11 +885,13 @@ unsigned long long launch_key(const shy_world* w) {
   };
   mix(&w->P, sizeof(w->P));
   for (const auto& T : w->terrains) mix(&T, sizeof(T));
-  const int shape[6] = {w->batch_grid, w->batch_order, w->batch_block, w->batch_smem, w->graph_cycles, w->sm_count};
+  const int shape[7] = {w->batch_grid, w->batch_order, w->batch_block, w->batch_smem, w->graph_cycles, w->sm_count,
+                        w->batch_resort};
   mix(shape, sizeof(shape));
   const void* ptrs[] = {w->h, w->cq, w->rec, w->voltab, w->trk, w->track_f, w->dpos, w->dspd, w->dvs, w->dage,
                         w->dgain, w->down, w->dterr, w->dcell, w->dctr, w->dsteep, w->arr, w->dorder, w->dkey,
-                        w->drank, w->dhist, w->dterrains, w->stats, w->bar, w->relax, w->hq_relax};
+                        w->drank, w->dhist, w->dterrains, w->stats, w->bar, w->relax, w->hq_relax,
+                        w->dpos2, w->dspd2, w->dvs2, w->dage2, w->dgain2, w->dterr2, w->dresort};
   mix(ptrs, sizeof(ptrs));
   return h;
 }

@@ -267,6 +267,66 @@ def test_every_launch_shape_gives_the_oracle_bits(shy, po):
         w.close()
 
 
+@pytest.mark.parametrize("block,grid,order,resort", [(256, 0, 1, 1), (256, 0, 1, 2), (128, 5, 1, 3),
+                                                     (64, 0, 0, 7), (256, 3, -1, 16), (64, 7, 1, 1)])
+def test_redeal_gives_the_oracle_bits(shy, po, block, grid, order, resort):
+    """Live drops re-sorted by their cell and dealt to the CTAs again every
+    `resort` steps (slots in global memory), after spawn in drop or
+    spawn-cell order, with one or several slots per thread: the oracle's
+    bits, on one terrain and on a batch of three (the sort key crosses
+    terrain boundaries)."""
+    nx, ny, drops = 96, 80, 3000
+    H = po.value_noise(nx, ny, 21)
+    m = po.Maps(nx, ny, height=H)
+    acc = po.erode_batched(m, 3, 0, drops, 2)
+    w = shy.World(nx, ny, seed=3)
+    w.set_field("height", H)
+    w.set_launch(grid, order)
+    w.set_block(block, 0)
+    w.set_resort(resort)
+    w.erode(drops, 2)
+    compare_all(w.get_field, m, po, f"re-deal every {resort}")
+    assert w.stats().drop_steps == acc.steps
+    w.close()
+
+    sizes = [(64, 48), (40, 72), (56, 56)]
+    seeds = [11, 12, 13]
+    b = shy.Batch(sizes, [900, 1500, 700], seeds)
+    hs = [po.value_noise(x, y, 30 + t) for t, (x, y) in enumerate(sizes)]
+    for t, h in enumerate(hs):
+        b.set_field(t, "height", h)
+    b.set_launch(grid, order)
+    b.set_block(block, 0)
+    b.set_resort(resort)
+    b.erode(2)
+    for t, ((x, y), h) in enumerate(zip(sizes, hs)):
+        mt = po.Maps(x, y, height=h)
+        po.erode_batched(mt, seeds[t], 0, [900, 1500, 700][t], 2)
+        compare_all(lambda f: b.get_field(t, f), mt, po, f"batch terrain {t}, re-deal every {resort}")
+    b.close()
+
+
+def test_redeal_in_cuda_graphs_gives_the_oracle_bits(shy, po):
+    """The re-deal interval is part of what a captured graph is keyed on:
+    changing it between calls captures again, and the bits stay the
+    oracle's."""
+    nx, ny = 96, 80
+    H = po.value_noise(nx, ny, 21)
+    w = shy.World(nx, ny, seed=3)
+    w.set_field("height", H)
+    w.set_launch(0, 1)
+    w.set_block(256, 0)
+    w.set_graph(2)
+    w.set_resort(4)
+    w.erode(2000, 2)
+    w.set_resort(0)
+    w.erode(2000, 2)
+    m = po.Maps(nx, ny, height=H)
+    po.erode_batched(m, 3, 0, 2000, 4)
+    compare_all(w.get_field, m, po, "graphs with re-deals")
+    w.close()
+
+
 def test_autotune_applies_a_shape_and_keeps_results(shy, po):
     from simplehydrology_gb300 import autotune
     nx, ny, drops = 96, 80, 2000
@@ -278,6 +338,8 @@ def test_autotune_applies_a_shape_and_keeps_results(shy, po):
     assert all(t > 0 for t in times.values())
     graph, gtimes = autotune.autotune.last_graphs
     assert graph in gtimes and sorted(gtimes) == sorted(autotune.GRAPHS)
+    resort, rtimes = autotune.autotune.last_resorts
+    assert resort in rtimes and sorted(rtimes) == sorted(autotune.RESORTS)
     w.erode(drops, 2)  # with the chosen shape
     m = po.Maps(nx, ny, height=H)
     po.erode_batched(m, 3, 0, drops, 2)
