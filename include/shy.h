@@ -173,7 +173,8 @@ int shy_world_timing(shy_world* w, shy_timing* out);
 /* Where the batched kernel's time goes, as seen by its first CTA, summed
  * over all cycles since creation: phase_ms[6] = {descend phase, barrier
  * wait, cascade scan phase, barrier wait, settle phase (steep cascades,
- * height updates, retirements), barrier wait plus spawn and exit};
+ * height updates, retirements), barrier wait plus spawn, re-deals (see
+ * shy_world_set_resort) and exit};
  * *iterations = lock-step steps run. */
 int shy_world_lockstep_profile(shy_world* w, double* phase_ms, uint64_t* iterations);
 /* Launch shape of the batched kernel: at most `grid` CTAs (0, the default:

@@ -120,12 +120,16 @@ def autotune(world, drops: int | None = None, cycles: int = 3, shapes=None, sms:
         for shape in shapes:
             times[shape] = _time(path, shape, 0, drops, cycles, 1)
         best = min(times, key=times.get)
+        # every setting warms up over the same cycles (enough to capture the
+        # largest graph) and is timed over the same later ones: later cycles
+        # carry fewer drop-steps, so unequal windows would favour one setting
         gc = max([cycles] + [int(g) for g in graphs])
+        gw = max([1] + [int(g) for g in graphs])
         for g in graphs:
-            gtimes[int(g)] = _time(path, best, int(g), drops, gc, max(1, int(g)))
+            gtimes[int(g)] = _time(path, best, int(g), drops, gc, gw)
         graph = min(gtimes, key=gtimes.get) if gtimes else 0
         for r in resorts:
-            rtimes[int(r)] = _time(path, best, graph, drops, gc, max(1, graph), int(r))
+            rtimes[int(r)] = _time(path, best, graph, drops, gc, gw, int(r))
     finally:
         os.remove(path)
     apply(world, best)
