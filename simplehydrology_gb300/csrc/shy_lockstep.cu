@@ -770,19 +770,26 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     // Each iteration loads the next slot's state before working on its own,
     // so that with several slots per thread (slots in global memory) their
     // loads overlap the work instead of preceding it.
+    // With re-deals (several slots per thread, in runs of cells), the three
+    // phases sweep the slots in alternating directions, so that each phase
+    // starts on the cells the one before ended on, while L2 still holds them:
+    // descend forwards on even steps, scan backwards, settle forwards, and
+    // the reverse on odd steps.  Slot order changes no result.
+    const bool rev_d = redeals && (step & 1);
     int ag_n = 0, ti_n = 0;
     float2 p_n = make_float2(0.0f, 0.0f), s_n = p_n, v_n = p_n;
     long long gn_n = 0;
     if ((int)threadIdx.x < nd) {
-      const int j = threadIdx.x;
+      const int j = rev_d ? nd - 1 - (int)threadIdx.x : (int)threadIdx.x;
       ag_n = S.age[j]; ti_n = S.terr[j]; p_n = S.pos[j]; s_n = S.spd[j]; v_n = S.vs[j]; gn_n = S.gain[j];
     }
-    for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+      const int j = rev_d ? nd - 1 - i : i;
       const int ag = ag_n, ti = ti_n;
       float2 p = p_n, s = s_n, v = v_n;
       long long gn = gn_n;
-      if (j + (int)blockDim.x < nd) {
-        const int jn = j + blockDim.x;
+      if (i + (int)blockDim.x < nd) {
+        const int jn = rev_d ? nd - 1 - (i + (int)blockDim.x) : i + (int)blockDim.x;
         ag_n = S.age[jn]; ti_n = S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; v_n = S.vs[jn]; gn_n = S.gain[jn];
       }
       if (ag < 0) continue;
@@ -897,18 +904,21 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     // centre instead and is masked out.  The centre only changes through a
     // transfer, so without any excess to begin with the sequential loop moves
     // nothing and the cascade ends here.
+    const bool rev_s = redeals && !(step & 1);
     long long c2_n = -1;
     int ti_n2 = 0;
     if ((int)threadIdx.x < nd) {
-      c2_n = S.ctr[threadIdx.x];
-      ti_n2 = S.terr[threadIdx.x];
+      const int j = rev_s ? nd - 1 - (int)threadIdx.x : (int)threadIdx.x;
+      c2_n = S.ctr[j];
+      ti_n2 = S.terr[j];
     }
-    for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) {
       const long long c2 = c2_n;
       const int ti = ti_n2;
-      if (j + (int)blockDim.x < nd) {  // the next slot's claim, loaded ahead
-        c2_n = S.ctr[j + blockDim.x];
-        ti_n2 = S.terr[j + blockDim.x];
+      if (i + (int)blockDim.x < nd) {  // the next slot's claim, loaded ahead
+        const int jn = rev_s ? nd - 1 - (i + (int)blockDim.x) : i + (int)blockDim.x;
+        c2_n = S.ctr[jn];
+        ti_n2 = S.terr[jn];
       }
       if (c2 < 0) continue;
       const Terrain T = TT[ti];
@@ -994,17 +1004,19 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       for (long long i = w0 + threadIdx.x; i < w1; i += blockDim.x) other[i] = 0ull;
     }
     unsigned long long retired = 0;
+    const bool rev_t = redeals && (step & 1);
     int ag_f = -1;
     long long c_f = -1, own_f = 0;
     if ((int)threadIdx.x < nd) {
-      const int j = threadIdx.x;
+      const int j = rev_t ? nd - 1 - (int)threadIdx.x : (int)threadIdx.x;
       ag_f = S.age[j]; c_f = S.cell[j]; own_f = S.own[j];
     }
-    for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+      const int j = rev_t ? nd - 1 - i : i;
       const int ag = ag_f;
       const long long c = c_f, own = own_f;
-      if (j + (int)blockDim.x < nd) {  // the next slot, loaded ahead
-        const int jn = j + blockDim.x;
+      if (i + (int)blockDim.x < nd) {  // the next slot, loaded ahead
+        const int jn = rev_t ? nd - 1 - (i + (int)blockDim.x) : i + (int)blockDim.x;
         ag_f = S.age[jn]; c_f = S.cell[jn]; own_f = S.own[jn];
       }
       if (ag == -1) continue;
