@@ -78,9 +78,9 @@ def peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def profiled_traffic():
-    """Per-launch DRAM bytes of the lock-step kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "lockstep_kernel_1024.md")
+def profiled_traffic(name="lockstep_kernel_1024.md"):
+    """Per-launch DRAM bytes of the lock-step kernel from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
     try:
         with open(path) as f:
             for line in f:
@@ -378,9 +378,12 @@ def run_ours(args):
     bytes_per_launch = BYTES_PER_STEP * steps_total / n_launch
     achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
-    # the committed capture covers the default 1024^2 / 65,536-drop workload only
+    # the committed captures cover the default 1024^2 / 65,536-drop workload
+    # and the default large workload (its three timed cycles, re-deal on)
     plain_default = args.workload == "plain" and (args.map, args.drops) == (1024, 65536)
-    traffic = profiled_traffic() if plain_default else None
+    large_default = args.workload == "large" and (args.map, args.drops) == (NX, DROPS) and args.resort is None
+    traffic = (profiled_traffic() if plain_default else
+               profiled_traffic("lockstep_kernel_8192_dram.md") if large_default else None)
     l2 = shy.measure_l2(dev)
     kernel_s = tm.ms[0] / 1e3
     atomics = 4.0 * steps_total / kernel_s
