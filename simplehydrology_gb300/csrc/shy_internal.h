@@ -19,8 +19,10 @@ namespace shy {
 // terrain t is element cell_base + x * ny + y (x-major like the reference's
 // math::flatten, source/include/math.h:11-14).
 // Buckets of cells the batched mode's re-deal sorts live drops into, at
-// most; and its default steps between re-deals.
-const int kResortBuckets = 8192;
+// most (a launch uses about four per run of drops, in multiples of
+// kResortBucketStep); and its default steps between re-deals.
+const int kResortBuckets = 65536;
+const int kResortBucketStep = 4096;
 const int kResortSteps = 16;
 
 struct Terrain {

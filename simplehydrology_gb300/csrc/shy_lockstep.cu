@@ -82,11 +82,6 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
 __device__ __forceinline__ void red_release_add_u64(unsigned long long* p, unsigned long long v) {
   asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
@@ -272,7 +267,8 @@ struct LockArgs {
   long long* gain2;
   int* terr2;
   int* rhist;    // re-deal: live drops per bucket of cells, then offsets; zero between re-deals
-  int rshift;    //   bucket = cell >> rshift (at most kResortBuckets buckets)
+  int rshift;    //   bucket = cell >> rshift
+  int rbuckets;  //   buckets in use: a multiple of kResortBucketStep, at most kResortBuckets
   int resort;    //   steps between re-deals (0: never; only with slots in global memory)
   int smem_slots;   // 1: drop slots and queue live in dynamic shared memory
   int smem_allowed;  // 0: keep the slots in global memory even when they would fit
@@ -519,15 +515,15 @@ __device__ __forceinline__ void steep_apply(const SteepCell& q, const Terrain& T
   if (q.u.out.dc != 0) add_i64(&cq[c2].hq, q.u.out.dc);
 }
 
-// Exclusive prefix sum of the kResortBuckets counts h[] in place (16-byte
-// aligned), by one CTA of kBlock threads: each thread sums a stretch of
-// 4-int vectors (loaded four at a time, so that a stretch costs few round
-// trips), the CTA scans the stretch sums, each thread writes its stretch's
-// offsets.
+// Exclusive prefix sum of the n counts h[] in place (16-byte aligned; n a
+// multiple of kResortBucketStep), by one CTA of kBlock threads: each thread
+// sums a stretch of 4-int vectors (loaded four at a time, so that a stretch
+// costs few round trips), the CTA scans the stretch sums, each thread
+// writes its stretch's offsets.
 template <int kBlock>
-__device__ void cta_exclusive_scan(int* h) {
-  static_assert(kResortBuckets % (16 * kBlock) == 0, "stretches of whole groups of four vectors");
-  constexpr int kVec = kResortBuckets / 4 / kBlock;  // vectors per thread
+__device__ void cta_exclusive_scan(int* h, int n) {
+  static_assert(kResortBucketStep % (16 * kBlock) == 0, "stretches of whole groups of four vectors");
+  const int kVec = n / 4 / kBlock;  // vectors per thread, a multiple of 4
   __shared__ int s_w[kBlock / 32];
   int4* v = reinterpret_cast<int4*>(h) + threadIdx.x * kVec;
   int sum = 0;
@@ -618,7 +614,7 @@ __device__ __noinline__ Redealt redeal(const LockArgs& a, const Terrain* TT, lon
     }
   }
   if (!grid_barrier(a.bar, passed, nullptr)) return r;
-  if (blockIdx.x == 0) cta_exclusive_scan<kBlock>(a.rhist);
+  if (blockIdx.x == 0) cta_exclusive_scan<kBlock>(a.rhist, a.rbuckets);
   if (!grid_barrier(a.bar, passed, nullptr)) return r;
   const long long R = order_run(live, gridDim.x);
   const Slots D = slots_global(a, buf ^ 1, 0);
@@ -657,8 +653,8 @@ __device__ __noinline__ Redealt redeal(const LockArgs& a, const Terrain* TT, lon
   r.lo = sr.lo;
   r.nd = sr.nd;
   r.ok = true;
-  const long long w0 = (long long)blockIdx.x * kResortBuckets / gridDim.x;
-  const long long w1 = (long long)(blockIdx.x + 1) * kResortBuckets / gridDim.x;
+  const long long w0 = (long long)blockIdx.x * a.rbuckets / gridDim.x;
+  const long long w1 = (long long)(blockIdx.x + 1) * a.rbuckets / gridDim.x;
   for (long long i = w0 + threadIdx.x; i < w1; i += kBlock) a.rhist[i] = 0;
   return r;
 }
@@ -723,8 +719,8 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     for (long long i = w0 + threadIdx.x; i < w1; i += blockDim.x) a.arr[i] = 0ull;
   }
   if (redeals) {  // and the re-deal's bucket counts
-    const long long w0 = (long long)blockIdx.x * kResortBuckets / gridDim.x;
-    const long long w1 = (long long)(blockIdx.x + 1) * kResortBuckets / gridDim.x;
+    const long long w0 = (long long)blockIdx.x * a.rbuckets / gridDim.x;
+    const long long w1 = (long long)(blockIdx.x + 1) * a.rbuckets / gridDim.x;
     for (long long i = w0 + threadIdx.x; i < w1; i += blockDim.x) a.rhist[i] = 0;
   }
 
@@ -1235,11 +1231,19 @@ int order_shift(long long cells) {
   return shift;
 }
 
-// the bucket shift of the re-deal: at most kResortBuckets buckets of cells
-int resort_shift(long long cells) {
-  int shift = 0;
-  while (((cells - 1) >> shift) + 1 > kResortBuckets) ++shift;
-  return shift;
+// The re-deal's buckets for `total` drops on `cells` cells and a grid of
+// `grid` CTAs: about four per run of drops (finer buckets order a run's
+// drops along the map, coarser ones keep CTA 0's prefix sum short), at most
+// kResortBuckets, the count used rounded up to whole kResortBucketStep.
+void resort_buckets(long long cells, long long total, long long grid, int* shift, int* used) {
+  const long long R = order_run(total, grid);
+  long long want = 4 * ((total + R - 1) / R);
+  if (want > kResortBuckets) want = kResortBuckets;
+  int s = 0;
+  while (((cells - 1) >> s) + 1 > want) ++s;
+  const long long n = ((cells - 1) >> s) + 1;
+  *shift = s;
+  *used = (int)((n + kResortBucketStep - 1) / kResortBucketStep * kResortBucketStep);
 }
 
 cudaError_t launch_spawn_order(shy_world* w, int total) {
@@ -1352,6 +1356,7 @@ cudaError_t launch_lockstep_n(LockArgs& a, int sm_count, int grid_hint, cudaStre
     if ((e = launch_facts<kBlock, true>(&fr)) != cudaSuccess) return e;
     if (fr->per0 < 1) return cudaErrorLaunchOutOfResources;
     const long long gr = (long long)fr->per0 * sm_count < want ? (long long)fr->per0 * sm_count : want;
+    resort_buckets(a.cells, a.total_drops, gr, &a.rshift, &a.rbuckets);
     return cudaLaunchCooperativeKernel((const void*)lockstep_kernel<kBlock, true>, dim3((int)gr), dim3(kBlock),
                                        args, 0, stream);
   }
@@ -1410,7 +1415,8 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.gain2 = w->dgain2;
   a.terr2 = w->dterr2;
   a.rhist = w->dresort;
-  a.rshift = resort_shift(w->cells);
+  a.rshift = 0;  // set with the grid (launch_lockstep_n)
+  a.rbuckets = 0;
   a.resort = w->batch_resort < 0 ? (ordered ? kResortSteps : 0) : w->batch_resort;
   a.smem_slots = 0;
   a.P = w->P;
@@ -1483,6 +1489,7 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.age2 = a.terr2 = a.rhist = nullptr;
   a.gain2 = nullptr;
   a.rshift = 0;
+  a.rbuckets = 0;
   a.resort = 0;  // no second set of slots in the caller's buffers
   a.smem_slots = 0;
   a.P = b.P;
