@@ -37,10 +37,17 @@ def test_hook_rejects_long_stalls(shy):
     assert L.shy_debug_stall_waits(0) == 0
 
 
-def test_batched_barrier_times_out_then_world_recovers(shy, po, stall):
+@pytest.mark.parametrize("redeal", [False, True])
+def test_batched_barrier_times_out_then_world_recovers(shy, po, stall, redeal):
+    """Both instantiations of the lock-step kernel: slots in shared memory,
+    and slots in global memory with the live drops re-dealt every step."""
     nx, ny, drops, seed = 96, 80, 600, 11
     H = po.value_noise(nx, ny, 3)
     w = shy.World(nx, ny, seed=seed)
+    if redeal:
+        w.set_launch(0, 1)
+        w.set_block(256, 0)
+        w.set_resort(1)
     w.set_field("height", H)
     with pytest.raises(shy.ShyError) as ei:
         w.erode(drops, 1)
