@@ -275,23 +275,22 @@ class BatchWorkload:
         self.w.set_cycle(0)
 
     def host_buffers(self, torch):
-        bufs = []
-        for i, h in enumerate(self.h0):
-            d = {}
-            for f in FIELDS:
-                b = torch.empty(h.shape, dtype=torch.float32, pin_memory=True).numpy()
-                b[...] = h if f == "height" else 0.0
-                d[f] = b
-            bufs.append(d)
+        # every terrain's cells back to back, one pinned array per field: the
+        # whole batch's state moves in one call each way (shy_world_set_state)
+        import numpy as np
+        flat = np.concatenate([np.asarray(h, np.float32).reshape(-1) for h in self.h0])
+        bufs = {}
+        for f in FIELDS:
+            b = torch.empty(flat.shape, dtype=torch.float32, pin_memory=True).numpy()
+            b[...] = flat if f == "height" else 0.0
+            bufs[f] = b
         return bufs
 
     def upload(self, bufs):
-        for i, d in enumerate(bufs):
-            self.w.set_state(i, **d)
+        self.w.set_state_all(**bufs)
 
     def download(self, bufs):
-        for i, d in enumerate(bufs):
-            self.w.get_state(i, out=d)
+        self.w.get_state_all(out=bufs)
 
 
 FIELDS = ("height", "discharge", "momentum_x", "momentum_y")

@@ -149,6 +149,15 @@ int shy_terrain_set_state(shy_world* w, int terrain, const float* height, const 
                           const float* momentum_x, const float* momentum_y, size_t count);
 int shy_terrain_get_state(shy_world* w, int terrain, float* height, float* discharge, float* momentum_x,
                           float* momentum_y, size_t count);
+/* The same for every terrain of the world at once (no reference
+ * counterpart: the reference has one terrain): each non-NULL array holds all
+ * cells, terrain after terrain in creation order, each terrain x-major
+ * (count = the sum of nx * ny over the terrains).  One copy per field and one
+ * host synchronisation, however many terrains. */
+int shy_world_set_state(shy_world* w, const float* height, const float* discharge, const float* momentum_x,
+                        const float* momentum_y, size_t count);
+int shy_world_get_state(shy_world* w, float* height, float* discharge, float* momentum_x, float* momentum_y,
+                        size_t count);
 /* The same state calls on DEVICE memory (no reference counterpart: the
  * reference has no device): each non-NULL pointer is nx * ny floats of device
  * (or managed) memory of the world's device.  The copies run on the world's

@@ -178,6 +178,48 @@ class _Handle:
         check(lib().shy_terrain_get_state(self._w, terrain, *ptrs, n))
         return out
 
+    def _cells_total(self):
+        sizes = getattr(self, "sizes", None) or [(self.nx, self.ny)]
+        return sum(int(x) * int(y) for x, y in sizes)
+
+    def set_state_all(self, **fields):
+        """Every terrain's height / discharge / momentum_x / momentum_y in one
+        call (shy_world_set_state): float32 arrays of all cells, terrain after
+        terrain in creation order, each x-major; fields not given are left
+        unchanged."""
+        unknown = set(fields) - set(self._STATE)
+        if unknown:
+            raise ValueError(f"unknown fields {sorted(unknown)}")
+        n = self._cells_total()
+        keep, ptrs = [], []
+        for name in self._STATE:
+            a = fields.get(name)
+            if a is None:
+                ptrs.append(None)
+                continue
+            a = np.ascontiguousarray(a, np.float32).reshape(n)
+            keep.append(a)
+            ptrs.append(_fptr(a))
+        check(lib().shy_world_set_state(self._w, *ptrs, n))
+
+    def get_state_all(self, out=None):
+        """The four state fields of every terrain (shy_world_get_state), as
+        flat arrays laid out like set_state_all's, into `out` when given."""
+        n = self._cells_total()
+        if out is None:
+            out = {name: np.empty(n, np.float32) for name in self._STATE}
+        ptrs = []
+        for name in self._STATE:
+            a = out.get(name)
+            if a is None:
+                ptrs.append(None)
+                continue
+            if a.dtype != np.float32 or a.size != n or not a.flags.c_contiguous:
+                raise ValueError(f"{name}: want a contiguous float32 array of {n} elements")
+            ptrs.append(_fptr(a))
+        check(lib().shy_world_get_state(self._w, *ptrs, n))
+        return out
+
     def _device_args(self, terrain, tensors):
         nx, ny = self._terrain_shape(terrain)
         ptrs = []

@@ -122,6 +122,8 @@ SIGNATURES = {
     "shy_world_sync": (C.c_int, [W]),
     "shy_terrain_set_state": (C.c_int, [W, C.c_int, FP, FP, FP, FP, C.c_size_t]),
     "shy_terrain_get_state": (C.c_int, [W, C.c_int, FP, FP, FP, FP, C.c_size_t]),
+    "shy_world_set_state": (C.c_int, [W, FP, FP, FP, FP, C.c_size_t]),
+    "shy_world_get_state": (C.c_int, [W, FP, FP, FP, FP, C.c_size_t]),
     "shy_terrain_set_state_device": (C.c_int, [W, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_size_t]),
     "shy_terrain_get_state_device": (C.c_int, [W, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

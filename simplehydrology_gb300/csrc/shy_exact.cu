@@ -285,6 +285,16 @@ cudaError_t launch_pack_state(shy_world* w, int t, const float* d, const float* 
   return cudaGetLastError();
 }
 
+cudaError_t launch_pack_state_all(shy_world* w, const float* d, const float* mx, const float* my) {
+  pack_state_kernel<<<blocks_for(w->cells), kBlock, 0, w->stream>>>(w->rec, d, mx, my, w->cells, w->P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_state_all(shy_world* w, float* d, float* mx, float* my) {
+  unpack_state_kernel<<<blocks_for(w->cells), kBlock, 0, w->stream>>>(w->rec, d, mx, my, w->cells);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_unpack_state(shy_world* w, int t, float* d, float* mx, float* my) {
   const Terrain& T = w->terrains[t];
   const long long n = (long long)T.nx * T.ny;

@@ -281,6 +281,9 @@ cudaError_t launch_scatter_comp(shy_world* w, int terrain, int comp, const float
 // erf records included; and back out
 cudaError_t launch_pack_state(shy_world* w, int t, const float* d, const float* mx, const float* my);
 cudaError_t launch_unpack_state(shy_world* w, int t, float* d, float* mx, float* my);
+// the same over every terrain's cells at once (arrays of w->cells floats)
+cudaError_t launch_pack_state_all(shy_world* w, const float* d, const float* mx, const float* my);
+cudaError_t launch_unpack_state_all(shy_world* w, float* d, float* mx, float* my);
 // timing: open a launch interval of `kind` (returns the pair index or -1)
 cudaError_t timing_begin(shy_world* w, int kind, int* slot);
 cudaError_t timing_end(shy_world* w, int slot);

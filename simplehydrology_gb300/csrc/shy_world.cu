@@ -629,6 +629,58 @@ int shy_terrain_get_state(shy_world* w, int t, float* height, float* discharge, 
   return SHY_OK;
 }
 
+// Every terrain's state in one call each way: the arrays hold all cells,
+// terrain after terrain in creation order (the world's own packing).
+int shy_world_set_state(shy_world* w, const float* height, const float* discharge, const float* momentum_x,
+                        const float* momentum_y, size_t count) {
+  int rc = check_world(w);
+  if (rc) return rc;
+  if (count != (size_t)w->cells) {
+    set_error("shy_world_set_state: count %zu, want %lld (all terrains' cells)", count, w->cells);
+    return SHY_ERR_INVALID_ARG;
+  }
+  if (momentum_y && !w->stage) SHY_CHECK_CUDA(dalloc(&w->stage, (size_t)w->cells), "allocate staging");
+  const size_t bytes = sizeof(float) * (size_t)w->cells;
+  cudaStream_t s = w->stream;
+  if (height) {
+    SHY_CHECK_CUDA(cudaMemcpyAsync(w->h, height, bytes, cudaMemcpyHostToDevice, s), "upload heights");
+    w->hq_stale = true;
+  }
+  if (discharge) SHY_CHECK_CUDA(cudaMemcpyAsync(w->scratch, discharge, bytes, cudaMemcpyHostToDevice, s), "upload");
+  if (momentum_x) SHY_CHECK_CUDA(cudaMemcpyAsync(w->relax, momentum_x, bytes, cudaMemcpyHostToDevice, s), "upload");
+  if (momentum_y) SHY_CHECK_CUDA(cudaMemcpyAsync(w->stage, momentum_y, bytes, cudaMemcpyHostToDevice, s), "upload");
+  if (discharge || momentum_x || momentum_y)
+    SHY_CHECK_CUDA(launch_pack_state_all(w, discharge ? w->scratch : nullptr, momentum_x ? w->relax : nullptr,
+                                         momentum_y ? w->stage : nullptr),
+                   "pack state");
+  if (discharge) w->ceq_source = ERF_DEVICE;
+  SHY_CHECK_CUDA(cudaStreamSynchronize(s), "synchronize");
+  return SHY_OK;
+}
+
+int shy_world_get_state(shy_world* w, float* height, float* discharge, float* momentum_x, float* momentum_y,
+                        size_t count) {
+  int rc = check_world(w);
+  if (rc) return rc;
+  if (count != (size_t)w->cells) {
+    set_error("shy_world_get_state: count %zu, want %lld (all terrains' cells)", count, w->cells);
+    return SHY_ERR_INVALID_ARG;
+  }
+  if (momentum_y && !w->stage) SHY_CHECK_CUDA(dalloc(&w->stage, (size_t)w->cells), "allocate staging");
+  const size_t bytes = sizeof(float) * (size_t)w->cells;
+  cudaStream_t s = w->stream;
+  if (discharge || momentum_x || momentum_y)
+    SHY_CHECK_CUDA(launch_unpack_state_all(w, discharge ? w->scratch : nullptr, momentum_x ? w->relax : nullptr,
+                                           momentum_y ? w->stage : nullptr),
+                   "unpack state");
+  if (height) SHY_CHECK_CUDA(cudaMemcpyAsync(height, w->h, bytes, cudaMemcpyDeviceToHost, s), "download heights");
+  if (discharge) SHY_CHECK_CUDA(cudaMemcpyAsync(discharge, w->scratch, bytes, cudaMemcpyDeviceToHost, s), "download");
+  if (momentum_x) SHY_CHECK_CUDA(cudaMemcpyAsync(momentum_x, w->relax, bytes, cudaMemcpyDeviceToHost, s), "download");
+  if (momentum_y) SHY_CHECK_CUDA(cudaMemcpyAsync(momentum_y, w->stage, bytes, cudaMemcpyDeviceToHost, s), "download");
+  SHY_CHECK_CUDA(cudaStreamSynchronize(s), "synchronize");
+  return SHY_OK;
+}
+
 // device pointers of the state calls: device (or managed) memory of the
 // world's device, or null
 static int check_device_ptrs(shy_world* w, const char* fn, const void* const* p, int n) {

@@ -375,3 +375,40 @@ def test_cycles_as_cuda_graphs_give_the_oracle_bits(shy, po):
     compare_all(w.get_field, m, po, "graphs")
     assert w.cycle() == 13
     w.close()
+
+
+def test_whole_world_state_equals_per_terrain_state(shy, po):
+    """shy_world_set_state / shy_world_get_state move every terrain's state
+    in one call each way, laid out terrain after terrain; the result equals
+    the per-terrain state calls' bit for bit, and a batch uploaded either way
+    erodes to the same bits."""
+    sizes = [(64, 48), (40, 72), (56, 56)]
+    seeds = [21, 22, 23]
+    drops = [900, 1500, 700]
+    rng = np.random.default_rng(5)
+    hs = [po.value_noise(x, y, 40 + t) for t, (x, y) in enumerate(sizes)]
+    ds = [rng.random((x, y), dtype=np.float32) * 3 for x, y in sizes]
+    mxs = [rng.standard_normal((x, y)).astype(np.float32) for x, y in sizes]
+    mys = [rng.standard_normal((x, y)).astype(np.float32) for x, y in sizes]
+    outs = []
+    for whole in (False, True):
+        b = shy.Batch(sizes, drops, seeds)
+        if whole:
+            cat = lambda arrs: np.concatenate([a.reshape(-1) for a in arrs])
+            b.set_state_all(height=cat(hs), discharge=cat(ds), momentum_x=cat(mxs), momentum_y=cat(mys))
+        else:
+            for t in range(len(sizes)):
+                b.set_state(t, height=hs[t], discharge=ds[t], momentum_x=mxs[t], momentum_y=mys[t])
+        st = b.get_state_all()
+        b.erode(2)
+        st2 = b.get_state_all()
+        per = [b.get_state(t) for t in range(len(sizes))]
+        outs.append((st, st2, per))
+        b.close()
+    for k in outs[0][0]:
+        assert np.array_equal(bits(outs[0][0][k]), bits(outs[1][0][k])), k
+        assert np.array_equal(bits(outs[0][1][k]), bits(outs[1][1][k])), k
+    # the flat layout is the per-terrain arrays back to back
+    for k in outs[1][1]:
+        flat = np.concatenate([p[k].reshape(-1) for p in outs[1][2]])
+        assert np.array_equal(bits(outs[1][1][k]), bits(flat)), k
