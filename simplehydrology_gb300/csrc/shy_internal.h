@@ -156,7 +156,6 @@ struct shy_world {
   float2* dspd = nullptr;
   float2* dvs = nullptr;      // {volume, sediment}
   int* dage = nullptr;        // -1: not descending
-  long long* dgain = nullptr; // evaporation gain so far, 32.32
   long long* down = nullptr;  // the drop's own height change this step, 32.32
   int* dterr = nullptr;       // terrain of the slot
   long long* dcell = nullptr; // cell of this step's exchange, -1 if none
@@ -174,7 +173,6 @@ struct shy_world {
   float2* dspd2 = nullptr;
   float2* dvs2 = nullptr;
   int* dage2 = nullptr;
-  long long* dgain2 = nullptr;
   int* dterr2 = nullptr;
   int* dresort = nullptr;
   float* stage = nullptr;             // cells floats, third staging buffer of the state calls
@@ -231,7 +229,6 @@ struct CycleBuffers {
   float* track_f;
   float2 *pos, *spd, *vs;
   int* age;
-  long long* gain;
   long long* own;
   int* terr;
   long long* cell;

@@ -67,7 +67,7 @@ namespace {
 const int kLockBlock = 256;
 const int kSmemTerrains = 128;
 // shared-memory bytes per drop slot: its state plus one steep-queue entry
-const int kSlotBytes = 3 * 8 + 4 * 8 + 2 * 4 + (int)sizeof(SteepCell);
+const int kSlotBytes = 3 * 8 + 3 * 8 + 2 * 4 + (int)sizeof(SteepCell);
 // A grid barrier gives up (and flags SHY_ERR_TIMEOUT) after this long.
 const unsigned long long kBarrierLimitNs = 2000000000ull;
 
@@ -249,7 +249,6 @@ struct LockArgs {
   float2* spd;
   float2* vs;
   int* age;
-  long long* gain;  // evaporation gain of the drop so far, 32.32
   long long* own;   // the drop's own height change this step, 32.32
   int* terr;
   long long* cell;
@@ -264,7 +263,6 @@ struct LockArgs {
   float2* spd2;
   float2* vs2;
   int* age2;
-  long long* gain2;
   int* terr2;
   int* rhist;    // re-deal: live drops per bucket of cells, then offsets; zero between re-deals
   int rshift;    //   bucket = cell >> rshift
@@ -284,7 +282,6 @@ struct Slots {
   float2* pos;
   float2* spd;
   float2* vs;  // {volume, sediment}
-  long long* gain;
   long long* own;
   long long* cell;  // cell of this step's exchange, -1 if none
   long long* ctr;   // cascade centre this slot runs this step, -1 if none
@@ -301,7 +298,6 @@ __device__ __forceinline__ Slots slots_global(const LockArgs& a, int buf, long l
   S.pos = (buf ? a.pos2 : a.pos) + lo;
   S.spd = (buf ? a.spd2 : a.spd) + lo;
   S.vs = (buf ? a.vs2 : a.vs) + lo;
-  S.gain = (buf ? a.gain2 : a.gain) + lo;
   S.own = a.own + lo;
   S.cell = a.cell + lo;
   S.ctr = a.ctr + lo;
@@ -319,7 +315,6 @@ __device__ __forceinline__ Slots slots_of(const LockArgs& a, unsigned char* smem
     S.pos = reinterpret_cast<float2*>(p); p += 8 * cap;
     S.spd = reinterpret_cast<float2*>(p); p += 8 * cap;
     S.vs = reinterpret_cast<float2*>(p); p += 8 * cap;
-    S.gain = reinterpret_cast<long long*>(p); p += 8 * cap;
     S.own = reinterpret_cast<long long*>(p); p += 8 * cap;
     S.cell = reinterpret_cast<long long*>(p); p += 8 * cap;
     S.ctr = reinterpret_cast<long long*>(p); p += 8 * cap;
@@ -620,18 +615,16 @@ __device__ __noinline__ Redealt redeal(const LockArgs& a, const Terrain* TT, lon
   const Slots D = slots_global(a, buf ^ 1, 0);
   int ag_n = -1, ti_n = 0;
   float2 p_n = make_float2(0.0f, 0.0f), s_n = p_n, v_n = p_n;
-  long long g_n = 0;
   if ((int)threadIdx.x < nd) {
     const int j = threadIdx.x;
-    ag_n = S.age[j]; ti_n = S.terr[j]; p_n = S.pos[j]; s_n = S.spd[j]; v_n = S.vs[j]; g_n = S.gain[j];
+    ag_n = S.age[j]; ti_n = S.terr[j]; p_n = S.pos[j]; s_n = S.spd[j]; v_n = S.vs[j];
   }
   for (int j = threadIdx.x; j < nd; j += kBlock) {
     const int ag = ag_n, ti = ti_n;
     const float2 p = p_n, sp = s_n, vs = v_n;
-    const long long gn = g_n;
     if (j + kBlock < nd) {
       const int jn = j + kBlock;
-      ag_n = S.age[jn]; ti_n = S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; v_n = S.vs[jn]; g_n = S.gain[jn];
+      ag_n = S.age[jn]; ti_n = S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; v_n = S.vs[jn];
     }
     if (ag < 0) continue;
     const long long k = atomicAdd(&a.rhist[drop_cell(TT[ti], p) >> a.rshift], 1);
@@ -645,7 +638,6 @@ __device__ __noinline__ Redealt redeal(const LockArgs& a, const Terrain* TT, lon
     D.spd[d] = sp;
     D.vs[d] = vs;
     D.age[d] = ag;
-    D.gain[d] = gn;
     D.terr[d] = ti;
   }
   if (!grid_barrier(a.bar, passed, nullptr)) return r;
@@ -688,6 +680,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   const long long run = order_run(a.total_drops, gridDim.x);
   int buf = 0;  // which set of persistent slot fields the CTA's slots are in
   const bool redeals = kRedeal && a.resort > 0 && !a.smem_slots;
+  const bool one_terrain = a.n_terrains == 1;  // every slot's terrain is 0: no need to load it
 
   const shy_params& P = a.P;
   const unsigned long long cycle = a.bar->cycle;
@@ -748,7 +741,6 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     S.pos[j] = make_float2((float)x, (float)y);
     S.spd[j] = make_float2(0.0f, 0.0f);
     S.vs[j] = make_float2(1.0f, 0.0f);
-    S.gain[j] = 0;
     atomicAdd(&a.cq[c].cnt[0], 1);
   }
   const unsigned long long born_all = block_sum_u64<kBlock>(born);  // valid in thread 0
@@ -774,19 +766,17 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     const bool rev_d = redeals && (step & 1);
     int ag_n = 0, ti_n = 0;
     float2 p_n = make_float2(0.0f, 0.0f), s_n = p_n, v_n = p_n;
-    long long gn_n = 0;
     if ((int)threadIdx.x < nd) {
       const int j = rev_d ? nd - 1 - (int)threadIdx.x : (int)threadIdx.x;
-      ag_n = S.age[j]; ti_n = S.terr[j]; p_n = S.pos[j]; s_n = S.spd[j]; v_n = S.vs[j]; gn_n = S.gain[j];
+      ag_n = S.age[j]; ti_n = one_terrain ? 0 : S.terr[j]; p_n = S.pos[j]; s_n = S.spd[j]; v_n = S.vs[j];
     }
     for (int i = threadIdx.x; i < nd; i += blockDim.x) {
       const int j = rev_d ? nd - 1 - i : i;
       const int ag = ag_n, ti = ti_n;
       float2 p = p_n, s = s_n, v = v_n;
-      long long gn = gn_n;
       if (i + (int)blockDim.x < nd) {
         const int jn = rev_d ? nd - 1 - (i + (int)blockDim.x) : i + (int)blockDim.x;
-        ag_n = S.age[jn]; ti_n = S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; v_n = S.vs[jn]; gn_n = S.gain[jn];
+        ag_n = S.age[jn]; ti_n = one_terrain ? 0 : S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; v_n = S.vs[jn];
       }
       if (ag < 0) continue;
       const Terrain T = TT[ti];
@@ -820,7 +810,6 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         const long long dep = shy_q32_dev(v.y);
         add_i64(&a.cq[c].e, dep);
         S.own[j] = dep;
-        gain_q += gn;
         S.age[j] = -2;
         S.ctr[j] = -1;
         continue;
@@ -872,11 +861,12 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       const float s0 = v.y;  // water.h:135-136, without the FP64 unit
       v.y = shy_evap_div_ff(v.y, &ev);
       v.x = vnext;
-      gn += shy_q32_dev(v.y - s0);  // exact difference (Sterbenz)
+      // the evaporation gain, an exact difference (Sterbenz), goes straight
+      // to the thread's integer total: no drop needs its own
+      gain_q += shy_q32_dev(v.y - s0);
       if (out) {  // water.h:139-142
         ++n_oob;
         loss_q += shy_q32_dev(v.y);
-        gain_q += gn;
         S.age[j] = -2;
         S.ctr[j] = -1;
         continue;
@@ -888,7 +878,6 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       S.pos[j] = p;
       S.spd[j] = s;
       S.vs[j] = v;
-      S.gain[j] = gn;
     }
     lap(0);
     if (!grid_barrier(a.bar, passed, nullptr)) { ok = false; break; }
@@ -906,7 +895,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     if ((int)threadIdx.x < nd) {
       const int j = rev_s ? nd - 1 - (int)threadIdx.x : (int)threadIdx.x;
       c2_n = S.ctr[j];
-      ti_n2 = S.terr[j];
+      ti_n2 = one_terrain ? 0 : S.terr[j];
     }
     for (int i = threadIdx.x; i < nd; i += blockDim.x) {
       const long long c2 = c2_n;
@@ -914,7 +903,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       if (i + (int)blockDim.x < nd) {  // the next slot's claim, loaded ahead
         const int jn = rev_s ? nd - 1 - (i + (int)blockDim.x) : i + (int)blockDim.x;
         c2_n = S.ctr[jn];
-        ti_n2 = S.terr[jn];
+        ti_n2 = one_terrain ? 0 : S.terr[jn];
       }
       if (c2 < 0) continue;
       const Terrain T = TT[ti];
@@ -1392,7 +1381,6 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.spd = w->dspd;
   a.vs = w->dvs;
   a.age = w->dage;
-  a.gain = w->dgain;
   a.own = w->down;
   a.terr = w->dterr;
   a.cell = w->dcell;
@@ -1412,7 +1400,6 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.spd2 = w->dspd2;
   a.vs2 = w->dvs2;
   a.age2 = w->dage2;
-  a.gain2 = w->dgain2;
   a.terr2 = w->dterr2;
   a.rhist = w->dresort;
   a.rshift = 0;  // set with the grid (launch_lockstep_n)
@@ -1476,7 +1463,6 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.spd = b.spd;
   a.vs = b.vs;
   a.age = b.age;
-  a.gain = b.gain;
   a.own = b.own;
   a.terr = b.terr;
   a.cell = b.cell;
@@ -1487,7 +1473,6 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.order = nullptr;
   a.pos2 = a.spd2 = a.vs2 = nullptr;
   a.age2 = a.terr2 = a.rhist = nullptr;
-  a.gain2 = nullptr;
   a.rshift = 0;
   a.rbuckets = 0;
   a.resort = 0;  // no second set of slots in the caller's buffers

@@ -28,7 +28,7 @@ struct NoallocScratch {
   // <= cells / 64 + (nx + ny) / 8 + 1 words each
   unsigned long long arr[2 * (SHY_NOALLOC_MAX_CELLS / 64 + (SHY_NOALLOC_MAX_CELLS + 1) / 8 + 2)];
   float2 pos[SHY_NOALLOC_MAX_DROPS], spd[SHY_NOALLOC_MAX_DROPS], vs[SHY_NOALLOC_MAX_DROPS];
-  long long gain[SHY_NOALLOC_MAX_DROPS], own[SHY_NOALLOC_MAX_DROPS];
+  long long own[SHY_NOALLOC_MAX_DROPS];
   long long cell[SHY_NOALLOC_MAX_DROPS], ctr[SHY_NOALLOC_MAX_DROPS];
   int age[SHY_NOALLOC_MAX_DROPS], terr[SHY_NOALLOC_MAX_DROPS];
   Terrain terrain;
@@ -212,7 +212,6 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
   b.spd = sc->spd;
   b.vs = sc->vs;
   b.age = sc->age;
-  b.gain = sc->gain;
   b.own = sc->own;
   b.terr = sc->terr;
   b.cell = sc->cell;
