@@ -158,8 +158,8 @@ struct shy_world {
   int* dage = nullptr;        // -1: not descending
   long long* down = nullptr;  // the drop's own height change this step, 32.32
   int* dterr = nullptr;       // terrain of the slot
-  long long* dcell = nullptr; // cell of this step's exchange, -1 if none
-  long long* dctr = nullptr;  // cascade centre this slot runs this step, -1 if none
+  int* dcell = nullptr;       // cell of this step's exchange within its terrain, -1 if none
+  int* dctr = nullptr;        // cascade centre this slot runs this step, within its terrain, -1 if none
   shy::SteepCell* dsteep = nullptr;  // steep-cascade queue (one entry per drop slot at most)
   unsigned long long* arr = nullptr;  // arrivals bitmaps (two step parities), all terrains
   long long arr_words = 0;            // words of one parity's bitmap
@@ -231,8 +231,8 @@ struct CycleBuffers {
   int* age;
   long long* own;
   int* terr;
-  long long* cell;
-  long long* ctr;
+  int* cell;
+  int* ctr;
   SteepCell* steep;
   unsigned long long* arr;  // two bitmaps of arr_words words
   long long arr_words;

@@ -67,7 +67,7 @@ namespace {
 const int kLockBlock = 256;
 const int kSmemTerrains = 128;
 // shared-memory bytes per drop slot: its state plus one steep-queue entry
-const int kSlotBytes = 3 * 8 + 3 * 8 + 2 * 4 + (int)sizeof(SteepCell);
+const int kSlotBytes = 3 * 8 + 8 + 4 * 4 + (int)sizeof(SteepCell);
 // A grid barrier gives up (and flags SHY_ERR_TIMEOUT) after this long.
 const unsigned long long kBarrierLimitNs = 2000000000ull;
 
@@ -251,8 +251,8 @@ struct LockArgs {
   int* age;
   long long* own;   // the drop's own height change this step, 32.32
   int* terr;
-  long long* cell;
-  long long* ctr;
+  int* cell;
+  int* ctr;
   SteepCell* steep;
   unsigned long long* arr;  // arrivals bitmaps, one per step parity, arr_words words each
   long long arr_words;
@@ -283,8 +283,8 @@ struct Slots {
   float2* spd;
   float2* vs;  // {volume, sediment}
   long long* own;
-  long long* cell;  // cell of this step's exchange, -1 if none
-  long long* ctr;   // cascade centre this slot runs this step, -1 if none
+  int* cell;  // cell of this step's exchange within the slot's terrain, -1 if none
+  int* ctr;   // cascade centre this slot runs this step, within its terrain, -1 if none
   int* age;         // >= 0 descending, -2 finished this step, -1 idle
   int* terr;
   SteepCell* steep;
@@ -316,8 +316,8 @@ __device__ __forceinline__ Slots slots_of(const LockArgs& a, unsigned char* smem
     S.spd = reinterpret_cast<float2*>(p); p += 8 * cap;
     S.vs = reinterpret_cast<float2*>(p); p += 8 * cap;
     S.own = reinterpret_cast<long long*>(p); p += 8 * cap;
-    S.cell = reinterpret_cast<long long*>(p); p += 8 * cap;
-    S.ctr = reinterpret_cast<long long*>(p); p += 8 * cap;
+    S.cell = reinterpret_cast<int*>(p); p += 4 * cap;
+    S.ctr = reinterpret_cast<int*>(p); p += 4 * cap;
     S.age = reinterpret_cast<int*>(p); p += 4 * cap;
     S.terr = reinterpret_cast<int*>(p);
   } else {
@@ -784,7 +784,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       const int ix = (int)p.x, iy = (int)p.y;
       const long long lc = (long long)ix * T.ny + iy;
       const long long c = T.cell_base + lc;
-      S.cell[j] = c;
+      S.cell[j] = (int)lc;  // < 2^31 cells per terrain
       // the five heights quad::_normal reads (0 outside the map)
       const bool xp = ix + 1 < T.nx, xm = ix > 0, yp = iy + 1 < T.ny, ym = iy > 0;
       // all loads issued together; a neighbour outside the map reads the
@@ -871,7 +871,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
         S.ctr[j] = -1;
         continue;
       }
-      S.ctr[j] = arrived_before == 0 ? c2 : -1;  // World::cascade(pos), water.h:151
+      S.ctr[j] = arrived_before == 0 ? jx * T.ny + jy : -1;  // World::cascade(pos), water.h:151
       if (arrived_before == 0)
         atomicOr(&a.arr[par * a.arr_words + arr_word(T, jx, jy)], arr_bit(jx, jy));
       S.age[j] = ag + 1;
@@ -890,7 +890,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     // transfer, so without any excess to begin with the sequential loop moves
     // nothing and the cascade ends here.
     const bool rev_s = redeals && !(step & 1);
-    long long c2_n = -1;
+    int c2_n = -1;
     int ti_n2 = 0;
     if ((int)threadIdx.x < nd) {
       const int j = rev_s ? nd - 1 - (int)threadIdx.x : (int)threadIdx.x;
@@ -898,16 +898,16 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       ti_n2 = one_terrain ? 0 : S.terr[j];
     }
     for (int i = threadIdx.x; i < nd; i += blockDim.x) {
-      const long long c2 = c2_n;
+      const int lc = c2_n;  // the claimed centre within the terrain, or -1
       const int ti = ti_n2;
       if (i + (int)blockDim.x < nd) {  // the next slot's claim, loaded ahead
         const int jn = rev_s ? nd - 1 - (i + (int)blockDim.x) : i + (int)blockDim.x;
         c2_n = S.ctr[jn];
         ti_n2 = one_terrain ? 0 : S.terr[jn];
       }
-      if (c2 < 0) continue;
+      if (lc < 0) continue;
       const Terrain T = TT[ti];
-      const int lc = (int)(c2 - T.cell_base);  // < 2^31 cells per terrain
+      const long long c2 = T.cell_base + lc;
       const int ix = lc / T.ny, iy = lc - ix * T.ny;
       longlong2 nv[8];
 #pragma unroll
@@ -990,22 +990,23 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     }
     unsigned long long retired = 0;
     const bool rev_t = redeals && (step & 1);
-    int ag_f = -1;
-    long long c_f = -1, own_f = 0;
+    int ag_f = -1, lc_f = -1, ti_f = 0;
+    long long own_f = 0;
     if ((int)threadIdx.x < nd) {
       const int j = rev_t ? nd - 1 - (int)threadIdx.x : (int)threadIdx.x;
-      ag_f = S.age[j]; c_f = S.cell[j]; own_f = S.own[j];
+      ag_f = S.age[j]; lc_f = S.cell[j]; own_f = S.own[j]; ti_f = one_terrain ? 0 : S.terr[j];
     }
     for (int i = threadIdx.x; i < nd; i += blockDim.x) {
       const int j = rev_t ? nd - 1 - i : i;
-      const int ag = ag_f;
-      const long long c = c_f, own = own_f;
+      const int ag = ag_f, lcs = lc_f, tis = ti_f;
+      const long long own = own_f;
       if (i + (int)blockDim.x < nd) {  // the next slot, loaded ahead
         const int jn = rev_t ? nd - 1 - (i + (int)blockDim.x) : i + (int)blockDim.x;
-        ag_f = S.age[jn]; c_f = S.cell[jn]; own_f = S.own[jn];
+        ag_f = S.age[jn]; lc_f = S.cell[jn]; own_f = S.own[jn]; ti_f = one_terrain ? 0 : S.terr[jn];
       }
       if (ag == -1) continue;
-      if (c >= 0) {
+      if (lcs >= 0) {
+        const long long c = TT[tis].cell_base + lcs;
         if (own != 0) add_i64(&a.cq[c].hq, own);
         a.cq[c].e = 0;
         a.cq[c].cnt[par] = 0;

@@ -29,7 +29,7 @@ struct NoallocScratch {
   unsigned long long arr[2 * (SHY_NOALLOC_MAX_CELLS / 64 + (SHY_NOALLOC_MAX_CELLS + 1) / 8 + 2)];
   float2 pos[SHY_NOALLOC_MAX_DROPS], spd[SHY_NOALLOC_MAX_DROPS], vs[SHY_NOALLOC_MAX_DROPS];
   long long own[SHY_NOALLOC_MAX_DROPS];
-  long long cell[SHY_NOALLOC_MAX_DROPS], ctr[SHY_NOALLOC_MAX_DROPS];
+  int cell[SHY_NOALLOC_MAX_DROPS], ctr[SHY_NOALLOC_MAX_DROPS];
   int age[SHY_NOALLOC_MAX_DROPS], terr[SHY_NOALLOC_MAX_DROPS];
   Terrain terrain;
   GridBar bar;
