@@ -210,6 +210,14 @@ int shy_world_set_block(shy_world* w, int threads, int smem_slots);
  * (see shy_world_set_launch), else never; 0 never; 1-4096 that many steps.
  * Results do not depend on it. */
 int shy_world_set_resort(shy_world* w, int steps);
+/* How a re-dealt batched cycle settles each step's height changes: 0 every
+ * drop adds its own change to its cell; 1 the drop that registered first in
+ * a cell adds the cell's whole pending sum (its slot then keeps no change of
+ * its own: fewer bytes per step, one more wait in settle, which pays only
+ * where the slots' loads miss L2 anyway); -1 (the default) 1 when the drop
+ * slots outgrow L2, else 0.  Only with re-deals (shy_world_set_resort).
+ * Results do not depend on it. */
+int shy_world_set_settle(shy_world* w, int mode);
 /* Batched cycles per CUDA graph: with k > 0, shy_erode / shy_batch_erode run
  * each k cycles as one graph (the lock-step and end-of-cycle launches of k
  * cycles), captured on the world's stream on first use and again whenever

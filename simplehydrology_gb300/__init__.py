@@ -117,6 +117,12 @@ class _Handle:
         16 steps with spawn-ordered slots, else never; 0 never)."""
         check(lib().shy_world_set_resort(self._w, steps))
 
+    def set_settle(self, mode: int = -1):
+        """With re-deals: 1 the first drop registered in a cell settles the
+        cell's whole step, 0 every drop its own change, -1 (default) 1 when
+        the slots outgrow L2."""
+        check(lib().shy_world_set_settle(self._w, mode))
+
     def set_graph(self, cycles_per_graph: int = 0):
         """Run batched cycles as CUDA graphs of this many cycles (0: none)."""
         check(lib().shy_world_set_graph(self._w, cycles_per_graph))

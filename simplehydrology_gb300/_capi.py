@@ -141,6 +141,7 @@ SIGNATURES = {
     "shy_world_set_block": (C.c_int, [W, C.c_int, C.c_int]),
     "shy_world_set_graph": (C.c_int, [W, C.c_int]),
     "shy_world_set_resort": (C.c_int, [W, C.c_int]),
+    "shy_world_set_settle": (C.c_int, [W, C.c_int]),
     "shy_debug_stall_waits": (C.c_int, [C.c_uint64]),
     "shy_erode": (C.c_int, [W, C.c_int, C.c_int]),
     "shy_erode_exact": (C.c_int, [W, P(C.c_int32), C.c_int]),

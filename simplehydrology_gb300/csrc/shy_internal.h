@@ -204,6 +204,8 @@ struct shy_world {
   int batch_smem = 1;         // 0: drop slots in global memory even where shared memory would hold them
   int batch_resort = -1;      // steps between re-deals of the live drops (-1: kResortSteps with
                               // spawn-ordered slots in global memory, else never; 0 never)
+  int batch_settle = -1;      // with re-deals: 1 the first drop in a cell settles it, 0 every drop
+                              // its own change, -1 the first when the slots outgrow L2
   int graph_cycles = 0;       // batched cycles per CUDA graph (0: launched one by one)
   cudaGraphExec_t gexec = nullptr;  // the captured cycles
   unsigned long long graph_key = 0; // what they were captured with (launch_key)

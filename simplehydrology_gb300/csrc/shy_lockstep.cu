@@ -29,8 +29,10 @@
 //   settle  the queued transfers go straight to the fixed-point heights (no
 //      height is read in this phase).  Every drop adds its own height change
 //      to its cell's fixed-point height and clears the cell's pending sum and
-//      count; finished drops retire.  The arrivals bitmap of the other step
-//      parity is cleared for the next step.
+//      count (or, when the slots outgrow L2, only the drop that registered
+//      first in the cell adds the cell's whole pending sum: see kLean);
+//      finished drops retire.  The arrivals bitmap of the other step parity
+//      is cleared for the next step.
 // With the cell state larger than L2, each cycle's drops are sorted by spawn
 // cell and dealt to the CTAs in runs of consecutive drops, round-robin: each
 // run is a compact stretch of the maps, and every CTA samples stretches from
@@ -66,6 +68,15 @@ namespace {
 // CTA's slots fit in one pass); 256 unless the world asks otherwise
 const int kLockBlock = 256;
 const int kSmemTerrains = 128;
+// With kLean (slots in global memory, larger than L2), a slot's age field
+// carries, besides the age (below 2^30: max_age < 1e6), this flag: the drop
+// was the first to register at the cell it is in.  In settle that drop alone
+// adds the cell's pending sum (every drop's change there, the same integer
+// sum) to its height and clears the cell's sum and count, so no slot needs
+// to keep its own change (8 B written and 8 B read per drop-step fewer).
+// The pending sum's load is a round trip in settle, which only pays where
+// the slots' own loads already miss L2.
+const int kFirstAtCell = 1 << 30;
 // shared-memory bytes per drop slot: its state plus one steep-queue entry
 const int kSlotBytes = 3 * 8 + 8 + 4 * 4 + (int)sizeof(SteepCell);
 // A grid barrier gives up (and flags SHY_ERR_TIMEOUT) after this long.
@@ -268,6 +279,7 @@ struct LockArgs {
   int rshift;    //   bucket = cell >> rshift
   int rbuckets;  //   buckets in use: a multiple of kResortBucketStep, at most kResortBuckets
   int resort;    //   steps between re-deals (0: never; only with slots in global memory)
+  int lean;      // 1: the slots outgrow L2 (the kLean instantiation, with re-deals)
   int smem_slots;   // 1: drop slots and queue live in dynamic shared memory
   int smem_allowed;  // 0: keep the slots in global memory even when they would fit
   shy_params P;
@@ -654,7 +666,8 @@ __device__ __noinline__ Redealt redeal(const LockArgs& a, const Terrain* TT, lon
 // 128 registers: two 256-thread CTAs per SM.  kRedeal: the instantiation
 // with the re-deal (slots in global memory, a.resort > 0); the other has no
 // trace of it, so that its slot pointers stay fixed for the whole cycle.
-template <int kBlock, bool kRedeal>
+// kLean (with kRedeal only): first-registered drops settle whole cells.
+template <int kBlock, bool kRedeal, bool kLean>
 __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
   extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ Terrain sT[kSmemTerrains];
@@ -737,11 +750,15 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     }
     ++n_drops;
     ++born;
-    S.age[j] = 0;
     S.pos[j] = make_float2((float)x, (float)y);
     S.spd[j] = make_float2(0.0f, 0.0f);
     S.vs[j] = make_float2(1.0f, 0.0f);
-    atomicAdd(&a.cq[c].cnt[0], 1);
+    if (kLean) {
+      S.age[j] = atomicAdd(&a.cq[c].cnt[0], 1) == 0 ? kFirstAtCell : 0;
+    } else {
+      S.age[j] = 0;
+      atomicAdd(&a.cq[c].cnt[0], 1);
+    }
   }
   const unsigned long long born_all = block_sum_u64<kBlock>(born);  // valid in thread 0
   bool ok = grid_barrier(a.bar, passed, &s_live, [] {}, a.stall_ns ? 1u : 0u,
@@ -772,19 +789,21 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     }
     for (int i = threadIdx.x; i < nd; i += blockDim.x) {
       const int j = rev_d ? nd - 1 - i : i;
-      const int ag = ag_n, ti = ti_n;
+      const int agr = ag_n, ti = ti_n;
       float2 p = p_n, s = s_n, v = v_n;
       if (i + (int)blockDim.x < nd) {
         const int jn = rev_d ? nd - 1 - (i + (int)blockDim.x) : i + (int)blockDim.x;
         ag_n = S.age[jn]; ti_n = one_terrain ? 0 : S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; v_n = S.vs[jn];
       }
-      if (ag < 0) continue;
+      if (agr < 0) continue;
+      const int ag = kLean ? (agr & (kFirstAtCell - 1)) : agr;
       const Terrain T = TT[ti];
       const CellQ* RT = a.cq + T.cell_base;
       const int ix = (int)p.x, iy = (int)p.y;
       const long long lc = (long long)ix * T.ny + iy;
       const long long c = T.cell_base + lc;
-      S.cell[j] = (int)lc;  // < 2^31 cells per terrain
+      // < 2^31 cells per terrain; with kLean only the cell's first drop settles it
+      S.cell[j] = (!kLean || (agr & kFirstAtCell)) ? (int)lc : -1;
       // the five heights quad::_normal reads (0 outside the map)
       const bool xp = ix + 1 < T.nx, xm = ix > 0, yp = iy + 1 < T.ny, ym = iy > 0;
       // all loads issued together; a neighbour outside the map reads the
@@ -809,7 +828,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       if ((float)ag > P.max_age || v.x < P.min_vol) {  // water.h:74-83
         const long long dep = shy_q32_dev(v.y);
         add_i64(&a.cq[c].e, dep);
-        S.own[j] = dep;
+        if (!kLean) S.own[j] = dep;
         S.age[j] = -2;
         S.ctr[j] = -1;
         continue;
@@ -857,7 +876,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       v.y += ex;
       const long long de = -shy_q32_dev(ex);
       add_i64(&a.cq[c].e, de);
-      S.own[j] = de;
+      if (!kLean) S.own[j] = de;
       const float s0 = v.y;  // water.h:135-136, without the FP64 unit
       v.y = shy_evap_div_ff(v.y, &ev);
       v.x = vnext;
@@ -874,7 +893,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       S.ctr[j] = arrived_before == 0 ? jx * T.ny + jy : -1;  // World::cascade(pos), water.h:151
       if (arrived_before == 0)
         atomicOr(&a.arr[par * a.arr_words + arr_word(T, jx, jy)], arr_bit(jx, jy));
-      S.age[j] = ag + 1;
+      S.age[j] = (ag + 1) | (kLean && arrived_before == 0 ? kFirstAtCell : 0);
       S.pos[j] = p;
       S.spd[j] = s;
       S.vs[j] = v;
@@ -994,19 +1013,27 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     long long own_f = 0;
     if ((int)threadIdx.x < nd) {
       const int j = rev_t ? nd - 1 - (int)threadIdx.x : (int)threadIdx.x;
-      ag_f = S.age[j]; lc_f = S.cell[j]; own_f = S.own[j]; ti_f = one_terrain ? 0 : S.terr[j];
+      ag_f = S.age[j]; lc_f = S.cell[j]; ti_f = one_terrain ? 0 : S.terr[j];
+      if (!kLean) own_f = S.own[j];
     }
     for (int i = threadIdx.x; i < nd; i += blockDim.x) {
       const int j = rev_t ? nd - 1 - i : i;
       const int ag = ag_f, lcs = lc_f, tis = ti_f;
-      const long long own = own_f;
+      long long own = own_f;
+      long long c = -1;
+      if (ag != -1 && lcs >= 0) {
+        c = TT[tis].cell_base + lcs;
+        // kLean: the cell's whole pending sum (final since descend), loaded
+        // before the next slot's fields so that the two round trips overlap
+        if (kLean) own = a.cq[c].e;
+      }
       if (i + (int)blockDim.x < nd) {  // the next slot, loaded ahead
         const int jn = rev_t ? nd - 1 - (i + (int)blockDim.x) : i + (int)blockDim.x;
-        ag_f = S.age[jn]; lc_f = S.cell[jn]; own_f = S.own[jn]; ti_f = one_terrain ? 0 : S.terr[jn];
+        ag_f = S.age[jn]; lc_f = S.cell[jn]; ti_f = one_terrain ? 0 : S.terr[jn];
+        if (!kLean) own_f = S.own[jn];
       }
       if (ag == -1) continue;
-      if (lcs >= 0) {
-        const long long c = TT[tis].cell_base + lcs;
+      if (c >= 0) {
         if (own != 0) add_i64(&a.cq[c].hq, own);
         a.cq[c].e = 0;
         a.cq[c].cnt[par] = 0;
@@ -1257,7 +1284,7 @@ namespace {
 // drops per CTA); each CTA's drop slots go to shared memory when they fit
 // without lowering that occupancy (and the world allows it), else to the
 // global arrays in `a`.
-// What a launch of lockstep_kernel<kBlock, kRedeal> needs to know about the device,
+// What a launch of lockstep_kernel<kBlock, kRedeal, kLean> needs to know about the device,
 // queried once per device and CTA size (and per dynamic shared-memory size
 // for the occupancy with slots in shared memory) rather than every cycle.
 struct LaunchFacts {
@@ -1272,7 +1299,7 @@ struct LaunchFacts {
 const int kMaxDevices = 64;
 std::mutex g_facts_mu;
 
-template <int kBlock, bool kRedeal>
+template <int kBlock, bool kRedeal, bool kLean>
 cudaError_t launch_facts(LaunchFacts** out) {
   static LaunchFacts facts[kMaxDevices];
   int dev = 0;
@@ -1283,9 +1310,10 @@ cudaError_t launch_facts(LaunchFacts** out) {
   if (!f.valid) {
     if ((e = cudaDeviceGetAttribute(&f.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
     cudaFuncAttributes fa;
-    if ((e = cudaFuncGetAttributes(&fa, lockstep_kernel<kBlock, kRedeal>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&fa, lockstep_kernel<kBlock, kRedeal, kLean>)) != cudaSuccess) return e;
     f.static_smem = (long long)fa.sharedSizeBytes;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f.per0, lockstep_kernel<kBlock, kRedeal>, kBlock, 0)) !=
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f.per0, lockstep_kernel<kBlock, kRedeal, kLean>, kBlock,
+                                                           0)) !=
         cudaSuccess)
       return e;
     f.valid = true;
@@ -1304,7 +1332,7 @@ cudaError_t launch_lockstep_n(LockArgs& a, int sm_count, int grid_hint, cudaStre
   std::lock_guard<std::mutex> lock(g_facts_mu);
   LaunchFacts* f = nullptr;
   cudaError_t e;
-  if ((e = launch_facts<kBlock, false>(&f)) != cudaSuccess) return e;
+  if ((e = launch_facts<kBlock, false, false>(&f)) != cudaSuccess) return e;
   if (f->per0 < 1) return cudaErrorLaunchOutOfResources;
   const long long max_dyn = (long long)f->optin - f->static_smem;
   long long want = ((long long)a.total_drops + 31) / 32;
@@ -1318,7 +1346,7 @@ cudaError_t launch_lockstep_n(LockArgs& a, int sm_count, int grid_hint, cudaStre
   a.smem_slots = 0;
   if (b <= max_dyn && a.smem_allowed) {
     if (b > 48 * 1024 && b > f->smem_set) {
-      if ((e = cudaFuncSetAttribute(lockstep_kernel<kBlock, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      if ((e = cudaFuncSetAttribute(lockstep_kernel<kBlock, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)b)) !=
           cudaSuccess)
         return e;
@@ -1326,7 +1354,7 @@ cudaError_t launch_lockstep_n(LockArgs& a, int sm_count, int grid_hint, cudaStre
     }
     if (b != f->last_b) {
       int per = 0;
-      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lockstep_kernel<kBlock, false>, kBlock,
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lockstep_kernel<kBlock, false, false>, kBlock,
                                                              (size_t)b)) !=
           cudaSuccess)
         return e;
@@ -1343,15 +1371,19 @@ cudaError_t launch_lockstep_n(LockArgs& a, int sm_count, int grid_hint, cudaStre
     // slots in global memory with re-deals: the other instantiation, with
     // its own residency (every CTA of a cooperative launch must fit at once)
     LaunchFacts* fr = nullptr;
-    if ((e = launch_facts<kBlock, true>(&fr)) != cudaSuccess) return e;
+    if ((e = (a.lean ? launch_facts<kBlock, true, true>(&fr) : launch_facts<kBlock, true, false>(&fr))) !=
+        cudaSuccess)
+      return e;
     if (fr->per0 < 1) return cudaErrorLaunchOutOfResources;
     const long long gr = (long long)fr->per0 * sm_count < want ? (long long)fr->per0 * sm_count : want;
     resort_buckets(a.cells, a.total_drops, gr, &a.rshift, &a.rbuckets);
-    return cudaLaunchCooperativeKernel((const void*)lockstep_kernel<kBlock, true>, dim3((int)gr), dim3(kBlock),
-                                       args, 0, stream);
+    const void* k = a.lean ? (const void*)lockstep_kernel<kBlock, true, true>
+                           : (const void*)lockstep_kernel<kBlock, true, false>;
+    return cudaLaunchCooperativeKernel(k, dim3((int)gr), dim3(kBlock), args, 0, stream);
   }
   a.resort = 0;
-  return cudaLaunchCooperativeKernel((const void*)lockstep_kernel<kBlock, false>, dim3(grid), dim3(kBlock), args, bytes,
+  a.lean = 0;
+  return cudaLaunchCooperativeKernel((const void*)lockstep_kernel<kBlock, false, false>, dim3(grid), dim3(kBlock), args, bytes,
                                      stream);
 }
 
@@ -1406,6 +1438,10 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.rshift = 0;  // set with the grid (launch_lockstep_n)
   a.rbuckets = 0;
   a.resort = w->batch_resort < 0 ? (ordered ? kResortSteps : 0) : w->batch_resort;
+  // the slots' persistent fields and per-step fields (about 40 B a drop)
+  // larger than L2: their loads miss anyway, so settling whole cells from
+  // their first drops costs no extra wait and saves the own-change bytes
+  a.lean = w->batch_settle < 0 ? ((long long)a.total_drops * 40 > w->l2_bytes ? 1 : 0) : w->batch_settle;
   a.smem_slots = 0;
   a.P = w->P;
   a.st = w->stats;
@@ -1477,6 +1513,7 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.rshift = 0;
   a.rbuckets = 0;
   a.resort = 0;  // no second set of slots in the caller's buffers
+  a.lean = 0;
   a.smem_slots = 0;
   a.P = b.P;
   a.st = b.st;

@@ -786,6 +786,17 @@ int shy_world_set_resort(shy_world* w, int steps) {
   return SHY_OK;
 }
 
+int shy_world_set_settle(shy_world* w, int mode) {
+  int rc = check_world(w);
+  if (rc) return rc;
+  if (mode < -1 || mode > 1) {
+    set_error("shy_world_set_settle: mode must be -1 (automatic), 0 or 1");
+    return SHY_ERR_INVALID_ARG;
+  }
+  w->batch_settle = mode;
+  return SHY_OK;
+}
+
 int shy_world_set_graph(shy_world* w, int cycles_per_graph) {
   int rc = check_world(w);
   if (rc) return rc;
@@ -933,8 +944,8 @@ unsigned long long launch_key(const shy_world* w) {
   };
   mix(&w->P, sizeof(w->P));
   for (const auto& T : w->terrains) mix(&T, sizeof(T));
-  const int shape[7] = {w->batch_grid, w->batch_order, w->batch_block, w->batch_smem, w->graph_cycles, w->sm_count,
-                        w->batch_resort};
+  const int shape[8] = {w->batch_grid, w->batch_order, w->batch_block, w->batch_smem, w->graph_cycles, w->sm_count,
+                        w->batch_resort, w->batch_settle};
   mix(shape, sizeof(shape));
   const void* ptrs[] = {w->h, w->cq, w->rec, w->voltab, w->trk, w->track_f, w->dpos, w->dspd, w->dvs, w->dage,
                         w->down, w->dterr, w->dcell, w->dctr, w->dsteep, w->arr, w->dorder, w->dkey,

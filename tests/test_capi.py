@@ -126,6 +126,7 @@ def test_new_entry_points_check_their_arguments_on_the_host(shy):
     assert L.shy_world_set_block(None, 256, 1) == -1
     assert L.shy_world_set_graph(None, 4) == -1
     assert L.shy_world_set_resort(None, 16) == -1
+    assert L.shy_world_set_settle(None, 1) == -1
     assert L.shy_world_set_state(None, None, None, None, None, 0) == -1
     assert L.shy_world_get_state(None, None, None, None, None, 0) == -1
     c = C.c_uint64()

@@ -267,14 +267,16 @@ def test_every_launch_shape_gives_the_oracle_bits(shy, po):
         w.close()
 
 
+@pytest.mark.parametrize("settle", [0, 1])
 @pytest.mark.parametrize("block,grid,order,resort", [(256, 0, 1, 1), (256, 0, 1, 2), (128, 5, 1, 3),
                                                      (64, 0, 0, 7), (256, 3, -1, 16), (64, 7, 1, 1)])
-def test_redeal_gives_the_oracle_bits(shy, po, block, grid, order, resort):
+def test_redeal_gives_the_oracle_bits(shy, po, block, grid, order, resort, settle):
     """Live drops re-sorted by their cell and dealt to the CTAs again every
     `resort` steps (slots in global memory), after spawn in drop or
-    spawn-cell order, with one or several slots per thread: the oracle's
-    bits, on one terrain and on a batch of three (the sort key crosses
-    terrain boundaries)."""
+    spawn-cell order, with one or several slots per thread, each drop
+    settling its own change or the first drop in a cell the cell's: the
+    oracle's bits, on one terrain and on a batch of three (the sort key
+    crosses terrain boundaries)."""
     nx, ny, drops = 96, 80, 3000
     H = po.value_noise(nx, ny, 21)
     m = po.Maps(nx, ny, height=H)
@@ -284,8 +286,9 @@ def test_redeal_gives_the_oracle_bits(shy, po, block, grid, order, resort):
     w.set_launch(grid, order)
     w.set_block(block, 0)
     w.set_resort(resort)
+    w.set_settle(settle)
     w.erode(drops, 2)
-    compare_all(w.get_field, m, po, f"re-deal every {resort}")
+    compare_all(w.get_field, m, po, f"re-deal every {resort}, settle {settle}")
     assert w.stats().drop_steps == acc.steps
     w.close()
 
@@ -298,6 +301,7 @@ def test_redeal_gives_the_oracle_bits(shy, po, block, grid, order, resort):
     b.set_launch(grid, order)
     b.set_block(block, 0)
     b.set_resort(resort)
+    b.set_settle(settle)
     b.erode(2)
     for t, ((x, y), h) in enumerate(zip(sizes, hs)):
         mt = po.Maps(x, y, height=h)
@@ -318,6 +322,7 @@ def test_redeal_in_cuda_graphs_gives_the_oracle_bits(shy, po):
     w.set_block(256, 0)
     w.set_graph(2)
     w.set_resort(4)
+    w.set_settle(1)
     w.erode(2000, 2)
     w.set_resort(0)
     w.erode(2000, 2)

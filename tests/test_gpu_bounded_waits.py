@@ -48,6 +48,7 @@ def test_batched_barrier_times_out_then_world_recovers(shy, po, stall, redeal):
         w.set_launch(0, 1)
         w.set_block(256, 0)
         w.set_resort(1)
+        w.set_settle(1)
     w.set_field("height", H)
     with pytest.raises(shy.ShyError) as ei:
         w.erode(drops, 1)
