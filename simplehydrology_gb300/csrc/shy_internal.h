@@ -154,7 +154,7 @@ struct shy_world {
   // drop slots (struct of arrays)
   float2* dpos = nullptr;
   float2* dspd = nullptr;
-  float2* dvs = nullptr;      // {volume, sediment}
+  float* dsed = nullptr;      // sediment (a drop's volume is the volume table's entry for its age)
   int* dage = nullptr;        // -1: not descending
   long long* down = nullptr;  // the drop's own height change this step, 32.32
   int* dterr = nullptr;       // terrain of the slot
@@ -171,7 +171,7 @@ struct shy_world {
   // drops between the two sets), and its bucket counts (kResortBuckets)
   float2* dpos2 = nullptr;
   float2* dspd2 = nullptr;
-  float2* dvs2 = nullptr;
+  float* dsed2 = nullptr;
   int* dage2 = nullptr;
   int* dterr2 = nullptr;
   int* dresort = nullptr;
@@ -229,7 +229,8 @@ struct CycleBuffers {
   const float* voltab;
   Tracks* trk;
   float* track_f;
-  float2 *pos, *spd, *vs;
+  float2 *pos, *spd;
+  float* sed;
   int* age;
   long long* own;
   int* terr;

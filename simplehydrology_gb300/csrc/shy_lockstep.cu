@@ -78,7 +78,7 @@ const int kSmemTerrains = 128;
 // the slots' own loads already miss L2.
 const int kFirstAtCell = 1 << 30;
 // shared-memory bytes per drop slot: its state plus one steep-queue entry
-const int kSlotBytes = 3 * 8 + 8 + 4 * 4 + (int)sizeof(SteepCell);
+const int kSlotBytes = 2 * 8 + 8 + 5 * 4 + (int)sizeof(SteepCell);
 // A grid barrier gives up (and flags SHY_ERR_TIMEOUT) after this long.
 const unsigned long long kBarrierLimitNs = 2000000000ull;
 
@@ -258,7 +258,7 @@ struct LockArgs {
   // in shared memory)
   float2* pos;
   float2* spd;
-  float2* vs;
+  float* sed;  // sediment (the volume is voltab[age])
   int* age;
   long long* own;   // the drop's own height change this step, 32.32
   int* terr;
@@ -272,7 +272,7 @@ struct LockArgs {
   // moves the live drops from one set to the other)
   float2* pos2;
   float2* spd2;
-  float2* vs2;
+  float* sed2;
   int* age2;
   int* terr2;
   int* rhist;    // re-deal: live drops per bucket of cells, then offsets; zero between re-deals
@@ -293,7 +293,7 @@ struct LockArgs {
 struct Slots {
   float2* pos;
   float2* spd;
-  float2* vs;  // {volume, sediment}
+  float* sed;  // sediment; a drop's volume is voltab[age] (it depends on nothing else)
   long long* own;
   int* cell;  // cell of this step's exchange within the slot's terrain, -1 if none
   int* ctr;   // cascade centre this slot runs this step, within its terrain, -1 if none
@@ -309,7 +309,7 @@ __device__ __forceinline__ Slots slots_global(const LockArgs& a, int buf, long l
   S.steep = a.steep + lo;
   S.pos = (buf ? a.pos2 : a.pos) + lo;
   S.spd = (buf ? a.spd2 : a.spd) + lo;
-  S.vs = (buf ? a.vs2 : a.vs) + lo;
+  S.sed = (buf ? a.sed2 : a.sed) + lo;
   S.own = a.own + lo;
   S.cell = a.cell + lo;
   S.ctr = a.ctr + lo;
@@ -326,11 +326,11 @@ __device__ __forceinline__ Slots slots_of(const LockArgs& a, unsigned char* smem
     S.steep = reinterpret_cast<SteepCell*>(p); p += sizeof(SteepCell) * cap;
     S.pos = reinterpret_cast<float2*>(p); p += 8 * cap;
     S.spd = reinterpret_cast<float2*>(p); p += 8 * cap;
-    S.vs = reinterpret_cast<float2*>(p); p += 8 * cap;
     S.own = reinterpret_cast<long long*>(p); p += 8 * cap;
     S.cell = reinterpret_cast<int*>(p); p += 4 * cap;
     S.ctr = reinterpret_cast<int*>(p); p += 4 * cap;
     S.age = reinterpret_cast<int*>(p); p += 4 * cap;
+    S.sed = reinterpret_cast<float*>(p); p += 4 * cap;
     S.terr = reinterpret_cast<int*>(p);
   } else {
     S = slots_global(a, 0, lo);
@@ -626,17 +626,19 @@ __device__ __noinline__ Redealt redeal(const LockArgs& a, const Terrain* TT, lon
   const long long R = order_run(live, gridDim.x);
   const Slots D = slots_global(a, buf ^ 1, 0);
   int ag_n = -1, ti_n = 0;
-  float2 p_n = make_float2(0.0f, 0.0f), s_n = p_n, v_n = p_n;
+  float2 p_n = make_float2(0.0f, 0.0f), s_n = p_n;
+  float e_n = 0.0f;
   if ((int)threadIdx.x < nd) {
     const int j = threadIdx.x;
-    ag_n = S.age[j]; ti_n = S.terr[j]; p_n = S.pos[j]; s_n = S.spd[j]; v_n = S.vs[j];
+    ag_n = S.age[j]; ti_n = S.terr[j]; p_n = S.pos[j]; s_n = S.spd[j]; e_n = S.sed[j];
   }
   for (int j = threadIdx.x; j < nd; j += kBlock) {
     const int ag = ag_n, ti = ti_n;
-    const float2 p = p_n, sp = s_n, vs = v_n;
+    const float2 p = p_n, sp = s_n;
+    const float se = e_n;
     if (j + kBlock < nd) {
       const int jn = j + kBlock;
-      ag_n = S.age[jn]; ti_n = S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; v_n = S.vs[jn];
+      ag_n = S.age[jn]; ti_n = S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; e_n = S.sed[jn];
     }
     if (ag < 0) continue;
     const long long k = atomicAdd(&a.rhist[drop_cell(TT[ti], p) >> a.rshift], 1);
@@ -648,7 +650,7 @@ __device__ __noinline__ Redealt redeal(const LockArgs& a, const Terrain* TT, lon
     const long long d = slot_range(live, gridDim.x, kr % gridDim.x, true).lo + (kr / gridDim.x) * R + k % R;
     D.pos[d] = p;
     D.spd[d] = sp;
-    D.vs[d] = vs;
+    D.sed[d] = se;
     D.age[d] = ag;
     D.terr[d] = ti;
   }
@@ -752,7 +754,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     ++born;
     S.pos[j] = make_float2((float)x, (float)y);
     S.spd[j] = make_float2(0.0f, 0.0f);
-    S.vs[j] = make_float2(1.0f, 0.0f);
+    S.sed[j] = 0.0f;
     if (kLean) {
       S.age[j] = atomicAdd(&a.cq[c].cnt[0], 1) == 0 ? kFirstAtCell : 0;
     } else {
@@ -782,21 +784,25 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
     // the reverse on odd steps.  Slot order changes no result.
     const bool rev_d = redeals && (step & 1);
     int ag_n = 0, ti_n = 0;
-    float2 p_n = make_float2(0.0f, 0.0f), s_n = p_n, v_n = p_n;
+    float2 p_n = make_float2(0.0f, 0.0f), s_n = p_n;
+    float e_n = 0.0f;
     if ((int)threadIdx.x < nd) {
       const int j = rev_d ? nd - 1 - (int)threadIdx.x : (int)threadIdx.x;
-      ag_n = S.age[j]; ti_n = one_terrain ? 0 : S.terr[j]; p_n = S.pos[j]; s_n = S.spd[j]; v_n = S.vs[j];
+      ag_n = S.age[j]; ti_n = one_terrain ? 0 : S.terr[j]; p_n = S.pos[j]; s_n = S.spd[j]; e_n = S.sed[j];
     }
     for (int i = threadIdx.x; i < nd; i += blockDim.x) {
       const int j = rev_d ? nd - 1 - i : i;
       const int agr = ag_n, ti = ti_n;
-      float2 p = p_n, s = s_n, v = v_n;
+      float2 p = p_n, s = s_n;
+      const float se = e_n;
       if (i + (int)blockDim.x < nd) {
         const int jn = rev_d ? nd - 1 - (i + (int)blockDim.x) : i + (int)blockDim.x;
-        ag_n = S.age[jn]; ti_n = one_terrain ? 0 : S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; v_n = S.vs[jn];
+        ag_n = S.age[jn]; ti_n = one_terrain ? 0 : S.terr[jn]; p_n = S.pos[jn]; s_n = S.spd[jn]; e_n = S.sed[jn];
       }
       if (agr < 0) continue;
       const int ag = kLean ? (agr & (kFirstAtCell - 1)) : agr;
+      // {volume, sediment}: the volume after `ag` evaporations (water.h:136)
+      float2 v = make_float2(__ldg(&a.voltab[ag < vmax ? ag : vmax]), se);
       const Terrain T = TT[ti];
       const CellQ* RT = a.cq + T.cell_base;
       const int ix = (int)p.x, iy = (int)p.y;
@@ -896,7 +902,7 @@ __global__ void __maxnreg__(128) lockstep_kernel(LockArgs a) {
       S.age[j] = (ag + 1) | (kLean && arrived_before == 0 ? kFirstAtCell : 0);
       S.pos[j] = p;
       S.spd[j] = s;
-      S.vs[j] = v;
+      S.sed[j] = v.y;
     }
     lap(0);
     if (!grid_barrier(a.bar, passed, nullptr)) { ok = false; break; }
@@ -1412,7 +1418,7 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.trk = w->trk;
   a.pos = w->dpos;
   a.spd = w->dspd;
-  a.vs = w->dvs;
+  a.sed = w->dsed;
   a.age = w->dage;
   a.own = w->down;
   a.terr = w->dterr;
@@ -1431,7 +1437,7 @@ cudaError_t launch_batched_cycle(shy_world* w) {
   a.order = ordered ? w->dorder : nullptr;
   a.pos2 = w->dpos2;
   a.spd2 = w->dspd2;
-  a.vs2 = w->dvs2;
+  a.sed2 = w->dsed2;
   a.age2 = w->dage2;
   a.terr2 = w->dterr2;
   a.rhist = w->dresort;
@@ -1498,7 +1504,7 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.trk = b.trk;
   a.pos = b.pos;
   a.spd = b.spd;
-  a.vs = b.vs;
+  a.sed = b.sed;
   a.age = b.age;
   a.own = b.own;
   a.terr = b.terr;
@@ -1508,7 +1514,8 @@ cudaError_t launch_cycle_buffers(const CycleBuffers& b, cudaStream_t stream) {
   a.arr = b.arr;
   a.arr_words = b.arr_words;
   a.order = nullptr;
-  a.pos2 = a.spd2 = a.vs2 = nullptr;
+  a.pos2 = a.spd2 = nullptr;
+  a.sed2 = nullptr;
   a.age2 = a.terr2 = a.rhist = nullptr;
   a.rshift = 0;
   a.rbuckets = 0;

@@ -27,7 +27,8 @@ struct NoallocScratch {
   // arrivals bitmaps, two step parities of ceil(nx / 8) * ceil(ny / 8)
   // <= cells / 64 + (nx + ny) / 8 + 1 words each
   unsigned long long arr[2 * (SHY_NOALLOC_MAX_CELLS / 64 + (SHY_NOALLOC_MAX_CELLS + 1) / 8 + 2)];
-  float2 pos[SHY_NOALLOC_MAX_DROPS], spd[SHY_NOALLOC_MAX_DROPS], vs[SHY_NOALLOC_MAX_DROPS];
+  float2 pos[SHY_NOALLOC_MAX_DROPS], spd[SHY_NOALLOC_MAX_DROPS];
+  float sed[SHY_NOALLOC_MAX_DROPS];
   long long own[SHY_NOALLOC_MAX_DROPS];
   int cell[SHY_NOALLOC_MAX_DROPS], ctr[SHY_NOALLOC_MAX_DROPS];
   int age[SHY_NOALLOC_MAX_DROPS], terr[SHY_NOALLOC_MAX_DROPS];
@@ -210,7 +211,7 @@ extern "C" int shy_erode_noalloc(int nx, int ny, const shy_params* params, uint6
   b.track_f = sc->track_f;
   b.pos = sc->pos;
   b.spd = sc->spd;
-  b.vs = sc->vs;
+  b.sed = sc->sed;
   b.age = sc->age;
   b.own = sc->own;
   b.terr = sc->terr;

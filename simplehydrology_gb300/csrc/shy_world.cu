@@ -96,11 +96,11 @@ void free_world(shy_world* w) {
   if (!w) return;
   if (w->stream) cudaStreamSynchronize(w->stream);
   if (w->gexec) cudaGraphExecDestroy(w->gexec);
-  void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dvs, w->dage,
+  void* ptrs[] = {w->h, w->root, w->plant, w->track_f, w->rec, w->effd, w->trk, w->cq, w->scratch, w->relax, w->dpos, w->dspd, w->dsed, w->dage,
                   w->dterr, w->dcell, w->dctr, w->dterrains, w->stats, w->bar, w->ddrop,
                   w->dtrace, w->dint, w->dspawn, w->normals, w->hq_relax, w->voltab, w->down,
                   w->plant_next, w->rootq, w->veg_claim, w->arr, w->feed, w->crand, w->plants, w->stage, w->dorder, w->dkey, w->drank, w->dhist,
-                  w->dsteep, w->dpos2, w->dspd2, w->dvs2, w->dage2, w->dterr2, w->dresort};
+                  w->dsteep, w->dpos2, w->dspd2, w->dsed2, w->dage2, w->dterr2, w->dresort};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& p : w->timing.pending) {
@@ -114,23 +114,25 @@ void free_world(shy_world* w) {
 
 int alloc_drop_slots(shy_world* w, int n) {
   if (n <= w->max_drops) return SHY_OK;
-  void* ptrs[] = {w->dpos, w->dspd, w->dvs, w->dage, w->dterr, w->dcell, w->dctr, w->down,
-                  w->dsteep, w->dorder, w->dkey, w->drank, w->dpos2, w->dspd2, w->dvs2, w->dage2, w->dterr2};
+  void* ptrs[] = {w->dpos, w->dspd, w->dsed, w->dage, w->dterr, w->dcell, w->dctr, w->down,
+                  w->dsteep, w->dorder, w->dkey, w->drank, w->dpos2, w->dspd2, w->dsed2, w->dage2, w->dterr2};
   SHY_CHECK_CUDA(cudaStreamSynchronize(w->stream), "synchronize");
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  w->dpos = w->dspd = w->dvs = nullptr;
+  w->dpos = w->dspd = nullptr;
+  w->dsed = nullptr;
   w->dage = w->dterr = nullptr;
   w->down = nullptr;
   w->dsteep = nullptr;
   w->dorder = w->dkey = w->drank = nullptr;
   w->dcell = w->dctr = nullptr;
-  w->dpos2 = w->dspd2 = w->dvs2 = nullptr;
+  w->dpos2 = w->dspd2 = nullptr;
+  w->dsed2 = nullptr;
   w->dage2 = w->dterr2 = nullptr;
   w->max_drops = 0;
   SHY_CHECK_CUDA(dalloc(&w->dpos, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dspd, n), "allocate drop slots");
-  SHY_CHECK_CUDA(dalloc(&w->dvs, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->dsed, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dage, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dterr, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dcell, n), "allocate drop slots");
@@ -142,7 +144,7 @@ int alloc_drop_slots(shy_world* w, int n) {
   SHY_CHECK_CUDA(dalloc(&w->drank, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dpos2, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dspd2, n), "allocate drop slots");
-  SHY_CHECK_CUDA(dalloc(&w->dvs2, n), "allocate drop slots");
+  SHY_CHECK_CUDA(dalloc(&w->dsed2, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dage2, n), "allocate drop slots");
   SHY_CHECK_CUDA(dalloc(&w->dterr2, n), "allocate drop slots");
   if (!w->dhist) SHY_CHECK_CUDA(dalloc(&w->dhist, 65536), "allocate drop slots");
@@ -947,10 +949,10 @@ unsigned long long launch_key(const shy_world* w) {
   const int shape[8] = {w->batch_grid, w->batch_order, w->batch_block, w->batch_smem, w->graph_cycles, w->sm_count,
                         w->batch_resort, w->batch_settle};
   mix(shape, sizeof(shape));
-  const void* ptrs[] = {w->h, w->cq, w->rec, w->voltab, w->trk, w->track_f, w->dpos, w->dspd, w->dvs, w->dage,
+  const void* ptrs[] = {w->h, w->cq, w->rec, w->voltab, w->trk, w->track_f, w->dpos, w->dspd, w->dsed, w->dage,
                         w->down, w->dterr, w->dcell, w->dctr, w->dsteep, w->arr, w->dorder, w->dkey,
                         w->drank, w->dhist, w->dterrains, w->stats, w->bar, w->relax, w->hq_relax,
-                        w->dpos2, w->dspd2, w->dvs2, w->dage2, w->dterr2, w->dresort};
+                        w->dpos2, w->dspd2, w->dsed2, w->dage2, w->dterr2, w->dresort};
   mix(ptrs, sizeof(ptrs));
   return h;
 }
